@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Marching-cubes throughput on one GB300: cells/s and HBM roofline fraction.
+
+Workload (one "step"): the full marching-cubes forward pipeline with duplicate
+point merging -- classify, count + scan, generate -- on a 512^3 float32 field
+(sum of 8 seeded isotropic Gaussian blobs on the unit cube, isovalue 0.5),
+field resident in HBM.  The field (537 MB) is larger than L2 (129 MB), so no
+flush is needed between steps.
+
+Reported:
+  value        cells/s over all ranks, device-timed (CUDA events, field in HBM)
+  e2e          the same metric through the public API from pinned host memory:
+               H2D field copy + marching_cubes() (count, host sizing, generate)
+               + D2H of vertices and connectivity, every step
+  roofline     dominant kernel (K1 point classification): algorithmic bytes
+               4P read + P/8 written per launch over its CUDA-event time
+  cpu_baseline the CPU implementation on a bounded z-slab sample of the same
+               field (see "sample")
+With --impl reference the reference's CPU implementation (the DaxToolkit
+worklets compiled from source, OpenMP over all host threads; the C oracle
+port where that library is absent) is timed on the same workload instead.
+
+Multi-GPU (torchrun): every rank processes its own 512^3 grid (independent
+grids, no collective on the data path): weak scaling, value = all ranks'
+cells / max over ranks of the timed region.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC cells/s & HBM roofline % at 512^3 fp32"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--size", type=int, default=512)
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="target CPU time of the bounded CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dram_traffic(kernel, workload):
+    """Per-launch DRAM bytes (read + write) recorded from an ncu capture."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and parts[1] == workload:
+            return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(field_host, dims, spacing, iso, target_s, kind_pref="reference", threads=None):
+    """Times count + merged generate of the CPU implementation on the first kz
+    z-planes of the field, kz chosen so the run takes about target_s."""
+    import numpy as np
+    import oracle
+    O = None
+    if kind_pref == "reference":
+        try:
+            O = oracle.Oracle("reference")
+        except Exception:
+            O = None
+    if O is None:
+        O = oracle.Oracle("port")
+    cores = O.set_threads(threads or O.max_threads()) if O.kind == "reference" else 1
+    nx, ny, nz = dims
+    f3 = field_host.reshape(nz, ny, nx)
+
+    def run(kz):
+        sub = np.ascontiguousarray(f3[:kz]).ravel()
+        g = oracle.make_grid((nx, ny, kz), spacing=spacing)
+        t0 = time.perf_counter()
+        count, _ = O.mc_count(g, sub, iso)
+        O.mc_generate(g, sub, iso, count, merge=True)
+        return time.perf_counter() - t0, (nx - 1) * (ny - 1) * (kz - 1)
+
+    t, c = run(min(nz, 9))
+    per_cell = t / c
+    kz = int(min(nz, max(9, target_s / per_cell / ((nx - 1) * (ny - 1)) + 1)))
+    t, c = run(kz)
+    return {"value": c / t, "unit": "cells/s", "cores": cores,
+            "kind": "reference" if O.kind == "reference" else "port",
+            "sample": "first %d of %d z-planes of the same field (%dx%dx%d points), "
+                      "count + merged generate" % (kz, nz, nx, ny, kz),
+            "seconds": t}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU implementation on the host cores; rank 0 only."""
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from daxtoolkit_gb300 import synthetic
+    n = args.size
+    dims = (n, n, n)
+    spacing = (1.0 / (n - 1),) * 3
+    field = synthetic.blob_field(dims, 8, seed=20260101, device="cpu").numpy()
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(field, dims, spacing, 0.5, min(per_step, 2.0))
+    vals = [cpu_baseline(field, dims, spacing, 0.5, per_step) for _ in range(args.steps)]
+    v = statistics.median([x["value"] for x in vals])
+    C = (n - 1) ** 3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * C / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config_dict(n),
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": vals[0]["cores"],
+                         "kind": vals[0]["kind"], "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(n):
+    return {"workload": "marching cubes forward, %d^3 points float32, 8 gaussian blobs "
+                        "(seed 20260101), isovalue 0.5, duplicate-point merge on" % n,
+            "grid_points": [n, n, n], "isovalue": 0.5, "merge": True,
+            "l2_policy": "inputs larger than L2 (field %d MB > 129 MB), no flush" %
+                         (4 * n ** 3 // 2 ** 20)}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    from daxtoolkit_gb300 import build as gbuild
+    gbuild.build()
+    from daxtoolkit_gb300 import capi, cont, synthetic
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.size
+    dims = (n, n, n)
+    spacing = (1.0 / (n - 1),) * 3
+    iso = 0.5
+    P, C = n ** 3, (n - 1) ** 3
+    field = synthetic.blob_field(dims, 8, seed=20260101, device=dev)
+    grid = cont.UniformGrid(dims, spacing=spacing)
+    g = grid.desc()
+    L = capi.lib()
+    stream = torch.cuda.current_stream()
+    s = ctypes.c_void_p(stream.cuda_stream)
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    nbytes = L.dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+    # size outputs once (the count is deterministic for a fixed field)
+    capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
+    T, V = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(T), ctypes.byref(V), s)
+    T, V = T.value, V.value
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+
+    def step():
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
+        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(field), iso, 1, ptr(scratch), nbytes,
+                  ptr(verts), V, ptr(conn), T, None, None, None, s)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    t_ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    # device totals/errors after the timed region
+    T2, V2 = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(T2), ctypes.byref(V2), s)
+    assert (T2.value, V2.value) == (T, V)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    ms_per_step = t_ms / args.steps
+    value = world * C * args.steps / (t_ms / 1e3)
+
+    # --- per-stage timing: K1 alone, count pass, generate pass -------------
+    bits = torch.empty(L.dax_gb300_classify_words(P), dtype=torch.int32, device=dev)
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    reps = max(5, args.steps)
+    k1 = lambda: capi.call("dax_gb300_classify_points", ptr(field), P, 0, iso, 0.0, ptr(bits), s)
+    k1()
+    t_k1 = timed(k1, reps)
+    t_count = timed(lambda: capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso,
+                                      ptr(scratch), nbytes, s), reps)
+    t_gen = timed(lambda: capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(field), iso, 1,
+                                    ptr(scratch), nbytes, ptr(verts), V, ptr(conn), T, None, None,
+                                    None, s), reps)
+
+    peak, peak_kind = measured_peaks()
+    k1_bytes = 4 * P + P / 8
+    achieved = k1_bytes / (t_k1 / 1e3) / 1e9
+    traffic = dram_traffic("k_classify_bits", "%dcube" % n)
+    alg_bytes = 4 * P + 12 * V + 12 * T
+    pipe_gbs = alg_bytes / (ms_per_step / 1e3) / 1e9
+
+    # --- end to end through the public API, host buffers ------------------
+    host_field = torch.empty(P, dtype=torch.float32, pin_memory=True)
+    host_field.copy_(field.cpu())
+    dev_field = torch.empty_like(field)
+    host_v = torch.empty((V, 3), dtype=torch.float32, pin_memory=True)
+    host_c = torch.empty((T, 3), dtype=torch.int32, pin_memory=True)
+
+    def e2e_step():
+        dev_field.copy_(host_field, non_blocking=True)
+        out = cont.marching_cubes(grid, dev_field, iso, merge=True)
+        host_v.copy_(out["verts"], non_blocking=True)
+        host_c.copy_(out["conn"], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    e2e_value = world * C / t_e2e
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config_dict(n),
+        "triangles": T, "merged_vertices": V,
+        "triangles_per_s": world * T / (ms_per_step / 1e3),
+        "roofline": {"bound": "hbm", "kernel": "k_classify_bits", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": k1_bytes, "ms_per_launch": t_k1},
+        "pipeline_roofline": {"achieved": pipe_gbs, "peak": peak, "unit": "GB/s",
+                              "frac": pipe_gbs / peak, "algorithmic_bytes": alg_bytes,
+                              "formula": "4P + 12V + 12T"},
+        "stages_ms": {"classify": t_k1, "count_scan_incl_classify": t_count,
+                      "generate": t_gen},
+        "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 4 * P,
+                "d2h_bytes_per_step": 12 * V + 12 * T, "ms_per_step": 1e3 * t_e2e},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        fh = field.cpu().numpy()
+        cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,341 @@
+"""Control-environment surface of the GB300 device adapter, in Python.
+
+Mirrors the part of ``dax::cont`` that the uniform-grid hot path uses --
+``UniformGrid`` (dax/cont/UniformGrid.h:114-252), ``DispatcherMapCell``
+(dax/cont/DispatcherMapCell.h:27-64), ``DispatcherGenerateInterpolatedCells``
+(dax/cont/DispatcherGenerateInterpolatedCells.h:34-301) and
+``DispatcherGenerateTopology`` (dax/cont/DispatcherGenerateTopology.h:30-258)
+-- with the same names, argument meaning and error types, over the C ABI in
+``include/dax_gb300.h``.  Arrays are torch CUDA tensors (the ArrayHandle's
+execution-side storage); torch supplies device memory and the current stream,
+all arithmetic runs in libdax_gb300.so.
+"""
+import ctypes
+
+import torch
+
+from . import capi
+
+__all__ = [
+    "UniformGrid", "UnstructuredGrid", "MarchingCubesCount", "MarchingCubesGenerate",
+    "ThresholdCount", "ThresholdTopology", "CellGradient", "DispatcherMapCell",
+    "DispatcherGenerateInterpolatedCells", "DispatcherGenerateTopology", "marching_cubes",
+    "threshold", "cell_gradient", "Scratch",
+]
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _require_field(field, grid):
+    if not isinstance(field, torch.Tensor) or not field.is_cuda:
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "field must be a CUDA tensor")
+    if field.dtype != torch.float32 or not field.is_contiguous():
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "field must be contiguous float32")
+    if field.numel() != grid.GetNumberOfPoints():
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "field has %d values, grid has %d points"
+                                        % (field.numel(), grid.GetNumberOfPoints()))
+
+
+class UniformGrid:
+    """Axis-aligned grid with implicit coordinates origin + spacing*(ijk+min)."""
+
+    def __init__(self, dims=None, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0),
+                 extent_min=(0, 0, 0)):
+        self.Origin = tuple(float(v) for v in origin)
+        self.Spacing = tuple(float(v) for v in spacing)
+        self.ExtentMin = tuple(int(v) for v in extent_min)
+        dims = dims or (1, 1, 1)
+        self.ExtentMax = tuple(self.ExtentMin[a] + int(dims[a]) - 1 for a in range(3))
+
+    def SetExtent(self, emin, emax):
+        self.ExtentMin, self.ExtentMax = tuple(map(int, emin)), tuple(map(int, emax))
+
+    def SetOrigin(self, o):
+        self.Origin = tuple(map(float, o))
+
+    def SetSpacing(self, s):
+        self.Spacing = tuple(map(float, s))
+
+    @property
+    def dims(self):
+        return tuple(self.ExtentMax[a] - self.ExtentMin[a] + 1 for a in range(3))
+
+    def GetNumberOfPoints(self):
+        d = self.dims
+        return d[0] * d[1] * d[2]
+
+    def GetNumberOfCells(self):
+        d = self.dims
+        if min(d) < 2:
+            return 0
+        return (d[0] - 1) * (d[1] - 1) * (d[2] - 1)
+
+    def desc(self):
+        g = capi.UniformGridDesc()
+        for a in range(3):
+            g.origin[a] = self.Origin[a]
+            g.spacing[a] = self.Spacing[a]
+            g.extent_min[a] = self.ExtentMin[a]
+            g.extent_max[a] = self.ExtentMax[a]
+        return g
+
+
+class UnstructuredGrid:
+    """Output grid: explicit points [N,3] and connectivity [cells, verts]."""
+
+    def __init__(self, points, connectivity):
+        self.points = points
+        self.connectivity = connectivity
+
+    def GetPointCoordinates(self):
+        return self.points
+
+    def GetCellConnections(self):
+        return self.connectivity
+
+    def GetNumberOfPoints(self):
+        return int(self.points.shape[0])
+
+    def GetNumberOfCells(self):
+        return int(self.connectivity.shape[0])
+
+
+class Scratch:
+    """Device scratch for the count/generate passes, grown on demand.
+
+    Allocation happens only when a larger grid is seen, so steady-state
+    pipelines allocate nothing.
+    """
+
+    def __init__(self, device=None):
+        self.device = device
+        self.buf = None
+
+    def get(self, nbytes):
+        if self.buf is None or self.buf.numel() < nbytes:
+            dev = self.device or torch.device("cuda", torch.cuda.current_device())
+            self.buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+        return self.buf
+
+
+_default_scratch = {}
+
+
+def _scratch_for(kind):
+    dev = torch.cuda.current_device()
+    key = (kind, dev)
+    if key not in _default_scratch:
+        _default_scratch[key] = Scratch()
+    return _default_scratch[key]
+
+
+# ---- worklets (descriptors; the arithmetic lives in the CUDA kernels) ----
+class MarchingCubesCount:
+    """dax/worklet/MarchingCubes.h:53-86."""
+
+    def __init__(self, isovalue):
+        self.IsoValue = float(isovalue)
+
+
+class MarchingCubesGenerate:
+    """dax/worklet/MarchingCubes.h:90-169."""
+
+    def __init__(self, isovalue):
+        self.IsoValue = float(isovalue)
+
+
+class ThresholdCount:
+    """dax/worklet/Threshold.h:69-96."""
+
+    def __init__(self, thresholdMin, thresholdMax):
+        self.ThresholdMin = float(thresholdMin)
+        self.ThresholdMax = float(thresholdMax)
+
+
+class ThresholdTopology:
+    """dax/worklet/Threshold.h:98-111."""
+
+
+class CellGradient:
+    """dax/worklet/CellGradient.h:28-48."""
+
+
+# ---- fused pipelines ------------------------------------------------------
+def marching_cubes(grid, field, isovalue, merge=True, records=False, scratch=None, stream=None):
+    """Count, size the outputs on the host, generate.  Returns a dict with
+    ``verts`` [V,3] f32, ``conn`` [T,3] i32 and, if ``records``, the
+    PointAsEdgeInterpolation arrays ``rec_first``, ``rec_second``, ``rec_weight``."""
+    _require_field(field, grid)
+    g = grid.desc()
+    s = _stream(stream)
+    nbytes = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    buf = (scratch or _scratch_for("mc")).get(nbytes)
+    capi.call("dax_gb300_mc_count", ctypes.byref(g), _ptr(field), float(isovalue), _ptr(buf),
+              buf.numel(), s)
+    T, Vm = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", _ptr(buf), ctypes.byref(T), ctypes.byref(Vm), s)
+    T = T.value
+    V = Vm.value if merge else 3 * T
+    dev = field.device
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+    ra = rb = rw = None
+    if records:
+        ra = torch.empty(V, dtype=torch.int32, device=dev)
+        rb = torch.empty(V, dtype=torch.int32, device=dev)
+        rw = torch.empty(V, dtype=torch.float32, device=dev)
+    capi.call("dax_gb300_mc_generate", ctypes.byref(g), _ptr(field), float(isovalue),
+              int(bool(merge)), _ptr(buf), buf.numel(), _ptr(verts), V, _ptr(conn), T, _ptr(ra),
+              _ptr(rb), _ptr(rw), s)
+    out = dict(verts=verts, conn=conn)
+    if records:
+        out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
+    return out
+
+
+def interpolate_point_field(rec_first, rec_second, rec_weight, field, stream=None):
+    out = torch.empty(rec_first.numel(), dtype=torch.float32, device=field.device)
+    capi.call("dax_gb300_interpolate_point_field", _ptr(rec_first), _ptr(rec_second),
+              _ptr(rec_weight), rec_first.numel(), _ptr(field), _ptr(out), _stream(stream))
+    return out
+
+
+def threshold(grid, field, lo, hi, compact_field=True, scratch=None, stream=None):
+    """Returns dict(conn [K,8] i32, coords [U,3] f32, field [U] f32 or None)."""
+    _require_field(field, grid)
+    g = grid.desc()
+    s = _stream(stream)
+    nbytes = capi.lib().dax_gb300_threshold_scratch_bytes(ctypes.byref(g))
+    buf = (scratch or _scratch_for("threshold")).get(nbytes)
+    capi.call("dax_gb300_threshold_count", ctypes.byref(g), _ptr(field), float(lo), float(hi),
+              _ptr(buf), buf.numel(), s)
+    K, U = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_threshold_totals", _ptr(buf), ctypes.byref(K), ctypes.byref(U), s)
+    K, U = K.value, U.value
+    dev = field.device
+    conn = torch.empty((K, 8), dtype=torch.int32, device=dev)
+    coords = torch.empty((U, 3), dtype=torch.float32, device=dev)
+    fout = torch.empty(U, dtype=torch.float32, device=dev) if compact_field else None
+    capi.call("dax_gb300_threshold_generate", ctypes.byref(g), _ptr(field), float(lo), float(hi),
+              _ptr(buf), buf.numel(), _ptr(conn), K, _ptr(coords), _ptr(fout), U, s)
+    return dict(conn=conn, coords=coords, field=fout)
+
+
+def cell_gradient(grid, field, out=None, stream=None):
+    _require_field(field, grid)
+    g = grid.desc()
+    if out is None:
+        out = torch.empty((grid.GetNumberOfCells(), 3), dtype=torch.float32, device=field.device)
+    capi.call("dax_gb300_cell_gradient", ctypes.byref(g), _ptr(field), _ptr(out), _stream(stream))
+    return out
+
+
+# ---- dispatchers ----------------------------------------------------------
+class DispatcherMapCell:
+    """DispatcherMapCell<Worklet>: one output value per cell, cell-id order."""
+
+    def __init__(self, worklet):
+        self.worklet = worklet
+
+    def Invoke(self, grid, field, stream=None):
+        _require_field(field, grid)
+        w = self.worklet
+        g = grid.desc()
+        C = grid.GetNumberOfCells()
+        if isinstance(w, MarchingCubesCount):
+            count = torch.empty(C, dtype=torch.int32, device=field.device)
+            capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field), w.IsoValue,
+                      _ptr(count), None, _stream(stream))
+            return count
+        if isinstance(w, ThresholdCount):
+            count = torch.empty(C, dtype=torch.int32, device=field.device)
+            capi.call("dax_gb300_threshold_classify_count", ctypes.byref(g), _ptr(field),
+                      w.ThresholdMin, w.ThresholdMax, _ptr(count), _stream(stream))
+            return count
+        if isinstance(w, CellGradient):
+            return cell_gradient(grid, field, stream=stream)
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "worklet %r has no GB300 kernel" % type(w).__name__)
+
+    def classify_cases(self, grid, field, stream=None):
+        """MarchingCubesCount with the per-cell case index as a second output."""
+        g = grid.desc()
+        C = grid.GetNumberOfCells()
+        count = torch.empty(C, dtype=torch.int32, device=field.device)
+        cases = torch.empty(C, dtype=torch.uint8, device=field.device)
+        capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field),
+                  self.worklet.IsoValue, _ptr(count), _ptr(cases), _stream(stream))
+        return count, cases
+
+
+class DispatcherGenerateInterpolatedCells:
+    """DispatcherGenerateInterpolatedCells<MarchingCubesGenerate>.
+
+    The count array is accepted for interface parity; on this device adapter
+    the generate pass recounts from the field (identical by construction for
+    MarchingCubesCount with the same isovalue) so that no per-cell array is
+    written or scanned.
+    """
+
+    def __init__(self, count, worklet):
+        self.count = count
+        self.worklet = worklet
+        self.RemoveDuplicatePoints = True
+        self.ReleaseCount = True
+        self._records = None
+
+    def SetRemoveDuplicatePoints(self, b):
+        self.RemoveDuplicatePoints = bool(b)
+
+    def GetRemoveDuplicatePoints(self):
+        return self.RemoveDuplicatePoints
+
+    def SetReleaseCount(self, b):
+        self.ReleaseCount = bool(b)
+
+    def Invoke(self, grid, field, stream=None):
+        out = marching_cubes(grid, field, self.worklet.IsoValue, merge=self.RemoveDuplicatePoints,
+                             records=True, stream=stream)
+        self._records = (out["rec_first"], out["rec_second"], out["rec_weight"])
+        if self.ReleaseCount:
+            self.count = None
+        return UnstructuredGrid(out["verts"], out["conn"])
+
+    def CompactPointField(self, field, stream=None):
+        if self._records is None:
+            raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "Invoke before CompactPointField")
+        return interpolate_point_field(*self._records, field, stream=stream)
+
+
+class DispatcherGenerateTopology:
+    """DispatcherGenerateTopology<ThresholdTopology> driven by a ThresholdCount."""
+
+    def __init__(self, count, worklet=None, threshold_worklet=None):
+        self.count = count
+        self.worklet = worklet or ThresholdTopology()
+        self.threshold = threshold_worklet
+        self.RemoveDuplicatePoints = True
+        self._field = None
+
+    def SetRemoveDuplicatePoints(self, b):
+        self.RemoveDuplicatePoints = bool(b)
+
+    def Invoke(self, grid, field, stream=None):
+        if self.threshold is None:
+            raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                            "the GB300 path needs the ThresholdCount worklet")
+        out = threshold(grid, field, self.threshold.ThresholdMin, self.threshold.ThresholdMax,
+                        stream=stream)
+        self._field = out["field"]
+        return UnstructuredGrid(out["coords"], out["conn"])
+
+    def CompactPointField(self, field=None):
+        return self._field

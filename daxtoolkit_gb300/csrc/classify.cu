@@ -1,0 +1,133 @@
+// K1: point classification into a bit stream, and the per-cell count kernels
+// behind DispatcherMapCell<MarchingCubesCount | ThresholdCount>.
+//
+// K1 is the only kernel that reads the whole field.  It is a pure stream: each
+// warp step loads 32 x float4 (512 B, fully coalesced, evict-first) and emits
+// four 32-bit words of classification bits, so HBM traffic is 4 B/point read +
+// 1/8 B/point written.  Everything downstream (counts, scans, generation)
+// works on the 16x smaller bit stream, which stays resident in L2.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "mc_case.cuh"
+
+namespace daxgb {
+
+template <int MODE>
+__device__ __forceinline__ uint32_t classify_point(float v, float a, float b) {
+  // MODE 0: marching-cubes inside test, values[i] > iso (dax/worklet/MarchingCubes.h:40-47)
+  // MODE 1: threshold test, min <= value <= max (dax/worklet/Threshold.h:40-43)
+  if (MODE == 0) return v > a ? 1u : 0u;
+  return (v >= a && v <= b) ? 1u : 0u;
+}
+
+// Each warp-chunk covers 128 points = 4 bit words.  UNROLL chunks per warp
+// step keep several 512 B loads in flight per warp.
+template <int MODE, bool VEC>
+__global__ void __launch_bounds__(256) k_classify_bits(const float* __restrict__ f, long long P,
+                                                       float a, float b,
+                                                       uint32_t* __restrict__ bits,
+                                                       long long nwords) {
+  constexpr int UNROLL = 4;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long nchunks = (P + 127) >> 7;
+  for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
+    float4 v[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const long long c = c0 + u;
+      const long long base = (c << 7) + lane * 4;
+      if (VEC && base + 3 < P) {
+        v[u] = __ldcs(reinterpret_cast<const float4*>(f + base));
+      } else {
+        // tail / unaligned path: NaN classifies as 0 in both modes
+        const float nan = __int_as_float(0x7fc00000);
+        v[u].x = (c < nchunks && base + 0 < P) ? __ldcs(f + base + 0) : nan;
+        v[u].y = (c < nchunks && base + 1 < P) ? __ldcs(f + base + 1) : nan;
+        v[u].z = (c < nchunks && base + 2 < P) ? __ldcs(f + base + 2) : nan;
+        v[u].w = (c < nchunks && base + 3 < P) ? __ldcs(f + base + 3) : nan;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const long long c = c0 + u;
+      uint32_t nib = classify_point<MODE>(v[u].x, a, b) | (classify_point<MODE>(v[u].y, a, b) << 1) |
+                     (classify_point<MODE>(v[u].z, a, b) << 2) |
+                     (classify_point<MODE>(v[u].w, a, b) << 3);
+      uint32_t w = nib << (4 * (lane & 7));
+      w |= __shfl_xor_sync(kFull, w, 1);
+      w |= __shfl_xor_sync(kFull, w, 2);
+      w |= __shfl_xor_sync(kFull, w, 4);
+      if ((lane & 7) == 0 && c < nchunks) bits[(c << 2) + (lane >> 3)] = w;
+    }
+  }
+  // zero the padding words after the last chunk (read by unaligned fetches)
+  if (blockIdx.x == 0 && threadIdx.x < 8) {
+    const long long w = (nchunks << 2) + threadIdx.x;
+    if (w < nwords) bits[w] = 0u;
+  }
+}
+
+void launch_classify_bits(int mode, const float* f, long long P, float a, float b, uint32_t* bits,
+                          long long nwords, int num_sms, cudaStream_t s) {
+  const long long nchunks = (P + 127) >> 7;
+  const long long want = (nchunks + 4 * 8 - 1) / (4 * 8);  // blocks of 8 warps x 4 chunks
+  const long long cap = (long long)num_sms * 8;
+  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+  const bool vec = (reinterpret_cast<uintptr_t>(f) & 15) == 0;
+  if (mode == 0) {
+    if (vec) k_classify_bits<0, true><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
+    else k_classify_bits<0, false><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
+  } else {
+    if (vec) k_classify_bits<1, true><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
+    else k_classify_bits<1, false><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
+  }
+}
+
+// ---- per-cell count arrays (the Dax count handles) ---------------------
+// One thread per cell, cells in id order; the 8 corner loads of neighbouring
+// threads overlap and are served by L1/L2.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cell_count(Grid g, const float* __restrict__ f, float a,
+                                                    float b, int32_t* __restrict__ count,
+                                                    uint8_t* __restrict__ cases) {
+  const int cx = g.nx - 1, cy = g.ny - 1;
+  const long long C = (long long)cx * cy * (g.nz - 1);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long row = c / cx;
+    const int i = (int)(c - row * cx);
+    const int j = (int)(row % cy);
+    const int k = (int)(row / cy);
+    const long long p0 = i + (long long)g.nx * (j + (long long)g.ny * k);
+    const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+    const float v[8] = {__ldg(f + p0),          __ldg(f + p0 + 1),          __ldg(f + p0 + dy + 1),
+                        __ldg(f + p0 + dy),     __ldg(f + p0 + dz),         __ldg(f + p0 + dz + 1),
+                        __ldg(f + p0 + dz + dy + 1), __ldg(f + p0 + dz + dy)};
+    if (MODE == 0) {
+      int cs = 0;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) cs |= (v[n] > a) << n;
+      count[c] = (int32_t)mc_num_tris(cs);
+      if (cases) cases[c] = (uint8_t)cs;
+    } else {
+      int valid = 1;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) valid &= (v[n] >= a && v[n] <= b);
+      count[c] = valid;
+    }
+  }
+}
+
+void launch_cell_count(int mode, const Grid& g, const float* f, float a, float b, int32_t* count,
+                       uint8_t* cases, int num_sms, cudaStream_t s) {
+  const long long C = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1);
+  const long long want = (C + 255) / 256;
+  const long long cap = (long long)num_sms * 16;
+  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+  if (mode == 0) k_cell_count<0><<<blocks, 256, 0, s>>>(g, f, a, b, count, cases);
+  else k_cell_count<1><<<blocks, 256, 0, s>>>(g, f, a, b, count, cases);
+}
+
+}  // namespace daxgb

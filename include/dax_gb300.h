@@ -1,0 +1,190 @@
+/*
+ * dax_gb300.h -- C ABI of the GB300 (sm_103a) device adapter for the Dax
+ * uniform-grid isosurface / threshold / gradient path.
+ *
+ * Plain C: raw device pointers, sizes, a POD grid descriptor and an opaque
+ * CUDA stream (cudaStream_t passed as void*; NULL = legacy default stream).
+ * Every call returns a dax_gb300_status; dax_gb300_last_error() returns the
+ * message of the last failing call on the calling thread.
+ *
+ * Work is stream-ordered and asynchronous unless the comment says "blocks".
+ * The only calls that block are the *_totals readers and the *_pipeline
+ * conveniences, mirroring the places where the Dax control environment needs
+ * a size on the host (ScanInclusive's return value,
+ * dax/cont/DispatcherGenerateInterpolatedCells.h:180-183, and
+ * dax/cont/DispatcherGenerateTopology.h:142-145).
+ *
+ * Ids follow dax::Id (int32, dax/Types.h:246-249).  Point fields are float32
+ * (dax::Scalar, dax/Types.h:265-268), one value per point, x fastest.
+ */
+#ifndef DAX_GB300_H
+#define DAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DAX_GB300_ABI_VERSION 1
+
+typedef enum dax_gb300_status {
+  DAX_GB300_SUCCESS = 0,
+  /* dax::cont::ErrorControlBadValue (dax/cont/ArrayHandle.h:110-123) */
+  DAX_GB300_ERROR_BAD_VALUE = 1,
+  /* dax::cont::ErrorControlOutOfMemory
+     (dax/thrust/cont/internal/ArrayManagerExecutionThrustDevice.h:97-100) */
+  DAX_GB300_ERROR_OUT_OF_MEMORY = 2,
+  /* dax::cont::ErrorExecution: an error raised on the device
+     (dax/exec/internal/ErrorMessageBuffer.h:46-66) */
+  DAX_GB300_ERROR_EXECUTION = 3,
+  /* a CUDA runtime call failed */
+  DAX_GB300_ERROR_CUDA = 4,
+  /* an output buffer is smaller than the result; nothing was written */
+  DAX_GB300_ERROR_CAPACITY = 5,
+  /* a bounded device-side wait (scan look-back) gave up */
+  DAX_GB300_ERROR_TIMEOUT = 6,
+  /* grid shape outside what the kernels support (see each call) */
+  DAX_GB300_ERROR_UNSUPPORTED = 7
+} dax_gb300_status;
+
+/* A dax::cont::UniformGrid (dax/cont/UniformGrid.h:114-252): point extent
+ * [extent_min, extent_max] inclusive, coordinates
+ * origin + spacing * (ijk + extent_min), computed in float. */
+typedef struct dax_gb300_uniform_grid {
+  float origin[3];
+  float spacing[3];
+  int32_t extent_min[3];
+  int32_t extent_max[3];
+} dax_gb300_uniform_grid;
+
+int dax_gb300_abi_version(void);
+const char* dax_gb300_last_error(void);
+
+/* Blocks until all work on `stream` is done and reports any sticky CUDA
+ * error.  Replaces DeviceAdapterAlgorithm<Tag>::Synchronize
+ * (dax/cuda/cont/internal/DeviceAdapterAlgorithmCuda.h:40-43). */
+int dax_gb300_synchronize(void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Point classification                                                      */
+/* ------------------------------------------------------------------------ */
+
+#define DAX_GB300_CLASSIFY_ABOVE 0    /* bit = value > a        (MarchingCubes.h:40-47) */
+#define DAX_GB300_CLASSIFY_IN_RANGE 1 /* bit = a <= value <= b  (Threshold.h:40-43)     */
+
+/* Number of uint32 words dax_gb300_classify_points writes for n points. */
+int64_t dax_gb300_classify_words(int64_t n);
+
+/* One bit per point, point i in bit (i % 32) of word i / 32, the first pass
+ * of the marching-cubes and threshold pipelines (the per-point half of
+ * GetHexahedronClassification / ThresholdFunction).  d_bits:
+ * uint32[dax_gb300_classify_words(n)]; the words after the last point are
+ * zero.  Asynchronous. */
+int dax_gb300_classify_points(const float* d_field, int64_t n, int mode, float a, float b,
+                              uint32_t* d_bits, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Marching cubes                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* Per-cell triangle count (and optionally the 8-bit case index) for every
+ * cell, in cell-id order: DispatcherMapCell<MarchingCubesCount>::Invoke
+ * (dax/cont/DispatcherMapCell.h:27-64 with dax/worklet/MarchingCubes.h:53-86).
+ * d_count: int32[cells]; d_cases: uint8[cells] or NULL. */
+int dax_gb300_mc_classify_count(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                float isovalue, int32_t* d_count, uint8_t* d_cases,
+                                void* stream);
+
+/* Device scratch the fused pipeline needs for this grid (bytes). */
+size_t dax_gb300_mc_scratch_bytes(const dax_gb300_uniform_grid* grid);
+
+/* Classify every point, count triangles and crossing edges per grid row and
+ * scan them (single pass, decoupled look-back): everything
+ * DispatcherGenerateInterpolatedCells::GenerateNewTopology does before its
+ * generate worklet (dax/cont/DispatcherGenerateInterpolatedCells.h:178-223).
+ * Asynchronous; results stay in d_scratch. */
+int dax_gb300_mc_count(const dax_gb300_uniform_grid* grid, const float* d_field, float isovalue,
+                       void* d_scratch, size_t scratch_bytes, void* stream);
+
+/* Blocks on `stream`, then returns the triangle count and the number of
+ * merged (unique-edge) vertices found by dax_gb300_mc_count, and any device
+ * error it raised.  Unmerged output has 3 * num_triangles vertices. */
+int dax_gb300_mc_totals(const void* d_scratch, int64_t* num_triangles,
+                        int64_t* num_merged_vertices, void* stream);
+
+/* Write the isosurface: the MarchingCubesGenerate worklet plus
+ * ResolveCoordinates (dax/cont/DispatcherGenerateInterpolatedCells.h:225-301,
+ * dax/worklet/MarchingCubes.h:121-168).
+ *   merge != 0 : SetRemoveDuplicatePoints(true)  -- vertices are the unique
+ *                crossing edges in ascending (first id, second id) order and
+ *                d_conn holds their indices;
+ *   merge == 0 : one vertex per triangle corner, d_conn = 0..3T-1.
+ * d_verts: float[vert_capacity][3]; d_conn: int32[tri_capacity][3].
+ * d_rec_first/d_rec_second/d_rec_weight (int32/int32/float [vert_capacity],
+ * any may be NULL) receive the PointAsEdgeInterpolation record of each
+ * vertex (dax/cont/internal/EdgeInterpolatedGrid.h:28-74), the input of
+ * dax_gb300_interpolate_point_field.  If a capacity is too small the call
+ * writes nothing and dax_gb300_mc_totals reports DAX_GB300_ERROR_CAPACITY.
+ * Must follow dax_gb300_mc_count on the same scratch, grid, field, isovalue
+ * and stream.  Asynchronous. */
+int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
+                          float isovalue, int merge, void* d_scratch, size_t scratch_bytes,
+                          float* d_verts, int64_t vert_capacity, int32_t* d_conn,
+                          int64_t tri_capacity, int32_t* d_rec_first, int32_t* d_rec_second,
+                          float* d_rec_weight, void* stream);
+
+/* CompactPointField for any scalar point field
+ * (dax/cont/DispatcherGenerateInterpolatedCells.h:107-141): out[v] =
+ * Lerp(in[first[v]], in[second[v]], weight[v]).  Asynchronous. */
+int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t* d_rec_second,
+                                      const float* d_rec_weight, int64_t n, const float* d_in,
+                                      float* d_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Threshold                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Per-cell 0/1 keep flag (all 8 point values in [lo, hi]):
+ * DispatcherMapCell<ThresholdCount<Scalar>> (dax/worklet/Threshold.h:69-96). */
+int dax_gb300_threshold_classify_count(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                       float lo, float hi, int32_t* d_count, void* stream);
+
+size_t dax_gb300_threshold_scratch_bytes(const dax_gb300_uniform_grid* grid);
+
+/* Classify, count kept cells and used points per row, scan (single pass).
+ * The front half of DispatcherGenerateTopology::GenerateNewTopology
+ * (dax/cont/DispatcherGenerateTopology.h:128-165).  Asynchronous. */
+int dax_gb300_threshold_count(const dax_gb300_uniform_grid* grid, const float* d_field, float lo,
+                              float hi, void* d_scratch, size_t scratch_bytes, void* stream);
+
+/* Blocks; kept cells K and used points (the compacted point count). */
+int dax_gb300_threshold_totals(const void* d_scratch, int64_t* kept_cells, int64_t* used_points,
+                               void* stream);
+
+/* Kept cells' connectivity into the compacted point list (int32[K][8], hex
+ * vertex order), the compacted coordinates (float[U][3]) and the compacted
+ * field (float[U], may be NULL): ThresholdTopology + FillPointMask +
+ * ResolveDuplicatePoints + CompactPointField
+ * (dax/cont/DispatcherGenerateTopology.h:98-258).  Asynchronous. */
+int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                 float lo, float hi, void* d_scratch, size_t scratch_bytes,
+                                 int32_t* d_conn, int64_t cell_capacity, float* d_coords,
+                                 float* d_field_out, int64_t point_capacity, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* CellGradient                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Per-cell gradient of a point scalar on voxels, float[cells][3]:
+ * DispatcherMapCell<CellGradient> (dax/worklet/CellGradient.h:28-48,
+ * dax/exec/Derivative.h:37-75).  Asynchronous. */
+int dax_gb300_cell_gradient(const dax_gb300_uniform_grid* grid, const float* d_field,
+                            float* d_gradient, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DAX_GB300_H */

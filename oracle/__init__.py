@@ -1,0 +1,152 @@
+"""numpy front end for the CPU oracle (test infrastructure only).
+
+``Oracle("port")`` loads the C restatement (``dax_oracle.c``);
+``Oracle("reference")`` loads ``ref_driver.cpp`` built against the DaxToolkit's
+own worklet headers (present only where the reference tree could be compiled).
+Both expose the same calls with the same argument meaning, so a test can run
+one against the other.  Nothing in the product package imports this module.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+
+class GridDesc(ctypes.Structure):
+    """Uniform grid: origin, spacing, point extent [min, max] (inclusive)."""
+
+    _fields_ = [("origin", ctypes.c_float * 3), ("spacing", ctypes.c_float * 3),
+                ("extent_min", ctypes.c_int32 * 3), ("extent_max", ctypes.c_int32 * 3)]
+
+
+def make_grid(dims, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0), extent_min=(0, 0, 0)):
+    g = GridDesc()
+    for a in range(3):
+        g.origin[a] = origin[a]
+        g.spacing[a] = spacing[a]
+        g.extent_min[a] = extent_min[a]
+        g.extent_max[a] = extent_min[a] + dims[a] - 1
+    return g
+
+
+def grid_dims(g):
+    return tuple(int(g.extent_max[a] - g.extent_min[a] + 1) for a in range(3))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    def __init__(self, kind="port"):
+        self.kind = kind
+        if kind == "port":
+            path, prefix = _build.build_oracle(), "orc_"
+        elif kind == "reference":
+            path, prefix = _build.build_ref(), "ref_"
+            if path is None or not os.path.exists(path):
+                raise RuntimeError("reference oracle not built (DaxToolkit tree unavailable)")
+        else:
+            raise ValueError(kind)
+        self.lib = ctypes.CDLL(path)
+        self._p = prefix
+        L = self.lib
+        vp, f32, i64 = ctypes.c_void_p, ctypes.c_float, ctypes.c_int64
+        gp = ctypes.POINTER(GridDesc)
+        self._count = getattr(L, prefix + "mc_count")
+        self._count.argtypes = [gp, vp, f32, vp, vp]
+        self._gen = getattr(L, prefix + "mc_generate")
+        self._gen.argtypes = [gp, vp, f32, vp, ctypes.c_int, vp, vp, vp, vp, vp,
+                              ctypes.POINTER(i64)]
+        self._gen.restype = i64
+        self._interp = getattr(L, prefix + "interpolate_point_field")
+        self._interp.argtypes = [vp, vp, vp, i64, vp, vp]
+        self._thr_count = getattr(L, prefix + "threshold_count")
+        self._thr_count.argtypes = [gp, vp, f32, f32, vp]
+        self._thr_gen = getattr(L, prefix + "threshold_generate")
+        self._thr_gen.argtypes = [gp, vp, vp, vp, vp, vp, ctypes.POINTER(i64)]
+        self._thr_gen.restype = i64
+        self._grad = getattr(L, prefix + "cell_gradient")
+        self._grad.argtypes = [gp, vp, vp]
+        if kind == "reference":
+            L.ref_set_threads.argtypes = [ctypes.c_int]
+            L.ref_max_threads.restype = ctypes.c_int
+
+    # -- threading (reference driver only; the C port is single-threaded) --
+    def set_threads(self, n):
+        if self.kind == "reference":
+            self.lib.ref_set_threads(int(n))
+            return int(n)
+        return 1
+
+    def max_threads(self):
+        return int(self.lib.ref_max_threads()) if self.kind == "reference" else 1
+
+    @staticmethod
+    def _cells(g):
+        d = grid_dims(g)
+        return 0 if min(d) < 2 else (d[0] - 1) * (d[1] - 1) * (d[2] - 1)
+
+    def mc_count(self, g, field, iso):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        C = self._cells(g)
+        count = np.zeros(C, np.int32)
+        cases = np.zeros(C, np.uint8)
+        self._count(ctypes.byref(g), _ptr(field), float(iso), _ptr(count), _ptr(cases))
+        return count, cases
+
+    def mc_generate(self, g, field, iso, count, merge=True):
+        """Returns dict(verts [V,3] f32, conn [T,3] i32, rec_a, rec_b, rec_w)."""
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        count = np.ascontiguousarray(count, dtype=np.int32)
+        T = int(count.astype(np.int64).sum())
+        cap = max(3 * T, 1)
+        verts = np.zeros((cap, 3), np.float32)
+        conn = np.zeros(cap, np.int32)
+        ra = np.zeros(cap, np.int32)
+        rb = np.zeros(cap, np.int32)
+        rw = np.zeros(cap, np.float32)
+        nv = ctypes.c_int64(0)
+        t = self._gen(ctypes.byref(g), _ptr(field), float(iso), _ptr(count), int(bool(merge)),
+                      _ptr(verts), _ptr(conn), _ptr(ra), _ptr(rb), _ptr(rw), ctypes.byref(nv))
+        assert t == T
+        V = nv.value
+        return dict(verts=verts[:V], conn=conn[:3 * T].reshape(T, 3), rec_a=ra[:V], rec_b=rb[:V],
+                    rec_w=rw[:V])
+
+    def interpolate_point_field(self, rec_a, rec_b, rec_w, field):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        out = np.zeros(len(rec_a), np.float32)
+        self._interp(_ptr(np.ascontiguousarray(rec_a)), _ptr(np.ascontiguousarray(rec_b)),
+                     _ptr(np.ascontiguousarray(rec_w)), len(rec_a), _ptr(field), _ptr(out))
+        return out
+
+    def threshold_count(self, g, field, lo, hi):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        count = np.zeros(self._cells(g), np.int32)
+        self._thr_count(ctypes.byref(g), _ptr(field), float(lo), float(hi), _ptr(count))
+        return count
+
+    def threshold_generate(self, g, field, count):
+        """Returns dict(conn [K,8] i32, coords [U,3] f32, field [U] f32)."""
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        count = np.ascontiguousarray(count, dtype=np.int32)
+        K = int(count.astype(np.int64).sum())
+        P = field.size
+        conn = np.zeros(max(8 * K, 1), np.int32)
+        coords = np.zeros((max(P, 1), 3), np.float32)
+        fout = np.zeros(max(P, 1), np.float32)
+        pu = ctypes.c_int64(0)
+        k = self._thr_gen(ctypes.byref(g), _ptr(field), _ptr(count), _ptr(conn), _ptr(coords),
+                          _ptr(fout), ctypes.byref(pu))
+        assert k == K
+        U = pu.value
+        return dict(conn=conn[:8 * K].reshape(K, 8), coords=coords[:U], field=fout[:U])
+
+    def cell_gradient(self, g, field):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        out = np.zeros((self._cells(g), 3), np.float32)
+        self._grad(ctypes.byref(g), _ptr(field), _ptr(out))
+        return out

@@ -1,0 +1,259 @@
+// Reference-side CPU driver: runs the DaxToolkit's OWN worklet functors
+// (MarchingCubesCount, MarchingCubesGenerate, ThresholdCount,
+// ThresholdTopology, CellGradient), its TopologyUniform connectivity and
+// point coordinates, its PointAsEdgeInterpolation ordering and dax::math::Lerp, compiled from the reference's headers.  Only the dispatcher
+// layer is restated here (the full dispatcher stack needs Boost.MPL and is not
+// buildable in this environment): it follows the Serial adapter's std::
+// algorithms step by step.
+//
+// TEST INFRASTRUCTURE ONLY: used to pin the C oracle (dax_oracle.c) and as
+// the timed CPU baseline.  Built by build_ref.sh into oracle/_ref/.
+//
+// With threads > 1 the per-cell / per-output loops run under OpenMP and the
+// scan and sort use libstdc++'s parallel mode, the CPU analogue of the
+// reference's OpenMP device adapter (dax/openmp/cont/internal/
+// DeviceAdapterAlgorithmOpenMP.h:34-139, Thrust's OMP backend).
+#include <dax/cont/internal/EdgeInterpolatedGrid.h>
+#include <dax/exec/internal/TopologyUniform.h>
+#include <dax/math/VectorAnalysis.h>
+#include <dax/worklet/CellGradient.h>
+#include <dax/worklet/MarchingCubes.h>
+#include <dax/worklet/Threshold.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#include <parallel/algorithm>
+#include <parallel/numeric>
+#endif
+
+namespace {
+
+struct RefGrid {
+  float origin[3];
+  float spacing[3];
+  int32_t extent_min[3];
+  int32_t extent_max[3];
+};
+
+int g_threads = 1;
+
+struct Ctx {
+  dax::exec::internal::TopologyUniform topo;
+  dax::Id numCells;
+  dax::Id numPoints;
+  explicit Ctx(const RefGrid* g) {
+    topo.Origin = dax::make_Vector3(g->origin[0], g->origin[1], g->origin[2]);
+    topo.Spacing = dax::make_Vector3(g->spacing[0], g->spacing[1], g->spacing[2]);
+    topo.Extent = dax::Extent3(dax::make_Id3(g->extent_min[0], g->extent_min[1], g->extent_min[2]),
+                               dax::make_Id3(g->extent_max[0], g->extent_max[1], g->extent_max[2]));
+    dax::Id3 d = dax::extentDimensions(topo.Extent);
+    numPoints = d[0] * d[1] * d[2];
+    numCells = (d[0] < 2 || d[1] < 2 || d[2] < 2) ? 0 : topo.GetNumberOfCells();
+  }
+  // Point coordinates of the uniform grid, origin + spacing * ijk with the
+  // extent minimum added (TopologyUniform::GetPointCoordiantes).
+  dax::Vector3 Coord(dax::Id p) const { return topo.GetPointCoordiantes(p); }
+  dax::exec::CellVertices<dax::CellTagVoxel> Verts(dax::Id cell) const {
+    return topo.GetCellConnections(cell);
+  }
+  template <typename T>
+  dax::exec::CellField<T, dax::CellTagVoxel> Gather(
+      const dax::exec::CellVertices<dax::CellTagVoxel>& v, const T* f) const {
+    dax::exec::CellField<T, dax::CellTagVoxel> vals;
+    for (int n = 0; n < 8; ++n) vals[n] = f[v[n]];
+    return vals;
+  }
+};
+
+template <typename It, typename Out>
+void partial_sum_any(It b, It e, Out o) {
+#ifdef _OPENMP
+  if (g_threads > 1) { __gnu_parallel::partial_sum(b, e, o); return; }
+#endif
+  std::partial_sum(b, e, o);
+}
+
+template <typename It>
+void sort_any(It b, It e) {
+#ifdef _OPENMP
+  if (g_threads > 1) { __gnu_parallel::sort(b, e); return; }
+#endif
+  std::sort(b, e);
+}
+
+// ScanInclusive + UpperBounds(counting) of DispatcherGenerateInterpolatedCells
+// / DispatcherGenerateTopology (GenerateNewTopology).
+dax::Id ScanAndUpperBounds(const int32_t* count, dax::Id C, std::vector<dax::Id>& cellOf) {
+  std::vector<dax::Id> scan(C);
+  partial_sum_any(count, count + C, scan.begin());
+  const dax::Id T = C ? scan[C - 1] : 0;
+  cellOf.resize(T);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id t = 0; t < T; ++t)
+    cellOf[t] = std::upper_bound(scan.begin(), scan.end(), t) - scan.begin();
+  return T;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ref_set_threads(int n) {
+  g_threads = n < 1 ? 1 : n;
+#ifdef _OPENMP
+  omp_set_num_threads(g_threads);
+#endif
+}
+
+int ref_max_threads() {
+#ifdef _OPENMP
+  return omp_get_num_procs();
+#else
+  return 1;
+#endif
+}
+
+void ref_mc_count(const RefGrid* g, const float* field, float iso, int32_t* count,
+                  uint8_t* cases) {
+  Ctx ctx(g);
+  dax::worklet::MarchingCubesCount worklet(iso);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id c = 0; c < ctx.numCells; ++c) {
+    dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(c);
+    dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> vals = ctx.Gather(v, field);
+    count[c] = (int32_t)worklet(vals);
+    if (cases)
+      cases[c] = (uint8_t)dax::worklet::internal::marchingcubes::GetHexahedronClassification(
+          dax::Scalar(iso), vals);
+  }
+}
+
+int64_t ref_mc_generate(const RefGrid* g, const float* field, float iso, const int32_t* count,
+                        int merge, float* verts, int32_t* conn, int32_t* rec_a, int32_t* rec_b,
+                        float* rec_w, int64_t* nverts) {
+  Ctx ctx(g);
+  *nverts = 0;
+  std::vector<dax::Id> cellOf;
+  const dax::Id T = ScanAndUpperBounds(count, ctx.numCells, cellOf);
+  if (T == 0) return 0;
+  dax::worklet::MarchingCubesGenerate worklet(iso);
+  std::vector<dax::PointAsEdgeInterpolation> recs(3 * T);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id t = 0; t < T; ++t) {
+    // ComputeVisitIndex: workId - LowerBounds(cellIds, cellIds[t])
+    const dax::Id visit =
+        t - (std::lower_bound(cellOf.begin(), cellOf.end(), cellOf[t]) - cellOf.begin());
+    dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cellOf[t]);
+    dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> vals = ctx.Gather(v, field);
+    dax::exec::InterpolatedCellPoints<dax::CellTagTriangle> out;
+    worklet(v, out, vals, visit);
+    for (int m = 0; m < 3; ++m) recs[3 * t + m] = out[m];
+  }
+  std::vector<dax::PointAsEdgeInterpolation> weights(recs);
+  if (merge) {
+    sort_any(weights.begin(), weights.end());
+    weights.erase(std::unique(weights.begin(), weights.end()), weights.end());
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+    for (dax::Id i = 0; i < 3 * T; ++i)
+      conn[i] = (int32_t)(std::lower_bound(weights.begin(), weights.end(), recs[i]) -
+                          weights.begin());
+  } else {
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+    for (dax::Id i = 0; i < 3 * T; ++i) conn[i] = (int32_t)i;
+  }
+  const dax::Id V = (dax::Id)weights.size();
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id i = 0; i < V; ++i) {
+    const dax::PointAsEdgeInterpolation& r = weights[i];
+    dax::Vector3 p = dax::math::Lerp(ctx.Coord(r.EdgeIdFirst), ctx.Coord(r.EdgeIdSecond),
+                                     r.Weight);
+    verts[3 * i + 0] = p[0];
+    verts[3 * i + 1] = p[1];
+    verts[3 * i + 2] = p[2];
+    if (rec_a) {
+      rec_a[i] = r.EdgeIdFirst;
+      rec_b[i] = r.EdgeIdSecond;
+      rec_w[i] = r.Weight;
+    }
+  }
+  *nverts = V;
+  return T;
+}
+
+void ref_interpolate_point_field(const int32_t* rec_a, const int32_t* rec_b, const float* rec_w,
+                                 int64_t n, const float* in, float* out) {
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (int64_t i = 0; i < n; ++i) out[i] = dax::math::Lerp(in[rec_a[i]], in[rec_b[i]], rec_w[i]);
+}
+
+void ref_threshold_count(const RefGrid* g, const float* field, float lo, float hi,
+                         int32_t* count) {
+  Ctx ctx(g);
+  dax::worklet::ThresholdCount<dax::Scalar> worklet(lo, hi);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id c = 0; c < ctx.numCells; ++c)
+    count[c] = (int32_t)worklet(ctx.Gather(ctx.Verts(c), field));
+}
+
+int64_t ref_threshold_generate(const RefGrid* g, const float* field, const int32_t* count,
+                               int32_t* conn, float* coords, float* field_out, int64_t* p_used) {
+  Ctx ctx(g);
+  *p_used = 0;
+  std::vector<dax::Id> cellOf;
+  const dax::Id K = ScanAndUpperBounds(count, ctx.numCells, cellOf);
+  if (K == 0) return 0;
+  dax::worklet::ThresholdTopology worklet;
+  std::vector<dax::Id> ids(8 * K);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id t = 0; t < K; ++t) {
+    dax::exec::CellVertices<dax::CellTagHexahedron> out;
+    worklet(ctx.Verts(cellOf[t]), out);
+    for (int n = 0; n < 8; ++n) ids[8 * t + n] = out[n];
+  }
+  // FillPointMask: ClearUsedPoints then GetUsedPoints through a permutation.
+  std::vector<dax::Id> mask(ctx.numPoints, 0);
+  for (dax::Id i = 0; i < 8 * K; ++i) mask[ids[i]] = 1;
+  // StreamCompact(coords, mask) and CompactPointField(field) in point order.
+  dax::Id U = 0;
+  for (dax::Id p = 0; p < ctx.numPoints; ++p) {
+    if (!mask[p]) continue;
+    dax::Vector3 c = ctx.Coord(p);
+    coords[3 * U + 0] = c[0];
+    coords[3 * U + 1] = c[1];
+    coords[3 * U + 2] = c[2];
+    field_out[U] = field[p];
+    ++U;
+  }
+  // ResolveDuplicatePoints: Copy, Sort, Unique, LowerBounds.
+  std::vector<dax::Id> used(ids);
+  sort_any(used.begin(), used.end());
+  used.erase(std::unique(used.begin(), used.end()), used.end());
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id i = 0; i < 8 * K; ++i)
+    conn[i] = (int32_t)(std::lower_bound(used.begin(), used.end(), ids[i]) - used.begin());
+  *p_used = U;
+  return K;
+}
+
+void ref_cell_gradient(const RefGrid* g, const float* field, float* out) {
+  Ctx ctx(g);
+  dax::worklet::CellGradient worklet;
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id c = 0; c < ctx.numCells; ++c) {
+    dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(c);
+    dax::exec::CellField<dax::Vector3, dax::CellTagVoxel> xyz;
+    for (int n = 0; n < 8; ++n) xyz[n] = ctx.Coord(v[n]);
+    dax::Vector3 grad = worklet(xyz, ctx.Gather(v, field));
+    out[3 * c + 0] = grad[0];
+    out[3 * c + 1] = grad[1];
+    out[3 * c + 2] = grad[2];
+  }
+}
+
+}  // extern "C"

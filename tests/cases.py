@@ -1,0 +1,115 @@
+"""Seeded parity cases shared by the CPU and GPU tests (small enough for the
+CPU oracle to finish in well under a second each)."""
+import numpy as np
+
+
+def linear_field(dims, grad=(1.0, 1.0, 1.0), origin=(0, 0, 0), spacing=(1, 1, 1), emin=(0, 0, 0)):
+    """x*gx + y*gy + z*gz on the grid's float coordinates (the reference's
+    unit-test fields, e.g. UnitTestWorkletMarchingCubes.cxx:94-101)."""
+    nx, ny, nz = dims
+    ax = [np.float32(origin[a]) + np.float32(spacing[a]) *
+          (np.arange(dims[a]) + emin[a]).astype(np.float32) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return (x * np.float32(grad[0]) + y * np.float32(grad[1]) + z * np.float32(grad[2])) \
+        .astype(np.float32).ravel()
+
+
+def all_cases_strip(iso=0.0, seed=5):
+    """A 769 x 2 x 2 grid whose cells at i = 3c have case index c for all 256
+    marching-cubes cases (other cells get whatever their points give)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = 3 * 256 + 1, 2, 2
+    f = rng.uniform(-1, 1, size=(nz, ny, nx)).astype(np.float32)
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    for c in range(256):
+        for n, (di, dj, dk) in enumerate(corners):
+            f[dk, dj, 3 * c + di] = iso + (0.5 if (c >> n) & 1 else -0.5)
+    return (nx, ny, nz), f.ravel()
+
+
+def random_blobs(dims, nblobs, seed, noise=0.0):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.1, 0.9, size=(nblobs, 3))
+    s = rng.uniform(0.05, 0.15, size=nblobs)
+    ax = [np.arange(dims[a]) / max(dims[a] - 1, 1) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    f = np.zeros_like(x)
+    for b in range(nblobs):
+        f += np.exp(-((x - c[b, 0]) ** 2 + (y - c[b, 1]) ** 2 + (z - c[b, 2]) ** 2) / (2 * s[b] ** 2))
+    if noise:
+        f += noise * rng.uniform(-1, 1, size=f.shape)
+    return f.astype(np.float32).ravel()
+
+
+def sphere(dims, noise=0.01, seed=1234):
+    rng = np.random.default_rng(seed)
+    ax = [np.arange(dims[a]) / (dims[a] - 1) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    r = np.sqrt((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2)
+    return (r + noise * rng.uniform(-1, 1, size=r.shape)).astype(np.float32).ravel()
+
+
+def mc_cases():
+    """(name, dims, origin, spacing, extent_min, field, isovalue)."""
+    out = []
+    out.append(("kat26_linear", (26, 26, 26), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                linear_field((26, 26, 26)), 70.0))
+    out.append(("sphere64", (64, 64, 64), (0, 0, 0), (1 / 63,) * 3, (0, 0, 0),
+                sphere((64, 64, 64)), 0.35))
+    d = (48, 40, 36)
+    out.append(("blobs_48x40x36", d, (0, 0, 0), tuple(1 / (n - 1) for n in d), (0, 0, 0),
+                random_blobs(d, 4, 11, noise=0.05), 0.5))
+    d = (33, 17, 5)
+    out.append(("odd_33x17x5_offset", d, (-1.5, 2.25, 0.125), (0.3, 0.7, 1.1), (3, -2, 7),
+                random_blobs(d, 3, 12), 0.4))
+    d, f = all_cases_strip()
+    out.append(("all256_strip", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), f, 0.0))
+    d = (70, 3, 4)
+    out.append(("wide_x_70x3x4", d, (0, 0, 0), (0.1, 0.2, 0.3), (0, 0, 0),
+                random_blobs(d, 2, 13, noise=0.3), 0.5))
+    d = (2, 2, 2)
+    out.append(("single_cell", d, (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                np.array([1, -1, 1, -1, -1, 1, 1, -1], np.float32), 0.0))
+    d = (20, 20, 20)
+    f = random_blobs(d, 3, 14)
+    f[::7] = np.nan
+    out.append(("nan_sprinkled", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), f, 0.5))
+    out.append(("all_inside", (9, 8, 7), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                np.ones(9 * 8 * 7, np.float32), 0.0))
+    out.append(("flat_no_cells", (16, 16, 1), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                random_blobs((16, 16, 1), 2, 15), 0.3))
+    d = (130, 9, 6)
+    out.append(("x130_two_words_tail", d, (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                random_blobs(d, 5, 16, noise=0.2), 0.45))
+    return out
+
+
+def threshold_cases():
+    out = []
+    out.append(("kat26_linear", (26, 26, 26), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                linear_field((26, 26, 26)), 70.0, 82.0))
+    d = (48, 40, 36)
+    out.append(("blobs_48x40x36", d, (0, 0, 0), tuple(1 / (n - 1) for n in d), (0, 0, 0),
+                random_blobs(d, 4, 11, noise=0.05), 0.3, 0.7))
+    d = (33, 17, 5)
+    out.append(("odd_33x17x5_offset", d, (-1.5, 2.25, 0.125), (0.3, 0.7, 1.1), (3, -2, 7),
+                random_blobs(d, 3, 12), 0.1, 0.6))
+    d = (130, 9, 6)
+    out.append(("x130", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 5, 16, noise=0.2),
+                0.2, 0.8))
+    out.append(("none_kept", (9, 8, 7), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                np.ones(9 * 8 * 7, np.float32), 2.0, 3.0))
+    out.append(("all_kept", (9, 8, 7), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                np.ones(9 * 8 * 7, np.float32), 0.0, 3.0))
+    return out
+
+
+def gradient_cases():
+    out = []
+    out.append(("kat8_linear", (8, 8, 8), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                linear_field((8, 8, 8))))
+    out.append(("sphere64", (64, 64, 64), (0, 0, 0), (1 / 63,) * 3, (0, 0, 0), sphere((64, 64, 64))))
+    d = (33, 17, 5)
+    out.append(("odd_33x17x5_offset", d, (-1.5, 2.25, 0.125), (0.3, 0.7, 1.1), (3, -2, 7),
+                random_blobs(d, 3, 12)))
+    return out

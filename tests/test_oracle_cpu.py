@@ -1,0 +1,128 @@
+"""The CPU oracle against the reference's own known answers and against the
+reference's worklets compiled from source (where the reference tree exists).
+
+Known answers (DaxToolkit unit tests):
+  * UnitTestWorkletMarchingCubes.cxx:39-40, :94-193 -- 26^3 grid, field x+y+z,
+    isovalue 70: points == 3 * cells unmerged, 45 unique points merged, and a
+    secondary linear field interpolates linearly (test_equal, 1e-4 ratio).
+  * UnitTestWorkletThreshold.cxx:40-42, :86-239 -- 26^3, [70, 82]: every kept
+    cell's points in range, coordinates of kept cells in input order.
+  * UnitTestWorkletCellGradient.cxx:31, :83-117 -- 8^3, x+y+z, gradient (1,1,1).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import cases
+
+
+def _grid(dims, origin=(0, 0, 0), spacing=(1, 1, 1), emin=(0, 0, 0)):
+    return oracle.make_grid(dims, origin, spacing, emin)
+
+
+def _kinds():
+    kinds = ["port"]
+    if oracle.build.reference_available():
+        kinds.append("reference")
+    return kinds
+
+
+def dax_test_equal(a, b, tol=1e-4):
+    """dax/testing/Testing.h:405-430 test_equal: |a-b| small relative to |a|+|b|."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    diff = np.abs(a - b)
+    scale = np.abs(a) + np.abs(b)
+    return bool(np.all((diff <= tol) | (diff <= tol * scale)))
+
+
+@pytest.mark.parametrize("kind", _kinds())
+def test_mc_known_answer(kind):
+    O = oracle.Oracle(kind)
+    g = _grid((26, 26, 26))
+    f = cases.linear_field((26, 26, 26))
+    count, _ = O.mc_count(g, f, 70.0)
+    assert int(count.sum()) == 61
+    un = O.mc_generate(g, f, 70.0, count, merge=False)
+    assert un["verts"].shape == (183, 3)
+    assert np.array_equal(un["conn"].ravel(), np.arange(183))
+    mg = O.mc_generate(g, f, 70.0, count, merge=True)
+    assert mg["verts"].shape == (45, 3)
+    # secondary field (-0.5, 1, 2) interpolates linearly
+    sec = cases.linear_field((26, 26, 26), grad=(-0.5, 1.0, 2.0))
+    for out in (un, mg):
+        vals = O.interpolate_point_field(out["rec_a"], out["rec_b"], out["rec_w"], sec)
+        expect = out["verts"].astype(np.float64) @ np.array([-0.5, 1.0, 2.0])
+        assert dax_test_equal(vals, expect)
+    # merged topology is the unmerged one with duplicates collapsed
+    assert np.array_equal(mg["verts"][mg["conn"].ravel()], un["verts"])
+
+
+@pytest.mark.parametrize("kind", _kinds())
+def test_threshold_known_answer(kind):
+    O = oracle.Oracle(kind)
+    g = _grid((26, 26, 26))
+    f = cases.linear_field((26, 26, 26))
+    count = O.threshold_count(g, f, 70.0, 82.0)
+    out = O.threshold_generate(g, f, count)
+    assert out["conn"].shape[1] == 8
+    assert np.all((out["field"] >= 70) & (out["field"] <= 82))
+    # CheckConnections: kept cells in input order, coordinates match
+    kept = np.nonzero(count)[0]
+    assert len(kept) == out["conn"].shape[0] == 10
+    d = 25
+    for n, c in enumerate(kept):
+        i, j, k = c % d, (c // d) % d, c // (d * d)
+        corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        for v, (di, dj, dk) in enumerate(corners):
+            assert np.array_equal(out["coords"][out["conn"][n, v]], [i + di, j + dj, k + dk])
+
+
+@pytest.mark.parametrize("kind", _kinds())
+def test_gradient_known_answer(kind):
+    O = oracle.Oracle(kind)
+    g = _grid((8, 8, 8))
+    grad = O.cell_gradient(g, cases.linear_field((8, 8, 8)))
+    assert grad.shape == (343, 3)
+    assert dax_test_equal(grad, np.ones_like(grad))
+
+
+@pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
+@pytest.mark.parametrize("case", cases.mc_cases(), ids=lambda c: c[0])
+def test_mc_port_matches_reference_build(case):
+    name, dims, origin, spacing, emin, f, iso = case
+    P, R = oracle.Oracle("port"), oracle.Oracle("reference")
+    g = _grid(dims, origin, spacing, emin)
+    c1, k1 = P.mc_count(g, f, iso)
+    c2, k2 = R.mc_count(g, f, iso)
+    assert np.array_equal(c1, c2) and np.array_equal(k1, k2)
+    for merge in (False, True):
+        a = P.mc_generate(g, f, iso, c1, merge)
+        b = R.mc_generate(g, f, iso, c2, merge)
+        for key in ("conn", "rec_a", "rec_b"):
+            assert np.array_equal(a[key], b[key]), key
+        for key in ("verts", "rec_w"):
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), key
+
+
+@pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
+@pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
+def test_threshold_port_matches_reference_build(case):
+    name, dims, origin, spacing, emin, f, lo, hi = case
+    P, R = oracle.Oracle("port"), oracle.Oracle("reference")
+    g = _grid(dims, origin, spacing, emin)
+    c1, c2 = P.threshold_count(g, f, lo, hi), R.threshold_count(g, f, lo, hi)
+    assert np.array_equal(c1, c2)
+    a, b = P.threshold_generate(g, f, c1), R.threshold_generate(g, f, c2)
+    assert np.array_equal(a["conn"], b["conn"])
+    assert np.array_equal(a["coords"].view(np.uint32), b["coords"].view(np.uint32))
+    assert np.array_equal(a["field"].view(np.uint32), b["field"].view(np.uint32))
+
+
+@pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
+@pytest.mark.parametrize("case", cases.gradient_cases(), ids=lambda c: c[0])
+def test_gradient_port_matches_reference_build(case):
+    name, dims, origin, spacing, emin, f = case
+    g = _grid(dims, origin, spacing, emin)
+    a = oracle.Oracle("port").cell_gradient(g, f)
+    b = oracle.Oracle("reference").cell_gradient(g, f)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))

@@ -1,0 +1,149 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the CPU
+oracle on the same float32 bytes.  Topology (case indices, counts,
+connectivity, interpolation end points) must be identical; vertex positions,
+weights, threshold coordinates and gradients are compared bit for bit as
+well (the kernels round every operation as the reference does)."""
+import numpy as np
+import pytest
+import torch
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(cont, dims, origin, spacing, emin):
+    return cont.UniformGrid(dims, origin, spacing, emin)
+
+
+def _ogrid(dims, origin, spacing, emin):
+    import oracle
+    return oracle.make_grid(dims, origin, spacing, emin)
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.mark.parametrize("case", cases.mc_cases(), ids=lambda c: c[0])
+def test_mc_classify_count(gb300, oracle_best, case):
+    name, dims, origin, spacing, emin, f, iso = case
+    cont = gb300
+    grid = _grid(cont, dims, origin, spacing, emin)
+    fd = torch.from_numpy(f).cuda()
+    count_ref, cases_ref = oracle_best.mc_count(_ogrid(dims, origin, spacing, emin), f, iso)
+    disp = cont.DispatcherMapCell(cont.MarchingCubesCount(iso))
+    count, cs = disp.classify_cases(grid, fd)
+    torch.cuda.synchronize()
+    assert np.array_equal(count.cpu().numpy(), count_ref)
+    assert np.array_equal(cs.cpu().numpy(), cases_ref)
+    assert np.array_equal(disp.Invoke(grid, fd).cpu().numpy(), count_ref)
+
+
+@pytest.mark.parametrize("merge", [True, False], ids=["merged", "unmerged"])
+@pytest.mark.parametrize("case", cases.mc_cases(), ids=lambda c: c[0])
+def test_mc_generate(gb300, oracle_best, case, merge):
+    name, dims, origin, spacing, emin, f, iso = case
+    cont = gb300
+    og = _ogrid(dims, origin, spacing, emin)
+    count, _ = oracle_best.mc_count(og, f, iso)
+    ref = oracle_best.mc_generate(og, f, iso, count, merge)
+    out = cont.marching_cubes(_grid(cont, dims, origin, spacing, emin), torch.from_numpy(f).cuda(),
+                              iso, merge=merge, records=True)
+    conn = out["conn"].cpu().numpy()
+    verts = out["verts"].cpu().numpy()
+    assert conn.shape == ref["conn"].shape
+    assert verts.shape == ref["verts"].shape
+    assert np.array_equal(conn, ref["conn"])
+    assert np.array_equal(out["rec_first"].cpu().numpy(), ref["rec_a"])
+    assert np.array_equal(out["rec_second"].cpu().numpy(), ref["rec_b"])
+    assert np.array_equal(_bits(out["rec_weight"].cpu().numpy()), _bits(ref["rec_w"]))
+    assert np.array_equal(_bits(verts), _bits(ref["verts"]))
+
+
+def test_mc_known_answer_counts(gb300):
+    cont = gb300
+    f = torch.from_numpy(cases.linear_field((26, 26, 26))).cuda()
+    grid = cont.UniformGrid((26, 26, 26))
+    assert cont.marching_cubes(grid, f, 70.0, merge=False)["verts"].shape[0] == 183
+    out = cont.marching_cubes(grid, f, 70.0, merge=True)
+    assert out["verts"].shape[0] == 45 and out["conn"].shape[0] == 61
+
+
+def test_mc_dispatchers_secondary_field(gb300, oracle_best):
+    """UnitTestWorkletMarchingCubes flow through the dispatcher surface:
+    count, generate without and with merging, CompactPointField."""
+    cont = gb300
+    dims = (26, 26, 26)
+    f = torch.from_numpy(cases.linear_field(dims)).cuda()
+    sec_np = cases.linear_field(dims, grad=(-0.5, 1.0, 2.0))
+    sec = torch.from_numpy(sec_np).cuda()
+    grid = cont.UniformGrid(dims)
+    count = cont.DispatcherMapCell(cont.MarchingCubesCount(70.0)).Invoke(grid, f)
+    disp = cont.DispatcherGenerateInterpolatedCells(count, cont.MarchingCubesGenerate(70.0))
+    disp.SetRemoveDuplicatePoints(False)
+    disp.SetReleaseCount(False)
+    og = disp.Invoke(grid, f)
+    assert og.GetNumberOfPoints() == 3 * og.GetNumberOfCells()
+    vals = disp.CompactPointField(sec).cpu().numpy()
+    ref_count, _ = oracle_best.mc_count(_ogrid(dims, (0, 0, 0), (1, 1, 1), (0, 0, 0)),
+                                        f.cpu().numpy(), 70.0)
+    ref = oracle_best.mc_generate(_ogrid(dims, (0, 0, 0), (1, 1, 1), (0, 0, 0)), f.cpu().numpy(),
+                                  70.0, ref_count, False)
+    ref_vals = oracle_best.interpolate_point_field(ref["rec_a"], ref["rec_b"], ref["rec_w"], sec_np)
+    assert np.array_equal(_bits(vals), _bits(ref_vals))
+    disp.SetRemoveDuplicatePoints(True)
+    og2 = disp.Invoke(grid, f)
+    assert og2.GetNumberOfPoints() == 45
+
+
+@pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
+def test_threshold(gb300, oracle_best, case):
+    name, dims, origin, spacing, emin, f, lo, hi = case
+    cont = gb300
+    og = _ogrid(dims, origin, spacing, emin)
+    count_ref = oracle_best.threshold_count(og, f, lo, hi)
+    ref = oracle_best.threshold_generate(og, f, count_ref)
+    grid = _grid(cont, dims, origin, spacing, emin)
+    fd = torch.from_numpy(f).cuda()
+    count = cont.DispatcherMapCell(cont.ThresholdCount(lo, hi)).Invoke(grid, fd)
+    assert np.array_equal(count.cpu().numpy(), count_ref)
+    out = cont.threshold(grid, fd, lo, hi)
+    assert np.array_equal(out["conn"].cpu().numpy(), ref["conn"])
+    assert np.array_equal(_bits(out["coords"].cpu().numpy()), _bits(ref["coords"]))
+    assert np.array_equal(_bits(out["field"].cpu().numpy()), _bits(ref["field"]))
+
+
+@pytest.mark.parametrize("case", cases.gradient_cases(), ids=lambda c: c[0])
+def test_cell_gradient(gb300, oracle_best, case):
+    name, dims, origin, spacing, emin, f = case
+    cont = gb300
+    ref = oracle_best.cell_gradient(_ogrid(dims, origin, spacing, emin), f)
+    out = cont.DispatcherMapCell(cont.CellGradient()).Invoke(
+        _grid(cont, dims, origin, spacing, emin), torch.from_numpy(f).cuda())
+    assert np.array_equal(_bits(out.cpu().numpy()), _bits(ref))
+
+
+def test_capacity_error_writes_nothing(gb300):
+    """A too-small output buffer is reported, and nothing is written."""
+    import ctypes
+    from daxtoolkit_gb300 import capi
+    cont = gb300
+    dims = (26, 26, 26)
+    grid = cont.UniformGrid(dims)
+    f = torch.from_numpy(cases.linear_field(dims)).cuda()
+    g = grid.desc()
+    n = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    scratch = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    capi.call("dax_gb300_mc_count", ctypes.byref(g), p(f), 70.0, p(scratch), n, s)
+    verts = torch.full((10, 3), -7.0, device="cuda")
+    conn = torch.full((10, 3), -7, dtype=torch.int32, device="cuda")
+    capi.call("dax_gb300_mc_generate", ctypes.byref(g), p(f), 70.0, 1, p(scratch), n, p(verts), 10,
+              p(conn), 10, None, None, None, s)
+    T, V = ctypes.c_int64(0), ctypes.c_int64(0)
+    st = capi.lib().dax_gb300_mc_totals(p(scratch), ctypes.byref(T), ctypes.byref(V), s)
+    assert st == capi.ERROR_CAPACITY
+    assert T.value == 61 and V.value == 45
+    assert bool((verts == -7.0).all()) and bool((conn == -7).all())
