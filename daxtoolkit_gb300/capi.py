@@ -78,6 +78,16 @@ SIGNATURES = {
     "dax_gb300_threshold_totals": ([vp, ctypes.POINTER(i64), ctypes.POINTER(i64), vp], i32),
     "dax_gb300_threshold_generate": ([gp, vp, f32, f32, vp, sz, vp, i64, vp, vp, i64, vp], i32),
     "dax_gb300_cell_gradient": ([gp, vp, vp, vp], i32),
+    "dax_gb300_field_adjoint": ([gp, vp, f32, vp, sz, vp, vp, vp, vp], i32),
+    "dax_gb300_mc_batch_create": ([i32, gp, vp, vp, ctypes.POINTER(vp)], i32),
+    "dax_gb300_mc_batch_destroy": ([vp], i32),
+    "dax_gb300_mc_batch_scratch_bytes": ([vp], sz),
+    "dax_gb300_mc_batch_count": ([vp, vp, sz, vp], i32),
+    "dax_gb300_mc_batch_totals": ([vp, vp, vp, vp, vp], i32),
+    "dax_gb300_mc_batch_generate": ([vp, i32, vp, sz, vp, i64, vp, i64, vp], i32),
+    "dax_gb300_mc_batch_capture": ([vp, i32, vp, sz, vp, i64, vp, i64, ctypes.POINTER(vp)], i32),
+    "dax_gb300_graph_launch": ([vp, vp], i32),
+    "dax_gb300_graph_destroy": ([vp], i32),
 }
 
 

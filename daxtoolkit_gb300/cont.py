@@ -339,3 +339,78 @@ class DispatcherGenerateTopology:
 
     def CompactPointField(self, field=None):
         return self._field
+
+
+class MarchingCubesBatch:
+    """Many uniform grids (own extents, fields, isovalues) through one launch
+    per pass: ``dax_gb300_mc_batch_*``.  Outputs are concatenated; grid g's
+    triangles are ``conn[tri_offsets[g]:tri_offsets[g+1]]`` and index the
+    grid's own vertices ``verts[vert_offsets[g]:vert_offsets[g+1]]`` (merged)."""
+
+    def __init__(self, grids, fields, isovalues):
+        self.grids = list(grids)
+        self.fields = list(fields)
+        for gr, f in zip(self.grids, self.fields):
+            _require_field(f, gr)
+        n = len(self.grids)
+        descs = (capi.UniformGridDesc * n)(*[gr.desc() for gr in self.grids])
+        ptrs = (ctypes.c_void_p * n)(*[f.data_ptr() for f in self.fields])
+        isos = (ctypes.c_float * n)(*[float(v) for v in isovalues])
+        h = ctypes.c_void_p()
+        capi.call("dax_gb300_mc_batch_create", n, descs, ptrs, isos, ctypes.byref(h))
+        self.handle = h
+        self.n = n
+        nbytes = capi.lib().dax_gb300_mc_batch_scratch_bytes(h)
+        self.scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.fields[0].device)
+        self.graph = None
+
+    def __del__(self):
+        try:
+            if self.graph:
+                capi.lib().dax_gb300_graph_destroy(self.graph)
+            if self.handle:
+                capi.lib().dax_gb300_mc_batch_destroy(self.handle)
+        except Exception:
+            pass
+
+    def count(self, stream=None):
+        capi.call("dax_gb300_mc_batch_count", self.handle, _ptr(self.scratch), self.scratch.numel(),
+                  _stream(stream))
+
+    def totals(self, stream=None):
+        t = (ctypes.c_int64 * (self.n + 1))()
+        v = (ctypes.c_int64 * (self.n + 1))()
+        capi.call("dax_gb300_mc_batch_totals", self.handle, _ptr(self.scratch), t, v,
+                  _stream(stream))
+        return list(t), list(v)
+
+    def generate(self, verts, conn, merge=True, stream=None):
+        capi.call("dax_gb300_mc_batch_generate", self.handle, int(bool(merge)), _ptr(self.scratch),
+                  self.scratch.numel(), _ptr(verts), verts.shape[0], _ptr(conn), conn.shape[0],
+                  _stream(stream))
+
+    def run(self, merge=True, stream=None):
+        """count, size on the host, generate; returns (verts, conn, tri_off, vert_off)."""
+        self.count(stream)
+        t, v = self.totals(stream)
+        dev = self.fields[0].device
+        V = v[-1] if merge else 3 * t[-1]
+        verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+        conn = torch.empty((t[-1], 3), dtype=torch.int32, device=dev)
+        self.generate(verts, conn, merge, stream)
+        if not merge:
+            v = [3 * x for x in t]
+        return verts, conn, t, v
+
+    def capture(self, verts, conn, merge=True):
+        """Capture count + generate into a CUDA graph writing into verts/conn."""
+        g = ctypes.c_void_p()
+        capi.call("dax_gb300_mc_batch_capture", self.handle, int(bool(merge)), _ptr(self.scratch),
+                  self.scratch.numel(), _ptr(verts), verts.shape[0], _ptr(conn), conn.shape[0],
+                  ctypes.byref(g))
+        if self.graph:
+            capi.lib().dax_gb300_graph_destroy(self.graph)
+        self.graph = g
+
+    def replay(self, stream=None):
+        capi.call("dax_gb300_graph_launch", self.graph, _stream(stream))

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/dax_gb300.h"
 #include "common.cuh"
@@ -78,14 +79,39 @@ int make_grid(const dax_gb300_uniform_grid* in, Grid& g) {
 
 bool has_cells(const Grid& g) { return g.nx >= 2 && g.ny >= 2 && g.nz >= 2; }
 
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Marching-cubes scratch: [Info][status 3 x tiles][wt][wv][act][bits].
+struct McLayout {
+  int tiles;
+  long long rowwords;
+  size_t info, status, wt, wv, act, bits, total, clear;
+};
+
+McLayout mc_layout(const Grid& g) {
+  McLayout L;
+  L.rowwords = g.R * g.wr;
+  L.tiles = daxgb::mc_scan_tiles(L.rowwords);
+  L.info = 0;
+  L.status = align256(sizeof(Info));
+  L.clear = align256(L.status + 3 * (size_t)L.tiles * 8);
+  L.wt = L.clear;
+  L.wv = align256(L.wt + 4 * (size_t)(L.rowwords + 1));
+  L.act = align256(L.wv + 4 * (size_t)(L.rowwords + 1));
+  L.bits = align256(L.act + 4 * (size_t)L.rowwords);
+  L.total = align256(L.bits + 4 * (size_t)daxgb::bit_words(g.P));
+  return L;
+}
+
+// Threshold scratch: [Info][status 2 x tiles][row_a][row_b][bits][used].
 struct Layout {
   int tiles;
   size_t info, status, row_a, row_b, bits, used, total, clear;
 };
 
-Layout layout(const Grid& g, bool with_used) {
+Layout layout(const Grid& g) {
   Layout L;
   L.tiles = (int)((g.R + daxgb::kRowsPerTile - 1) / daxgb::kRowsPerTile);
   L.info = 0;
@@ -95,7 +121,7 @@ Layout layout(const Grid& g, bool with_used) {
   L.row_b = align256(L.row_a + (size_t)(g.R + 1) * 8);
   L.bits = align256(L.row_b + (size_t)(g.R + 1) * 8);
   L.used = align256(L.bits + (size_t)daxgb::bit_words(g.P) * 4);
-  L.total = with_used ? align256(L.used + (size_t)g.R * g.wr * 4) : L.used;
+  L.total = align256(L.used + (size_t)g.R * g.wr * 4);
   return L;
 }
 
@@ -119,6 +145,8 @@ int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
   if (b) *b = h.total_b;
   if (h.error & daxgb::kErrTimeout)
     return fail(DAX_GB300_ERROR_TIMEOUT, "scan look-back wait expired on the device");
+  if (h.error & daxgb::kErrOverflow)
+    return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31-1 triangles or vertices");
   if (h.error & daxgb::kErrCapacity)
     return fail(DAX_GB300_ERROR_CAPACITY, "output capacity smaller than the result; nothing written");
   return DAX_GB300_SUCCESS;
@@ -130,27 +158,65 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
   int st = make_grid(grid, g);
   if (st) return st;
   if (!field || !scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
-  const Layout L = layout(g, mode == 1);
-  if (bytes < L.total) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than *_scratch_bytes()");
-  cudaError_t e = cudaMemsetAsync(scratch, 0, has_cells(g) ? L.clear : sizeof(Info), s);
-  if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
-  if (!has_cells(g)) return DAX_GB300_SUCCESS;  // no cells: totals stay 0
+  const size_t need = mode == 0 ? mc_layout(g).total : layout(g).total;
+  if (bytes < need) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than *_scratch_bytes()");
+  if (!has_cells(g)) {  // no cells: totals stay 0
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Info), s);
+    return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing scratch");
+  }
   const int sms = num_sms();
+  const daxgb::GridSet S = daxgb::single_set(g, field, a, b);
+  if (mode == 0) {
+    const McLayout L = mc_layout(g);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, L.clear, s);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
+    uint32_t* bits = at<uint32_t>(scratch, L.bits);
+    daxgb::launch_classify_bits(0, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
+    if ((st = check_launch("classify kernel"))) return st;
+    daxgb::launch_mc_scan(S, bits, at<uint32_t>(scratch, L.wt), at<uint32_t>(scratch, L.wv),
+                          at<uint32_t>(scratch, L.act), at<unsigned long long>(scratch, L.status),
+                          at<Info>(scratch, L.info), L.tiles, sms, s);
+    return check_launch("count/scan kernel");
+  }
+  const Layout L = layout(g);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, L.clear, s);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
   uint32_t* bits = at<uint32_t>(scratch, L.bits);
-  daxgb::launch_classify_bits(mode, field, g.P, a, b, bits, daxgb::bit_words(g.P), sms, s);
+  daxgb::launch_classify_bits(1, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
   if ((st = check_launch("classify kernel"))) return st;
-  Info* info = at<Info>(scratch, L.info);
-  auto* status = at<unsigned long long>(scratch, L.status);
-  if (mode == 0)
-    daxgb::launch_mc_rows(g, bits, at<long long>(scratch, L.row_a), at<long long>(scratch, L.row_b),
-                          status, info, L.tiles, s);
-  else
-    daxgb::launch_thr_rows(g, bits, at<uint32_t>(scratch, L.used), at<long long>(scratch, L.row_a),
-                           at<long long>(scratch, L.row_b), status, info, L.tiles, s);
+  daxgb::launch_thr_rows(g, bits, at<uint32_t>(scratch, L.used), at<long long>(scratch, L.row_a),
+                         at<long long>(scratch, L.row_b), at<unsigned long long>(scratch, L.status),
+                         at<Info>(scratch, L.info), L.tiles, s);
   return check_launch("row count/scan kernel");
 }
 
 }  // namespace
+
+// Batched marching cubes plan (host side of dax_gb300_mc_batch).
+struct dax_gb300_mc_batch {
+  int count = 0;
+  std::vector<daxgb::GridSlot> slots;
+  daxgb::GridSlot* d_slots = nullptr;
+  long long rows = 0, chunks = 0, words = 0, blocks = 0, rowwords = 0;
+  int max_wr = 1;
+  bool aligned = true;
+  int tiles = 0;
+  size_t off_info = 0, off_goff = 0, off_status = 0, off_wt = 0, off_wv = 0, off_act = 0,
+         off_bits = 0;
+  size_t clear = 0, total = 0;
+
+  daxgb::GridSet set() const {
+    daxgb::GridSet S{};
+    S.slots = d_slots;
+    S.count = count;
+    S.rows = rows;
+    S.chunks = chunks;
+    S.blocks = blocks;
+    S.rowwords = rowwords;
+    if (count == 1) S.one = slots[0];
+    return S;
+  }
+};
 
 extern "C" {
 
@@ -172,7 +238,13 @@ int dax_gb300_classify_points(const float* d_field, int64_t n, int mode, float a
   if (!d_field || !d_bits) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or bits");
   if (mode != DAX_GB300_CLASSIFY_ABOVE && mode != DAX_GB300_CLASSIFY_IN_RANGE)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "unknown classification mode");
-  daxgb::launch_classify_bits(mode, d_field, n, a, b, d_bits, daxgb::bit_words(n), num_sms(),
+  Grid g{};
+  g.P = n;
+  g.nx = 1;
+  g.ny = 1;
+  g.nz = 1;
+  const daxgb::GridSet S = daxgb::single_set(g, d_field, a, b);
+  daxgb::launch_classify_bits(mode, S, aligned16(d_field), d_bits, daxgb::bit_words(n), num_sms(),
                               static_cast<cudaStream_t>(stream));
   return check_launch("classify kernel");
 }
@@ -193,7 +265,7 @@ int dax_gb300_mc_classify_count(const dax_gb300_uniform_grid* grid, const float*
 size_t dax_gb300_mc_scratch_bytes(const dax_gb300_uniform_grid* grid) {
   Grid g;
   if (make_grid(grid, g)) return 0;
-  return layout(g, false).total;
+  return mc_layout(g).total;
 }
 
 int dax_gb300_mc_count(const dax_gb300_uniform_grid* grid, const float* d_field, float isovalue,
@@ -221,11 +293,12 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
       tri_capacity < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
-  const Layout L = layout(g, false);
+  const McLayout L = mc_layout(g);
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
-  daxgb::launch_mc_emit(g, d_field, isovalue, merge != 0, at<uint32_t>(d_scratch, L.bits),
-                        at<long long>(d_scratch, L.row_a), at<long long>(d_scratch, L.row_b),
+  daxgb::launch_mc_emit(daxgb::single_set(g, d_field, isovalue, 0.0f), merge != 0,
+                        at<uint32_t>(d_scratch, L.bits), at<uint32_t>(d_scratch, L.wt),
+                        at<uint32_t>(d_scratch, L.wv), at<uint32_t>(d_scratch, L.act),
                         at<Info>(d_scratch, L.info), d_verts, vert_capacity, d_conn, tri_capacity,
                         d_rec_first, d_rec_second, d_rec_weight, num_sms(),
                         static_cast<cudaStream_t>(stream));
@@ -258,7 +331,7 @@ int dax_gb300_threshold_classify_count(const dax_gb300_uniform_grid* grid, const
 size_t dax_gb300_threshold_scratch_bytes(const dax_gb300_uniform_grid* grid) {
   Grid g;
   if (make_grid(grid, g)) return 0;
-  return layout(g, true).total;
+  return layout(g).total;
 }
 
 int dax_gb300_threshold_count(const dax_gb300_uniform_grid* grid, const float* d_field, float lo,
@@ -286,7 +359,7 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
   if ((!d_conn && cell_capacity > 0) || (!d_coords && point_capacity > 0) || cell_capacity < 0 ||
       point_capacity < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
-  const Layout L = layout(g, true);
+  const Layout L = layout(g);
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_threshold_scratch_bytes()");
   daxgb::launch_thr_emit(g, d_field, at<uint32_t>(d_scratch, L.bits),
@@ -306,6 +379,198 @@ int dax_gb300_cell_gradient(const dax_gb300_uniform_grid* grid, const float* d_f
   if (!d_field || !d_gradient) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or gradient");
   daxgb::launch_cell_gradient(g, d_field, d_gradient, num_sms(), static_cast<cudaStream_t>(stream));
   return check_launch("cell gradient kernel");
+}
+
+int dax_gb300_field_adjoint(const dax_gb300_uniform_grid* grid, const float* d_field,
+                            float isovalue, const void* d_scratch, size_t scratch_bytes,
+                            const float* d_grad_vertices, const float* d_grad_cell_gradient,
+                            float* d_grad_field, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!d_grad_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output");
+  if (!has_cells(g) || (!d_grad_vertices && !d_grad_cell_gradient)) {
+    cudaError_t e = cudaMemsetAsync(d_grad_field, 0, (size_t)g.P * sizeof(float), s);
+    return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing adjoint");
+  }
+  if (!d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field");
+  const McLayout L = mc_layout(g);
+  if (d_grad_vertices && (!d_scratch || scratch_bytes < L.total))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "vertex adjoint needs the dax_gb300_mc_count scratch");
+  void* sc = const_cast<void*>(d_scratch);
+  daxgb::launch_field_adjoint(g, d_field, isovalue, d_grad_vertices ? at<uint32_t>(sc, L.bits) : nullptr,
+                              d_grad_vertices ? at<uint32_t>(sc, L.wv) : nullptr,
+                              d_grad_vertices, d_grad_cell_gradient, d_grad_field, num_sms(), s);
+  return check_launch("field adjoint kernel");
+}
+
+int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids,
+                              const float* const* d_fields, const float* isovalues,
+                              dax_gb300_mc_batch** out) {
+  if (!out || num_grids < 1 || !grids || !d_fields || !isovalues)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "bad batch arguments");
+  *out = nullptr;
+  auto* b = new dax_gb300_mc_batch();
+  b->count = num_grids;
+  b->slots.resize(num_grids);
+  for (int i = 0; i < num_grids; ++i) {
+    Grid g;
+    int st = make_grid(&grids[i], g);
+    if (st) { delete b; return st; }
+    if (!has_cells(g)) { delete b; return fail(DAX_GB300_ERROR_BAD_VALUE, "batch grid without cells"); }
+    if (!d_fields[i]) { delete b; return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field in batch"); }
+    daxgb::GridSlot& sl = b->slots[i];
+    sl.g = g;
+    sl.field = d_fields[i];
+    sl.iso = isovalues[i];
+    sl.iso_hi = 0.0f;
+    sl.chunk0 = b->chunks;
+    sl.word0 = 4 * b->chunks;
+    sl.row0 = b->rows;
+    sl.blk0 = b->blocks;
+    sl.rw0 = b->rowwords;
+    b->rowwords += g.R * g.wr;
+    b->blocks += (long long)g.nz * ((g.ny + daxgb::kRowsPerEmitBlock - 1) / daxgb::kRowsPerEmitBlock);
+    b->chunks += (g.P + 127) / 128;
+    b->rows += g.R;
+    if (g.wr > b->max_wr) b->max_wr = g.wr;
+    b->aligned = b->aligned && aligned16(d_fields[i]);
+  }
+  b->words = 4 * b->chunks + 8;
+  b->tiles = daxgb::mc_scan_tiles(b->rowwords);
+  b->off_info = 0;
+  b->off_goff = align256(sizeof(Info));
+  b->off_status = align256(b->off_goff + 16 * (size_t)(num_grids + 1));
+  b->clear = align256(b->off_status + 3 * (size_t)b->tiles * 8);
+  b->off_wt = b->clear;
+  b->off_wv = align256(b->off_wt + 4 * (size_t)(b->rowwords + 1));
+  b->off_act = align256(b->off_wv + 4 * (size_t)(b->rowwords + 1));
+  b->off_bits = align256(b->off_act + 4 * (size_t)b->rowwords);
+  b->total = align256(b->off_bits + 4 * (size_t)b->words);
+  if (num_grids > 1) {
+    cudaError_t e = cudaMalloc(&b->d_slots, sizeof(daxgb::GridSlot) * num_grids);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_slots, b->slots.data(), sizeof(daxgb::GridSlot) * num_grids,
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      if (b->d_slots) cudaFree(b->d_slots);
+      delete b;
+      return e == cudaErrorMemoryAllocation ? fail(DAX_GB300_ERROR_OUT_OF_MEMORY, "batch table")
+                                            : cuda_fail(e, "uploading batch table");
+    }
+  }
+  *out = b;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_mc_batch_destroy(dax_gb300_mc_batch* b) {
+  if (!b) return DAX_GB300_SUCCESS;
+  if (b->d_slots) cudaFree(b->d_slots);
+  delete b;
+  return DAX_GB300_SUCCESS;
+}
+
+size_t dax_gb300_mc_batch_scratch_bytes(const dax_gb300_mc_batch* b) { return b ? b->total : 0; }
+
+int dax_gb300_mc_batch_count(dax_gb300_mc_batch* b, void* d_scratch, size_t scratch_bytes,
+                             void* stream) {
+  if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
+  if (scratch_bytes < b->total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(d_scratch, 0, b->clear, s);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
+  const daxgb::GridSet S = b->set();
+  uint32_t* bits = at<uint32_t>(d_scratch, b->off_bits);
+  daxgb::launch_classify_bits(0, S, b->aligned, bits, b->words, num_sms(), s);
+  int st = check_launch("batch classify kernel");
+  if (st) return st;
+  daxgb::launch_mc_scan(S, bits, at<uint32_t>(d_scratch, b->off_wt),
+                        at<uint32_t>(d_scratch, b->off_wv), at<uint32_t>(d_scratch, b->off_act),
+                        at<unsigned long long>(d_scratch, b->off_status),
+                        at<Info>(d_scratch, b->off_info), b->tiles, num_sms(), s);
+  if ((st = check_launch("batch row count/scan kernel"))) return st;
+  daxgb::launch_grid_offsets(S, at<uint32_t>(d_scratch, b->off_wt),
+                             at<uint32_t>(d_scratch, b->off_wv),
+                             at<long long>(d_scratch, b->off_goff), s);
+  return check_launch("batch offsets kernel");
+}
+
+int dax_gb300_mc_batch_totals(const dax_gb300_mc_batch* b, const void* d_scratch,
+                              int64_t* tri_offsets, int64_t* vert_offsets, void* stream) {
+  if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<long long> h(2 * (size_t)(b->count + 1));
+  cudaError_t e = cudaMemcpyAsync(h.data(), static_cast<const char*>(d_scratch) + b->off_goff,
+                                  h.size() * 8, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "reading batch offsets");
+  int st = read_totals(d_scratch, nullptr, nullptr, s);
+  for (int i = 0; i <= b->count; ++i) {
+    if (tri_offsets) tri_offsets[i] = h[2 * i];
+    if (vert_offsets) vert_offsets[i] = h[2 * i + 1];
+  }
+  return st;
+}
+
+int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* b, int merge, void* d_scratch,
+                                size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                                int32_t* d_conn, int64_t tri_capacity, void* stream) {
+  if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
+  if (scratch_bytes < b->total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
+  if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
+  daxgb::launch_mc_emit(b->set(), merge != 0, at<uint32_t>(d_scratch, b->off_bits),
+                        at<uint32_t>(d_scratch, b->off_wt), at<uint32_t>(d_scratch, b->off_wv),
+                        at<uint32_t>(d_scratch, b->off_act),
+                        at<Info>(d_scratch, b->off_info), d_verts, vert_capacity, d_conn,
+                        tri_capacity, nullptr, nullptr, nullptr, num_sms(),
+                        static_cast<cudaStream_t>(stream));
+  return check_launch("batch generate kernel");
+}
+
+int dax_gb300_mc_batch_capture(dax_gb300_mc_batch* b, int merge, void* d_scratch,
+                               size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                               int32_t* d_conn, int64_t tri_capacity, void** graph) {
+  if (!graph) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL graph handle");
+  *graph = nullptr;
+  cudaStream_t s;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "creating capture stream");
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(s);
+    return cuda_fail(e, "begin capture");
+  }
+  int st = dax_gb300_mc_batch_count(b, d_scratch, scratch_bytes, s);
+  if (!st)
+    st = dax_gb300_mc_batch_generate(b, merge, d_scratch, scratch_bytes, d_verts, vert_capacity,
+                                     d_conn, tri_capacity, s);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(s, &g);
+  cudaStreamDestroy(s);
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "end capture");
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "instantiate graph");
+  *graph = ex;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_graph_launch(void* graph, void* stream) {
+  if (!graph) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL graph");
+  cudaError_t e = cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph),
+                                  static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "graph launch");
+}
+
+int dax_gb300_graph_destroy(void* graph) {
+  if (graph) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph));
+  return DAX_GB300_SUCCESS;
 }
 
 }  // extern "C"

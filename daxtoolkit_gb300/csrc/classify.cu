@@ -21,45 +21,92 @@ __device__ __forceinline__ uint32_t classify_point(float v, float a, float b) {
 }
 
 // Each warp-chunk covers 128 points = 4 bit words.  UNROLL chunks per warp
-// step keep several 512 B loads in flight per warp.
+// step keep several 512 B loads in flight per warp.  Chunks are global over
+// the grid set; each grid's chunks start on a fresh chunk, so a chunk never
+// straddles two grids and each grid's bits start on a word boundary.
 template <int MODE, bool VEC>
-__global__ void __launch_bounds__(256) k_classify_bits(const float* __restrict__ f, long long P,
-                                                       float a, float b,
-                                                       uint32_t* __restrict__ bits,
+__global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __restrict__ bits,
                                                        long long nwords) {
   constexpr int UNROLL = 4;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long nchunks = (P + 127) >> 7;
-  for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
-    float4 v[UNROLL];
+  const long long nchunks = S.chunks;
+  const float nan = __int_as_float(0x7fc00000);  // classifies as 0 in both modes
+  if (S.count == 1) {
+    // one grid: field pointer and thresholds are loop invariants
+    const float* __restrict__ f = S.one.field;
+    const long long P = S.one.g.P;
+    const float a = S.one.iso, b = S.one.iso_hi;
+    for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
+      float4 v[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const long long c = c0 + u;
-      const long long base = (c << 7) + lane * 4;
-      if (VEC && base + 3 < P) {
-        v[u] = __ldcs(reinterpret_cast<const float4*>(f + base));
-      } else {
-        // tail / unaligned path: NaN classifies as 0 in both modes
-        const float nan = __int_as_float(0x7fc00000);
-        v[u].x = (c < nchunks && base + 0 < P) ? __ldcs(f + base + 0) : nan;
-        v[u].y = (c < nchunks && base + 1 < P) ? __ldcs(f + base + 1) : nan;
-        v[u].z = (c < nchunks && base + 2 < P) ? __ldcs(f + base + 2) : nan;
-        v[u].w = (c < nchunks && base + 3 < P) ? __ldcs(f + base + 3) : nan;
+      for (int u = 0; u < UNROLL; ++u) {
+        const long long base = ((c0 + u) << 7) + lane * 4;
+        if (VEC && base + 3 < P) {
+          v[u] = __ldcs(reinterpret_cast<const float4*>(f + base));
+        } else {
+          v[u].x = base + 0 < P ? __ldcs(f + base + 0) : nan;
+          v[u].y = base + 1 < P ? __ldcs(f + base + 1) : nan;
+          v[u].z = base + 2 < P ? __ldcs(f + base + 2) : nan;
+          v[u].w = base + 3 < P ? __ldcs(f + base + 3) : nan;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint32_t nib = classify_point<MODE>(v[u].x, a, b) |
+                             (classify_point<MODE>(v[u].y, a, b) << 1) |
+                             (classify_point<MODE>(v[u].z, a, b) << 2) |
+                             (classify_point<MODE>(v[u].w, a, b) << 3);
+        uint32_t w = nib << (4 * (lane & 7));
+        w |= __shfl_xor_sync(kFull, w, 1);
+        w |= __shfl_xor_sync(kFull, w, 2);
+        w |= __shfl_xor_sync(kFull, w, 4);
+        if ((lane & 7) == 0 && c0 + u < nchunks) bits[((c0 + u) << 2) + (lane >> 3)] = w;
       }
     }
+  } else {
+    for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
+      float4 v[UNROLL];
+      float a[UNROLL], b[UNROLL];
+      long long wout[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const long long c = c0 + u;
-      uint32_t nib = classify_point<MODE>(v[u].x, a, b) | (classify_point<MODE>(v[u].y, a, b) << 1) |
-                     (classify_point<MODE>(v[u].z, a, b) << 2) |
-                     (classify_point<MODE>(v[u].w, a, b) << 3);
-      uint32_t w = nib << (4 * (lane & 7));
-      w |= __shfl_xor_sync(kFull, w, 1);
-      w |= __shfl_xor_sync(kFull, w, 2);
-      w |= __shfl_xor_sync(kFull, w, 4);
-      if ((lane & 7) == 0 && c < nchunks) bits[(c << 2) + (lane >> 3)] = w;
+      for (int u = 0; u < UNROLL; ++u) {
+        const long long c = c0 + u;
+        v[u] = make_float4(nan, nan, nan, nan);
+        a[u] = b[u] = 0.0f;
+        wout[u] = -1;
+        if (c < nchunks) {
+          const GridSlot& sl = S.slots[slot_of_chunk(S, c)];
+          const long long lc = c - sl.chunk0;
+          const long long base = (lc << 7) + lane * 4;
+          const float* f = sl.field;
+          const long long P = sl.g.P;
+          a[u] = sl.iso;
+          b[u] = sl.iso_hi;
+          wout[u] = sl.word0 + (lc << 2);
+          if (VEC && base + 3 < P) {
+            v[u] = __ldcs(reinterpret_cast<const float4*>(f + base));
+          } else {
+            if (base + 0 < P) v[u].x = __ldcs(f + base + 0);
+            if (base + 1 < P) v[u].y = __ldcs(f + base + 1);
+            if (base + 2 < P) v[u].z = __ldcs(f + base + 2);
+            if (base + 3 < P) v[u].w = __ldcs(f + base + 3);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint32_t nib = classify_point<MODE>(v[u].x, a[u], b[u]) |
+                             (classify_point<MODE>(v[u].y, a[u], b[u]) << 1) |
+                             (classify_point<MODE>(v[u].z, a[u], b[u]) << 2) |
+                             (classify_point<MODE>(v[u].w, a[u], b[u]) << 3);
+        uint32_t w = nib << (4 * (lane & 7));
+        w |= __shfl_xor_sync(kFull, w, 1);
+        w |= __shfl_xor_sync(kFull, w, 2);
+        w |= __shfl_xor_sync(kFull, w, 4);
+        if ((lane & 7) == 0 && wout[u] >= 0) bits[wout[u] + (lane >> 3)] = w;
+      }
     }
   }
   // zero the padding words after the last chunk (read by unaligned fetches)
@@ -69,20 +116,20 @@ __global__ void __launch_bounds__(256) k_classify_bits(const float* __restrict__
   }
 }
 
-void launch_classify_bits(int mode, const float* f, long long P, float a, float b, uint32_t* bits,
+void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
                           long long nwords, int num_sms, cudaStream_t s) {
-  const long long nchunks = (P + 127) >> 7;
-  const long long want = (nchunks + 4 * 8 - 1) / (4 * 8);  // blocks of 8 warps x 4 chunks
-  const long long cap = (long long)num_sms * 8;
-  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
-  const bool vec = (reinterpret_cast<uintptr_t>(f) & 15) == 0;
-  if (mode == 0) {
-    if (vec) k_classify_bits<0, true><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
-    else k_classify_bits<0, false><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
-  } else {
-    if (vec) k_classify_bits<1, true><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
-    else k_classify_bits<1, false><<<blocks, 256, 0, s>>>(f, P, a, b, bits, nwords);
+  const long long want = (S.chunks + 4 * 8 - 1) / (4 * 8);  // blocks of 8 warps x 4 chunks
+#define DAXGB_K1(M, V)                                                         \
+  {                                                                            \
+    const int blocks = resident_blocks(k_classify_bits<M, V>, 256, 0, num_sms, want); \
+    k_classify_bits<M, V><<<blocks, 256, 0, s>>>(S, bits, nwords);             \
   }
+  if (mode == 0) {
+    if (all_aligned) DAXGB_K1(0, true) else DAXGB_K1(0, false)
+  } else {
+    if (all_aligned) DAXGB_K1(1, true) else DAXGB_K1(1, false)
+  }
+#undef DAXGB_K1
 }
 
 // ---- per-cell count arrays (the Dax count handles) ---------------------

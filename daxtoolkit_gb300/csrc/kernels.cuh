@@ -12,7 +12,8 @@ namespace daxgb {
 // that unaligned 64-bit fetches may touch.
 inline long long bit_words(long long P) { return ((P + 127) / 128) * 4 + 8; }
 
-constexpr int kRowsPerTile = 256;   // rows per look-back tile in K2
+constexpr int kRowsPerTile = 256;      // rows per look-back tile in K2
+constexpr int kRowsPerEmitBlock = 8;   // rows per block in K3 (one warp each)
 
 // Lanes that cooperate on one point row in K2/K3: the power of two >= the
 // row's word count, at most a warp.
@@ -22,17 +23,58 @@ inline int lanes_per_row(int wr) {
   return g;
 }
 
-void launch_classify_bits(int mode, const float* f, long long P, float a, float b, uint32_t* bits,
+// A GridSet holding one grid (no device table).
+inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
+  GridSet S{};
+  S.slots = nullptr;
+  S.count = 1;
+  S.rows = g.R;
+  S.chunks = (g.P + 127) / 128;
+  S.blocks = (long long)g.nz * ((g.ny + kRowsPerEmitBlock - 1) / kRowsPerEmitBlock);
+  S.rowwords = g.R * g.wr;
+  S.one.g = g;
+  S.one.field = field;
+  S.one.iso = a;
+  S.one.iso_hi = b;
+  S.one.chunk0 = 0;
+  S.one.word0 = 0;
+  S.one.row0 = 0;
+  S.one.blk0 = 0;
+  S.one.rw0 = 0;
+  return S;
+}
+
+void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
                           long long nwords, int num_sms, cudaStream_t s);
 void launch_cell_count(int mode, const Grid& g, const float* f, float a, float b, int32_t* count,
                        uint8_t* cases, int num_sms, cudaStream_t s);
 
-void launch_mc_rows(const Grid& g, const uint32_t* bits, long long* row_t, long long* row_v,
-                    unsigned long long* status, Info* info, int tiles, cudaStream_t s);
-void launch_mc_emit(const Grid& g, const float* f, float iso, bool merge, const uint32_t* bits,
-                    const long long* row_t, const long long* row_v, Info* info, float* verts,
+// Blocks of a grid-stride kernel that are resident at once on `num_sms` SMs
+// (never more than `want`): one wave, no tail.
+template <typename K>
+inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long long want) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const long long cap = (long long)num_sms * per_sm;
+  return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+// Marching cubes over row words: K2 (count + scan) writes per-word exclusive
+// triangle / vertex offsets wt, wv (uint32[rowwords + 1]) and the compacted
+// list of active words act (uint32[rowwords]); K3 emits from them.
+int mc_scan_tiles(long long rowwords);
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wt, uint32_t* wv,
+                    uint32_t* act, unsigned long long* status, Info* info, int tiles, int num_sms,
+                    cudaStream_t s);
+void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const uint32_t* wt,
+                    const uint32_t* wv, const uint32_t* act, Info* info, float* verts,
                     long long vcap, int32_t* conn, long long tcap, int32_t* ra, int32_t* rb,
                     float* rw, int num_sms, cudaStream_t s);
+// goff[2g], goff[2g+1]: first triangle / merged vertex of grid g; then totals.
+void launch_grid_offsets(const GridSet& S, const uint32_t* wt, const uint32_t* wv,
+                         long long* goff, cudaStream_t s);
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s);
 
@@ -43,6 +85,10 @@ void launch_thr_emit(const Grid& g, const float* f, const uint32_t* bits, const 
                      const long long* row_k, const long long* row_u, Info* info, int32_t* conn,
                      long long kcap, float* coords, float* fout, long long ucap, int num_sms,
                      cudaStream_t s);
+
+void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32_t* bits,
+                          const uint32_t* wv, const float* dverts, const float* dgrad,
+                          float* out, int num_sms, cudaStream_t s);
 
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s);
 

@@ -1,23 +1,29 @@
 // Marching cubes on the classification bit stream.
 //
-// K2 (k_mc_rows): for every point row r = (j, k)
-//     T[r] = triangles of cell row r      = sum NumFaces[case(i)]
-//     V[r] = crossing edges owned by row r = edges (p, p + e_axis) whose end
-//            points classify differently, axis x < y < z
-//   then a single-pass decoupled look-back scan over tiles of 256 rows turns
-//   them into exclusive row offsets.  V counts exactly the vertices of the
-//   merged output: a cell's triangle-table row references exactly its
-//   sign-change edges, every grid edge belongs to a cell, and the reference's
-//   merged order, ascending (first id, second id), is ascending (owner point,
-//   axis) on a uniform grid -- i.e. row order, then x, then axis.  So the
-//   reference's Sort/Unique/LowerBounds
-//   (dax/cont/DispatcherGenerateInterpolatedCells.h:276-291) becomes a rank.
+// Work is indexed by "row words": word m of point row r covers points
+// i = 32m .. 32m+31 of that row (and the cells whose first point they are);
+// row words are numbered r * wr + m, which is point order.
 //
-// K3 (k_mc_emit): for every row with output, recompute cases from the bits,
-//   write vertices at V-offset + rank and triangles at T-offset + rank; a
-//   triangle corner's vertex id is the row offset of the edge's owner row
-//   plus the edge's rank inside that row.  Field values are read only at
-//   crossing-edge end points.
+// K2 (k_mc_scan): for every row word
+//     T = triangles of its cells            = sum NumFaces[case(i)]
+//     V = crossing edges its points own      = edges (p, p + e_axis) whose end
+//         points classify differently, axis x < y < z
+//     A = 1 if T or V is non-zero
+//   and a single-pass decoupled look-back scan (three chains) over tiles of
+//   1024 words turns them into exclusive offsets per word plus a compacted
+//   list of the active words.  V counts exactly the vertices of the merged
+//   output: a cell's triangle-table row references exactly its sign-change
+//   edges, every grid edge belongs to a cell, and the reference's merged
+//   order, ascending (first id, second id), is ascending (owner point, axis)
+//   on a uniform grid -- point order, then axis.  So the reference's
+//   Sort/Unique/LowerBounds (dax/cont/DispatcherGenerateInterpolatedCells.h:
+//   276-291) becomes a rank: offset of the owner word + popcount.
+//
+// K3 (k_mc_emit): one thread per ACTIVE word (from the compacted list):
+//   recompute cases from the bits, write the word's vertices at its V offset
+//   and its cells' triangles at its T offset; a triangle corner's vertex id
+//   is the V offset of the edge's owner word plus the edge's rank inside it.
+//   Field values are read only at crossing-edge end points.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mc_case.cuh"
@@ -83,103 +89,125 @@ __device__ __forceinline__ void crossing_masks(const Grid& g, const uint32_t* bi
 }
 
 // ---------------------------------------------------------------------------
-// K2: per-row counts + look-back scan.  256 rows per tile, G lanes per row.
-template <int G>
-__global__ void __launch_bounds__(256) k_mc_rows(Grid g, const uint32_t* __restrict__ bits,
-                                                 long long* __restrict__ row_t,
-                                                 long long* __restrict__ row_v,
-                                                 unsigned long long* __restrict__ status,
-                                                 Info* __restrict__ info, int tiles) {
-  constexpr int RT = kRowsPerTile;
-  constexpr int GPB = 256 / G;
-  __shared__ int s_tile;
-  __shared__ int s_t[RT], s_v[RT];
-  __shared__ long long s_wt[8], s_wv[8];
-  __shared__ long long s_ex[2];
-  if (threadIdx.x == 0) s_tile = (int)atomicAdd(&info->ticket, 1u);
-  __syncthreads();
-  const int tile = s_tile;
-  const long long r0 = (long long)tile * RT;
-  const int gl = threadIdx.x & (G - 1);
-  const int grp = threadIdx.x / G;
-  for (int lr = grp; lr < RT; lr += GPB) {
-    const long long r = r0 + lr;
-    int t = 0, v = 0;
-    if (r < g.R) {
-      const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-      const bool cells = (j < g.ny - 1) && (k < g.nz - 1);
-      for (int m = gl; m < g.wr; m += G) {
-        uint32_t X, Y, Z;
-        crossing_masks(g, bits, j, k, m, X, Y, Z);
-        v += __popc(X) + __popc(Y) + __popc(Z);
-        if (cells) {
-          const long long pos = r * g.nx + 32ll * m;
-          const CornerWords w = corner_words(g, bits, pos);
-          uint32_t act = active_cells(w, low_mask(g.nx - 1 - 32 * m));
-          while (act) {
-            const int q = __ffs(act) - 1;
-            act &= act - 1;
-            t += mc_num_tris(case_of(w, q));
-          }
-        }
-      }
+// K2: counts per row word + three-chain look-back scan.
+
+// Triangle and crossing-edge counts of word m of row r.  Eight word fetches
+// per 32 points: (a, a+x) of the four rows (j..j+1, k..k+1).
+__device__ __forceinline__ void mc_word_counts(const Grid& g, const uint32_t* bits, long long r,
+                                               int m, int& t, int& v) {
+  const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+  const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+  const long long pos = r * g.nx + 32ll * m;
+  const uint32_t pmask = low_mask(g.nx - 32 * m);
+  const uint32_t xmask = low_mask(g.nx - 1 - 32 * m);
+  CornerWords w{};
+  bits_at2(bits, pos, w.a, w.a1);
+  if (hy) bits_at2(bits, pos + dy, w.b, w.b1);
+  if (hz) bits_at2(bits, pos + dz, w.c, w.c1);
+  if (hy && hz) bits_at2(bits, pos + dy + dz, w.d, w.d1);
+  v = __popc((w.a ^ w.a1) & xmask);
+  if (hy) v += __popc((w.a ^ w.b) & pmask);
+  if (hz) v += __popc((w.a ^ w.c) & pmask);
+  t = 0;
+  if (hy && hz) {
+    uint32_t act = active_cells(w, xmask);
+    while (act) {
+      const int q = __ffs(act) - 1;
+      act &= act - 1;
+      t += mc_num_tris(case_of(w, q));
     }
-    t = group_sum(t, G);
-    v = group_sum(v, G);
-    if (gl == 0) {
-      s_t[lr] = t;
-      s_v[lr] = v;
-    }
-  }
-  __syncthreads();
-  // block-wide exclusive scan, thread tid <-> row r0 + tid
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long t0 = s_t[tid], v0 = s_v[tid];
-  long long ti = t0, vi = v0;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long ut = __shfl_up_sync(kFull, ti, o), uv = __shfl_up_sync(kFull, vi, o);
-    if (lane >= o) { ti += ut; vi += uv; }
-  }
-  if (lane == 31) { s_wt[warp] = ti; s_wv[warp] = vi; }
-  __syncthreads();
-  long long wt = 0, wv = 0, aggt = 0, aggv = 0;
-#pragma unroll
-  for (int w = 0; w < 8; ++w) {
-    if (w < warp) { wt += s_wt[w]; wv += s_wv[w]; }
-    aggt += s_wt[w];
-    aggv += s_wv[w];
-  }
-  if (warp == 0) s_ex[0] = warp_lookback(status, tile, aggt, &info->error);
-  if (warp == 1) s_ex[1] = warp_lookback(status + tiles, tile, aggv, &info->error);
-  __syncthreads();
-  const long long r = r0 + tid;
-  if (r < g.R) {
-    row_t[r] = s_ex[0] + wt + ti - t0;
-    row_v[r] = s_ex[1] + wv + vi - v0;
-  }
-  if (tile == tiles - 1 && tid == 0) {
-    row_t[g.R] = s_ex[0] + aggt;
-    row_v[g.R] = s_ex[1] + aggv;
-    info->total_a = s_ex[0] + aggt;
-    info->total_b = s_ex[1] + aggv;
   }
 }
 
-void launch_mc_rows(const Grid& g, const uint32_t* bits, long long* row_t, long long* row_v,
-                    unsigned long long* status, Info* info, int tiles, cudaStream_t s) {
-  switch (lanes_per_row(g.wr)) {
-    case 1: k_mc_rows<1><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
-    case 2: k_mc_rows<2><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
-    case 4: k_mc_rows<4><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
-    case 8: k_mc_rows<8><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
-    case 16: k_mc_rows<16><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
-    default: k_mc_rows<32><<<tiles, 256, 0, s>>>(g, bits, row_t, row_v, status, info, tiles); break;
+constexpr int kWordsPerThread = 4;
+constexpr int kWordsPerTile = 256 * kWordsPerThread;
+
+__device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int& si, long long& r,
+                                            int& m) {
+  si = S.count == 1 ? 0 : slot_of_rowword(S, gw);
+  const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+  const long long lw = gw - sl.rw0;
+  r = lw / sl.g.wr;
+  m = (int)(lw - r * sl.g.wr);
+}
+
+__global__ void __launch_bounds__(256) k_mc_scan(GridSet S, const uint32_t* __restrict__ bits,
+                                                 uint32_t* __restrict__ wt,
+                                                 uint32_t* __restrict__ wv,
+                                                 uint32_t* __restrict__ act,
+                                                 unsigned long long* __restrict__ status,
+                                                 Info* __restrict__ info, int tiles) {
+  __shared__ int s_tile;
+  const int tid = threadIdx.x;
+  while (true) {
+    if (tid == 0) s_tile = (int)atomicAdd(&info->ticket, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= tiles) break;
+    const long long w0 = (long long)tile * kWordsPerTile + (long long)tid * kWordsPerThread;
+    int tc[kWordsPerThread], vc[kWordsPerThread];
+#pragma unroll
+    for (int e = 0; e < kWordsPerThread; ++e) {
+      tc[e] = vc[e] = 0;
+      const long long gw = w0 + e;
+      if (gw < S.rowwords) {
+        int si, m;
+        long long r;
+        locate_word(S, gw, si, r, m);
+        const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+        if (sl.g.nx >= 2 && sl.g.ny >= 2 && sl.g.nz >= 2)
+          mc_word_counts(sl.g, bits + sl.word0, r, m, tc[e], vc[e]);
+      }
+    }
+    long long mine[3] = {0, 0, 0};
+#pragma unroll
+    for (int e = 0; e < kWordsPerThread; ++e) {
+      mine[0] += tc[e];
+      mine[1] += vc[e];
+      mine[2] += (tc[e] | vc[e]) ? 1 : 0;
+    }
+    long long ex[3], agg[3], base[3];
+    block_exclusive_scan<3>(mine, ex, agg);
+    block_lookback<3>(status, tiles, tile, agg, &info->error, base);
+    long long ot = base[0] + ex[0], ov = base[1] + ex[1], oa = base[2] + ex[2];
+#pragma unroll
+    for (int e = 0; e < kWordsPerThread; ++e) {
+      const long long gw = w0 + e;
+      if (gw < S.rowwords) {
+        wt[gw] = (uint32_t)ot;
+        wv[gw] = (uint32_t)ov;
+        if (tc[e] | vc[e]) act[oa++] = (uint32_t)gw;
+      }
+      ot += tc[e];
+      ov += vc[e];
+    }
+    if (tile == tiles - 1 && tid == 0) {
+      const long long T = base[0] + agg[0], V = base[1] + agg[1], A = base[2] + agg[2];
+      wt[S.rowwords] = (uint32_t)T;
+      wv[S.rowwords] = (uint32_t)V;
+      info->total_a = T;
+      info->total_b = V;
+      info->total_c = A;
+      if (T > 2147483647ll || V > 2147483647ll) atomicOr(&info->error, kErrOverflow);
+    }
   }
+}
+
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wt, uint32_t* wv,
+                    uint32_t* act, unsigned long long* status, Info* info, int tiles, int num_sms,
+                    cudaStream_t s) {
+  const int blocks = resident_blocks(k_mc_scan, 256, 0, num_sms, tiles);
+  k_mc_scan<<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, status, info, tiles);
+}
+
+int mc_scan_tiles(long long rowwords) {
+  return (int)((rowwords + kWordsPerTile - 1) / kWordsPerTile);
 }
 
 // ---------------------------------------------------------------------------
-// K3: emit.  One group of G lanes per row, rows in a grid-stride loop.
+// K3: emit, one thread per active row word.
 
 // Vertex on the edge owned by point (i, j, k) along `axis`:
 // weight = (iso - f[A]) / (f[B] - f[A]) (dax/worklet/MarchingCubes.h:160-161),
@@ -206,169 +234,166 @@ __device__ __forceinline__ void emit_vertex(const Grid& g, const float* __restri
   if (rw) rw[vid] = w;
 }
 
-template <int G, bool MERGE>
-__global__ void __launch_bounds__(256) k_mc_emit(Grid g, const float* __restrict__ f, float iso,
-                                                 const uint32_t* __restrict__ bits,
-                                                 const long long* __restrict__ row_t,
-                                                 const long long* __restrict__ row_v,
+// Crossing masks of one owner word plus its global vertex offset.
+struct OwnerWord {
+  uint32_t X, Y, Z;
+  long long base;
+};
+
+__device__ __forceinline__ OwnerWord owner_word(const Grid& g, const uint32_t* bits,
+                                                const uint32_t* wv_grid, int jq, int kq, int wq) {
+  const long long rq = (long long)kq * g.ny + jq;
+  const long long pos = rq * g.nx + 32ll * wq;
+  uint32_t a, a1;
+  bits_at2(bits, pos, a, a1);
+  const uint32_t pm = low_mask(g.nx - 32 * wq);
+  OwnerWord o;
+  o.X = (a ^ a1) & low_mask(g.nx - 1 - 32 * wq);
+  o.Y = jq < g.ny - 1 ? (a ^ bits_at(bits, pos + g.nx)) & pm : 0u;
+  o.Z = kq < g.nz - 1 ? (a ^ bits_at(bits, pos + (long long)g.nx * g.ny)) & pm : 0u;
+  o.base = __ldg(wv_grid + rq * g.wr + wq);
+  return o;
+}
+
+__device__ __forceinline__ long long owner_rank_id(const OwnerWord& o, int b, int axis) {
+  const uint32_t lm = (1u << b) - 1u;
+  long long id = o.base + __popc(o.X & lm) + __popc(o.Y & lm) + __popc(o.Z & lm);
+  if (axis >= 1) id += (o.X >> b) & 1u;
+  if (axis >= 2) id += (o.Y >> b) & 1u;
+  return id;
+}
+
+template <bool MERGE>
+__global__ void __launch_bounds__(256) k_mc_emit(GridSet S, const uint32_t* __restrict__ bits,
+                                                 const uint32_t* __restrict__ wt,
+                                                 const uint32_t* __restrict__ wv,
+                                                 const uint32_t* __restrict__ act,
                                                  Info* __restrict__ info,
                                                  float* __restrict__ verts, long long vcap,
                                                  int32_t* __restrict__ conn, long long tcap,
                                                  int32_t* __restrict__ ra, int32_t* __restrict__ rb,
                                                  float* __restrict__ rw) {
-  constexpr int GPB = 256 / G;
-  extern __shared__ uint32_t s_rows[];  // [GPB][4 rows][X, Y, Z, prefix][wr]
-  {
-    const long long T = info->total_a;
-    const long long V = MERGE ? info->total_b : 3 * T;
-    if (T > tcap || V > vcap) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&info->error, kErrCapacity);
-      return;
-    }
+  const long long T = info->total_a;
+  const long long V = MERGE ? info->total_b : 3 * T;
+  const long long A = info->total_c;
+  if (T > tcap || V > vcap || (info->error & (kErrOverflow | kErrTimeout))) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
+      atomicOr(&info->error, kErrCapacity);
+    return;
   }
-  const int gl = threadIdx.x & (G - 1);
-  const int grp = threadIdx.x / G;
-  const int wr = g.wr;
-  uint32_t* sm = s_rows + (size_t)grp * 16 * wr;
-  const long long ngroups = (long long)gridDim.x * GPB;
-  for (long long r = (long long)blockIdx.x * GPB + grp; r < g.R; r += ngroups) {
-    const long long vb = row_v[r], ve = row_v[r + 1];
-    const long long tb = row_t[r], te = row_t[r + 1];
-    if (vb == ve && tb == te) continue;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long ai = (long long)blockIdx.x * blockDim.x + threadIdx.x; ai < A; ai += stride) {
+    const long long gw = __ldg(act + ai);
+    int si, m;
+    long long r;
+    locate_word(S, gw, si, r, m);
+    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+    const Grid& g = sl.g;
+    const uint32_t* gb = bits + sl.word0;
+    const uint32_t* wvg = wv + sl.rw0;
+    const float* f = sl.field;
+    const float iso = sl.iso;
+    const long long t0 = __ldg(wt + gw), t1 = __ldg(wt + gw + 1);
+    const long long v0 = __ldg(wv + gw), v1 = __ldg(wv + gw + 1);
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    long long qbase[4] = {vb, 0, 0, 0};
+    const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+    const long long pos = r * g.nx + 32ll * m;
+    const uint32_t pmask = low_mask(g.nx - 32 * m);
+    const uint32_t xmask = low_mask(g.nx - 1 - 32 * m);
+    const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+    CornerWords w{};
+    bits_at2(gb, pos, w.a, w.a1);
+    if (hy) bits_at2(gb, pos + dy, w.b, w.b1);
+    if (hz) bits_at2(gb, pos + dz, w.c, w.c1);
+    if (hy && hz) bits_at2(gb, pos + dy + dz, w.d, w.d1);
+    if (MERGE && v1 > v0) {
+      const uint32_t X = (w.a ^ w.a1) & xmask;
+      const uint32_t Y = hy ? (w.a ^ w.b) & pmask : 0u;
+      const uint32_t Z = hz ? (w.a ^ w.c) & pmask : 0u;
+      long long vid = v0;
+      for (uint32_t u = X | Y | Z; u; u &= u - 1) {
+        const int q = __ffs(u) - 1;
+        const int i = 32 * m + q;
+        if ((X >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 0, vid++, verts, ra, rb, rw);
+        if ((Y >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 1, vid++, verts, ra, rb, rw);
+        if ((Z >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 2, vid++, verts, ra, rb, rw);
+      }
+    }
+    if (t1 == t0) continue;
+    // first vertex of this grid in the concatenated output (0 for one grid)
+    const long long vbase0 = S.count == 1 ? 0 : (MERGE ? (long long)__ldg(wv + sl.rw0)
+                                                       : 3ll * __ldg(wt + sl.rw0));
+    OwnerWord ow[4];
     if (MERGE) {
-      // crossing masks + in-row prefix for the owner rows (j..j+1, k..k+1)
-      const int nq = (te > tb) ? 4 : 1;
-      for (int qi = 0; qi < nq; ++qi) {
-        const int jq = j + (qi & 1), kq = k + (qi >> 1);
-        if (qi) qbase[qi] = row_v[(long long)kq * g.ny + jq];
-        int carry = 0;
-        for (int m0 = 0; m0 < wr; m0 += G) {
-          const int m = m0 + gl;
-          uint32_t X = 0, Y = 0, Z = 0;
-          if (m < wr) crossing_masks(g, bits, jq, kq, m, X, Y, Z);
-          const int cnt = __popc(X) + __popc(Y) + __popc(Z);
-          const int incl = group_inclusive_scan(cnt, G);
-          if (m < wr) {
-            uint32_t* q = sm + qi * 4 * wr;
-            q[m] = X;
-            q[wr + m] = Y;
-            q[2 * wr + m] = Z;
-            q[3 * wr + m] = (uint32_t)(carry + incl - cnt);
-          }
-          carry += group_last(incl, G);
-        }
-      }
-      __syncwarp(group_mask(G));
-      // vertices owned by row r
-      if (ve > vb) {
-        for (int m = gl; m < wr; m += G) {
-          const uint32_t X = sm[m], Y = sm[wr + m], Z = sm[2 * wr + m];
-          long long vid = vb + sm[3 * wr + m];
-          uint32_t u = X | Y | Z;
-          while (u) {
-            const int q = __ffs(u) - 1;
-            u &= u - 1;
-            const int i = 32 * m + q;
-            if ((X >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 0, vid++, verts, ra, rb, rw);
-            if ((Y >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 1, vid++, verts, ra, rb, rw);
-            if ((Z >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 2, vid++, verts, ra, rb, rw);
-          }
-        }
-      }
-    }
-    if (te > tb) {
-      long long carry = 0;
-      const long long pos0 = r * g.nx;
-      for (int m0 = 0; m0 < wr; m0 += G) {
-        const int m = m0 + gl;
-        CornerWords w{};
-        uint32_t act = 0;
-        int cnt = 0;
-        if (m < wr) {
-          w = corner_words(g, bits, pos0 + 32ll * m);
-          act = active_cells(w, low_mask(g.nx - 1 - 32 * m));
-          for (uint32_t u = act; u; u &= u - 1) cnt += mc_num_tris(case_of(w, __ffs(u) - 1));
-        }
-        const int incl = group_inclusive_scan(cnt, G);
-        long long tid = tb + carry + incl - cnt;
-        for (uint32_t u = act; u; u &= u - 1) {
-          const int q = __ffs(u) - 1;
-          const int i = 32 * m + q;
-          const uint64_t cw = kMcCase[case_of(w, q)];
-          const int nt = (int)(cw >> 60);
-          for (int tt = 0; tt < nt; ++tt, ++tid) {
 #pragma unroll
-            for (int corner = 0; corner < 3; ++corner) {
-              const int e = mc_edge(cw, 3 * tt + corner);
-              const int info_e = kEdgeOwner[e];
-              const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
-              const int axis = info_e >> 3;
-              if (MERGE) {
-                const int qi = dj + 2 * dk;
-                const int ii = i + di;
-                const int wq = ii >> 5, bq = ii & 31;
-                const uint32_t* qs = sm + qi * 4 * wr;
-                const uint32_t lm = (1u << bq) - 1u;
-                const uint32_t X = qs[wq], Y = qs[wr + wq], Z = qs[2 * wr + wq];
-                int rank = (int)qs[3 * wr + wq] + __popc(X & lm) + __popc(Y & lm) + __popc(Z & lm);
-                if (axis >= 1) rank += (X >> bq) & 1u;
-                if (axis >= 2) rank += (Y >> bq) & 1u;
-                conn[3 * tid + corner] = (int32_t)(qbase[qi] + rank);
-              } else {
-                const long long vid = 3 * tid + corner;
-                conn[vid] = (int32_t)vid;
-                emit_vertex(g, f, iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
-              }
+      for (int qi = 0; qi < 4; ++qi)
+        ow[qi] = owner_word(g, gb, wvg, j + (qi & 1), k + (qi >> 1), m);
+    }
+    long long tri = t0;
+    for (uint32_t u = active_cells(w, xmask); u; u &= u - 1) {
+      const int q = __ffs(u) - 1;
+      const int i = 32 * m + q;
+      const uint64_t cw = kMcCase[case_of(w, q)];
+      const int nt = (int)(cw >> 60);
+      for (int tt = 0; tt < nt; ++tt, ++tri) {
+#pragma unroll
+        for (int corner = 0; corner < 3; ++corner) {
+          const int e = mc_edge(cw, 3 * tt + corner);
+          const int info_e = kEdgeOwner[e];
+          const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
+          const int axis = info_e >> 3;
+          if (MERGE) {
+            const int ii = i + di;
+            long long vid;
+            if ((ii >> 5) == m) {
+              vid = owner_rank_id(ow[dj + 2 * dk], ii & 31, axis);
+            } else {  // the owner point is the first point of the next word
+              const OwnerWord o = owner_word(g, gb, wvg, j + dj, k + dk, m + 1);
+              vid = owner_rank_id(o, 0, axis);
             }
+            conn[3 * tri + corner] = (int32_t)(vid - vbase0);
+          } else {
+            const long long vid = 3 * tri + corner;
+            conn[vid] = (int32_t)(vid - vbase0);
+            emit_vertex(g, f, iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
           }
         }
-        carry += group_last(incl, G);
       }
     }
-    __syncwarp(group_mask(G));
   }
 }
 
-template <int G>
-static void launch_emit_g(const Grid& g, const float* f, float iso, bool merge,
-                          const uint32_t* bits, const long long* row_t, const long long* row_v,
-                          Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
-                          int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s) {
-  constexpr int GPB = 256 / G;
-  const size_t smem = merge ? (size_t)GPB * 16 * g.wr * sizeof(uint32_t) : 0;
-  const long long want = (g.R + GPB - 1) / GPB;
-  const long long cap = (long long)num_sms * 8;
-  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
-  if (merge) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_mc_emit<G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-    k_mc_emit<G, true><<<blocks, 256, smem, s>>>(g, f, iso, bits, row_t, row_v, info, verts, vcap,
-                                                 conn, tcap, ra, rb, rw);
-  } else {
-    k_mc_emit<G, false><<<blocks, 256, 0, s>>>(g, f, iso, bits, row_t, row_v, info, verts, vcap,
-                                               conn, tcap, ra, rb, rw);
-  }
-}
-
-void launch_mc_emit(const Grid& g, const float* f, float iso, bool merge, const uint32_t* bits,
-                    const long long* row_t, const long long* row_v, Info* info, float* verts,
+void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const uint32_t* wt,
+                    const uint32_t* wv, const uint32_t* act, Info* info, float* verts,
                     long long vcap, int32_t* conn, long long tcap, int32_t* ra, int32_t* rb,
                     float* rw, int num_sms, cudaStream_t s) {
-#define DAXGB_EMIT(G)                                                                           \
-  launch_emit_g<G>(g, f, iso, merge, bits, row_t, row_v, info, verts, vcap, conn, tcap, ra, rb, \
-                   rw, num_sms, s)
-  switch (lanes_per_row(g.wr)) {
-    case 1: DAXGB_EMIT(1); break;
-    case 2: DAXGB_EMIT(2); break;
-    case 4: DAXGB_EMIT(4); break;
-    case 8: DAXGB_EMIT(8); break;
-    case 16: DAXGB_EMIT(16); break;
-    default: DAXGB_EMIT(32); break;
+  // the active count lives on the device: launch one resident wave, grid-stride
+  const long long want = (S.rowwords + 255) / 256;
+  if (merge) {
+    const int blocks = resident_blocks(k_mc_emit<true>, 256, 0, num_sms, want);
+    k_mc_emit<true><<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, info, verts, vcap, conn, tcap,
+                                           ra, rb, rw);
+  } else {
+    const int blocks = resident_blocks(k_mc_emit<false>, 256, 0, num_sms, want);
+    k_mc_emit<false><<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, info, verts, vcap, conn, tcap,
+                                            ra, rb, rw);
   }
-#undef DAXGB_EMIT
+}
+
+// Per-grid offsets: goff[2g], goff[2g+1] = first triangle / merged vertex of
+// grid g; goff[2G], goff[2G+1] = totals.
+__global__ void k_grid_offsets(GridSet S, const uint32_t* __restrict__ wt,
+                               const uint32_t* __restrict__ wv, long long* __restrict__ goff) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= S.count; i += gridDim.x * blockDim.x) {
+    const long long w = i < S.count ? load_slot(S, i).rw0 : S.rowwords;
+    goff[2 * i] = wt[w];
+    goff[2 * i + 1] = wv[w];
+  }
+}
+
+void launch_grid_offsets(const GridSet& S, const uint32_t* wt, const uint32_t* wv,
+                         long long* goff, cudaStream_t s) {
+  k_grid_offsets<<<(S.count + 256) / 256, 256, 0, s>>>(S, wt, wv, goff);
 }
 
 // CompactPointField: out[v] = Lerp(in[first], in[second], weight).

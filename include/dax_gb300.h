@@ -143,6 +143,52 @@ int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t*
                                       float* d_out, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched marching cubes: many grids, one launch per pass                   */
+/* ------------------------------------------------------------------------ */
+
+/* A batch of uniform grids with their own extents, fields and isovalues.
+ * The plan owns a small device table (one entry per grid), uploaded at
+ * creation; it allocates nothing else.  The reference runs one dispatcher
+ * invocation per grid (dax/cont/DispatcherGenerateInterpolatedCells.h:145-254),
+ * so the batch has no direct counterpart; per grid the results equal
+ * dax_gb300_mc_count/generate on that grid alone. */
+typedef struct dax_gb300_mc_batch dax_gb300_mc_batch;
+
+/* d_fields: host array of num_grids device pointers; isovalues: host array. Blocks. */
+int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids,
+                              const float* const* d_fields, const float* isovalues,
+                              dax_gb300_mc_batch** out);
+int dax_gb300_mc_batch_destroy(dax_gb300_mc_batch* batch);
+size_t dax_gb300_mc_batch_scratch_bytes(const dax_gb300_mc_batch* batch);
+
+/* Classify + count + scan all grids (3 launches in total).  Asynchronous. */
+int dax_gb300_mc_batch_count(dax_gb300_mc_batch* batch, void* d_scratch, size_t scratch_bytes,
+                             void* stream);
+
+/* Blocks; per-grid triangle and merged-vertex offsets into the concatenated
+ * outputs (host int64[num_grids + 1] each; the last entry is the total). */
+int dax_gb300_mc_batch_totals(const dax_gb300_mc_batch* batch, const void* d_scratch,
+                              int64_t* tri_offsets, int64_t* vert_offsets, void* stream);
+
+/* Generate all grids into concatenated outputs: grid g's triangles are
+ * d_conn[tri_offsets[g] .. tri_offsets[g+1]) and index its own vertices
+ * (0-based within the grid), which are d_verts[vert_offsets[g] ..) when
+ * merged, d_verts[3 * tri_offsets[g] ..) when not.  Capacity rules as
+ * dax_gb300_mc_generate.  Asynchronous. */
+int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* batch, int merge, void* d_scratch,
+                                size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                                int32_t* d_conn, int64_t tri_capacity, void* stream);
+
+/* Capture count + generate of the batch into a CUDA graph (instantiated);
+ * *graph receives an opaque executable-graph handle.  Output buffers and
+ * scratch are baked into the graph.  Blocks while capturing. */
+int dax_gb300_mc_batch_capture(dax_gb300_mc_batch* batch, int merge, void* d_scratch,
+                               size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                               int32_t* d_conn, int64_t tri_capacity, void** graph);
+int dax_gb300_graph_launch(void* graph, void* stream);
+int dax_gb300_graph_destroy(void* graph);
+
+/* ------------------------------------------------------------------------ */
 /* Threshold                                                                 */
 /* ------------------------------------------------------------------------ */
 
@@ -182,6 +228,25 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
  * dax/exec/Derivative.h:37-75).  Asynchronous. */
 int dax_gb300_cell_gradient(const dax_gb300_uniform_grid* grid, const float* d_field,
                             float* d_gradient, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Adjoints (differentiable isosurface and gradient)                         */
+/* ------------------------------------------------------------------------ */
+
+/* dL/dfield (float[points]) from dL/d(merged isosurface vertices)
+ * (float[V][3], or NULL) and/or dL/d(cell gradients) (float[cells][3], or
+ * NULL): the adjoint of the edge interpolation
+ * (dax/worklet/MarchingCubes.h:160-161 with dax/math/VectorAnalysis.h:35-50)
+ * and of CellGradient (dax/exec/Derivative.h:37-58).  Each point gathers its
+ * incident edges and cells in a fixed order: deterministic, no atomics.
+ * When d_grad_vertices is given, d_scratch must hold a dax_gb300_mc_count of
+ * the same grid, field and isovalue (re-run it in the backward pass rather
+ * than keeping it).  Every point is written.  No reference counterpart (the
+ * reference has no adjoints).  Asynchronous. */
+int dax_gb300_field_adjoint(const dax_gb300_uniform_grid* grid, const float* d_field,
+                            float isovalue, const void* d_scratch, size_t scratch_bytes,
+                            const float* d_grad_vertices, const float* d_grad_cell_gradient,
+                            float* d_grad_field, void* stream);
 
 #ifdef __cplusplus
 }

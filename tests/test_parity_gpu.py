@@ -22,7 +22,13 @@ def _ogrid(dims, origin, spacing, emin):
 
 
 def _bits(a):
-    return np.ascontiguousarray(a).view(np.uint32)
+    """Bit patterns with every NaN mapped to one value: CUDA returns the
+    canonical NaN 0x7fffffff where the CPU propagates 0x7fc00000; all other
+    values must match bit for bit."""
+    a = np.ascontiguousarray(a)
+    b = a.view(np.uint32).copy()
+    b[np.isnan(a)] = 0x7FC00000
+    return b
 
 
 @pytest.mark.parametrize("case", cases.mc_cases(), ids=lambda c: c[0])
