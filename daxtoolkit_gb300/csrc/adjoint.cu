@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_field_adjoint(Grid g, const float* __re
 
 template <int G>
 static void launch_adj_g(const Grid& g, const float* f, float iso, const uint32_t* bits,
-                         const uint32_t* wv, const float* dverts, const float* dgrad,
+                         const WordOffsets* o, const float* dverts, const float* dgrad,
                          float* out, int num_sms, cudaStream_t s) {
   constexpr int GPB = 256 / G;
   const size_t smem = dverts ? (size_t)GPB * 12 * g.wr * sizeof(uint32_t) : 0;
@@ -180,13 +180,14 @@ static void launch_adj_g(const Grid& g, const float* f, float iso, const uint32_
   const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_field_adjoint<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_field_adjoint<G><<<blocks, 256, smem, s>>>(g, f, iso, bits, wv, dverts, dgrad, out);
+  k_field_adjoint<G><<<blocks, 256, smem, s>>>(g, f, iso, bits, o ? o->wv : nullptr, dverts,
+                                                dgrad, out);
 }
 
 void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32_t* bits,
-                          const uint32_t* wv, const float* dverts, const float* dgrad,
+                          const WordOffsets* o, const float* dverts, const float* dgrad,
                           float* out, int num_sms, cudaStream_t s) {
-#define DAXGB_ADJ(G) launch_adj_g<G>(g, f, iso, bits, wv, dverts, dgrad, out, num_sms, s)
+#define DAXGB_ADJ(G) launch_adj_g<G>(g, f, iso, bits, o, dverts, dgrad, out, num_sms, s)
   switch (lanes_per_row(g.wr)) {
     case 1: DAXGB_ADJ(1); break;
     case 2: DAXGB_ADJ(2); break;

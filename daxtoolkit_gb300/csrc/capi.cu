@@ -83,26 +83,32 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Marching-cubes scratch: [Info][status 3 x tiles][wt][wv][act][bits].
+// Marching-cubes scratch: [Info][status 3 x tiles][wc][wt][wv][act][bits].
 struct McLayout {
-  int tiles;
   long long rowwords;
-  size_t info, status, wt, wv, act, bits, total, clear;
+  int tiles;
+  size_t info, status, wc, wt, wv, act, bits, total, clear;
+  daxgb::WordOffsets offsets(void* base) const;
 };
 
-McLayout mc_layout(const Grid& g) {
+McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head) {
   McLayout L;
-  L.rowwords = g.R * g.wr;
-  L.tiles = daxgb::mc_scan_tiles(L.rowwords);
+  L.rowwords = rowwords;
+  L.tiles = daxgb::mc_scan_tiles(rowwords);
   L.info = 0;
-  L.status = align256(sizeof(Info));
-  L.clear = align256(L.status + 3 * (size_t)L.tiles * 8);
-  L.wt = L.clear;
-  L.wv = align256(L.wt + 4 * (size_t)(L.rowwords + 1));
-  L.act = align256(L.wv + 4 * (size_t)(L.rowwords + 1));
-  L.bits = align256(L.act + 4 * (size_t)L.rowwords);
-  L.total = align256(L.bits + 4 * (size_t)daxgb::bit_words(g.P));
+  L.status = align256(head);
+  L.clear = align256(L.status + 3 * 8 * (size_t)L.tiles);
+  L.wc = L.clear;
+  L.wt = align256(L.wc + 4 * (size_t)rowwords);
+  L.wv = align256(L.wt + 4 * (size_t)(rowwords + 1));
+  L.act = align256(L.wv + 4 * (size_t)(rowwords + 1));
+  L.bits = align256(L.act + 4 * (size_t)rowwords);
+  L.total = align256(L.bits + 4 * (size_t)bitwords);
   return L;
+}
+
+McLayout mc_layout(const Grid& g) {
+  return mc_layout_words(g.R * g.wr, daxgb::bit_words(g.P), sizeof(Info));
 }
 
 // Threshold scratch: [Info][status 2 x tiles][row_a][row_b][bits][used].
@@ -128,6 +134,16 @@ Layout layout(const Grid& g) {
 template <typename T>
 T* at(void* base, size_t off) {
   return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+daxgb::WordOffsets McLayout::offsets(void* base) const {
+  daxgb::WordOffsets o;
+  o.wc = at<uint32_t>(base, wc);
+  o.wt = at<uint32_t>(base, wt);
+  o.wv = at<uint32_t>(base, wv);
+  o.act = at<uint32_t>(base, act);
+  o.status = at<unsigned long long>(base, status);
+  return o;
 }
 
 int check_launch(const char* where) {
@@ -173,10 +189,10 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
     uint32_t* bits = at<uint32_t>(scratch, L.bits);
     daxgb::launch_classify_bits(0, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
     if ((st = check_launch("classify kernel"))) return st;
-    daxgb::launch_mc_scan(S, bits, at<uint32_t>(scratch, L.wt), at<uint32_t>(scratch, L.wv),
-                          at<uint32_t>(scratch, L.act), at<unsigned long long>(scratch, L.status),
-                          at<Info>(scratch, L.info), L.tiles, sms, s);
-    return check_launch("count/scan kernel");
+    const daxgb::WordOffsets o = L.offsets(scratch);
+    daxgb::launch_mc_scan(S, bits, o.wc, o.wt, o.wv, o.act, o.status, at<Info>(scratch, L.info),
+                          sms, s);
+    return check_launch("count/scan kernels");
   }
   const Layout L = layout(g);
   cudaError_t e = cudaMemsetAsync(scratch, 0, L.clear, s);
@@ -200,10 +216,8 @@ struct dax_gb300_mc_batch {
   long long rows = 0, chunks = 0, words = 0, blocks = 0, rowwords = 0;
   int max_wr = 1;
   bool aligned = true;
-  int tiles = 0;
-  size_t off_info = 0, off_goff = 0, off_status = 0, off_wt = 0, off_wv = 0, off_act = 0,
-         off_bits = 0;
-  size_t clear = 0, total = 0;
+  size_t off_goff = 0;
+  McLayout L;
 
   daxgb::GridSet set() const {
     daxgb::GridSet S{};
@@ -297,8 +311,7 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
   daxgb::launch_mc_emit(daxgb::single_set(g, d_field, isovalue, 0.0f), merge != 0,
-                        at<uint32_t>(d_scratch, L.bits), at<uint32_t>(d_scratch, L.wt),
-                        at<uint32_t>(d_scratch, L.wv), at<uint32_t>(d_scratch, L.act),
+                        at<uint32_t>(d_scratch, L.bits), L.offsets(d_scratch),
                         at<Info>(d_scratch, L.info), d_verts, vert_capacity, d_conn, tri_capacity,
                         d_rec_first, d_rec_second, d_rec_weight, num_sms(),
                         static_cast<cudaStream_t>(stream));
@@ -399,8 +412,9 @@ int dax_gb300_field_adjoint(const dax_gb300_uniform_grid* grid, const float* d_f
   if (d_grad_vertices && (!d_scratch || scratch_bytes < L.total))
     return fail(DAX_GB300_ERROR_BAD_VALUE, "vertex adjoint needs the dax_gb300_mc_count scratch");
   void* sc = const_cast<void*>(d_scratch);
+  const daxgb::WordOffsets wo = L.offsets(sc);
   daxgb::launch_field_adjoint(g, d_field, isovalue, d_grad_vertices ? at<uint32_t>(sc, L.bits) : nullptr,
-                              d_grad_vertices ? at<uint32_t>(sc, L.wv) : nullptr,
+                              d_grad_vertices ? &wo : nullptr,
                               d_grad_vertices, d_grad_cell_gradient, d_grad_field, num_sms(), s);
   return check_launch("field adjoint kernel");
 }
@@ -438,16 +452,8 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
     b->aligned = b->aligned && aligned16(d_fields[i]);
   }
   b->words = 4 * b->chunks + 8;
-  b->tiles = daxgb::mc_scan_tiles(b->rowwords);
-  b->off_info = 0;
   b->off_goff = align256(sizeof(Info));
-  b->off_status = align256(b->off_goff + 16 * (size_t)(num_grids + 1));
-  b->clear = align256(b->off_status + 3 * (size_t)b->tiles * 8);
-  b->off_wt = b->clear;
-  b->off_wv = align256(b->off_wt + 4 * (size_t)(b->rowwords + 1));
-  b->off_act = align256(b->off_wv + 4 * (size_t)(b->rowwords + 1));
-  b->off_bits = align256(b->off_act + 4 * (size_t)b->rowwords);
-  b->total = align256(b->off_bits + 4 * (size_t)b->words);
+  b->L = mc_layout_words(b->rowwords, b->words, b->off_goff + 16 * (size_t)(num_grids + 1));
   if (num_grids > 1) {
     cudaError_t e = cudaMalloc(&b->d_slots, sizeof(daxgb::GridSlot) * num_grids);
     if (e == cudaSuccess)
@@ -471,28 +477,25 @@ int dax_gb300_mc_batch_destroy(dax_gb300_mc_batch* b) {
   return DAX_GB300_SUCCESS;
 }
 
-size_t dax_gb300_mc_batch_scratch_bytes(const dax_gb300_mc_batch* b) { return b ? b->total : 0; }
+size_t dax_gb300_mc_batch_scratch_bytes(const dax_gb300_mc_batch* b) { return b ? b->L.total : 0; }
 
 int dax_gb300_mc_batch_count(dax_gb300_mc_batch* b, void* d_scratch, size_t scratch_bytes,
                              void* stream) {
   if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
-  if (scratch_bytes < b->total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
+  if (scratch_bytes < b->L.total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(d_scratch, 0, b->clear, s);
+  cudaError_t e = cudaMemsetAsync(d_scratch, 0, b->L.clear, s);
   if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
   const daxgb::GridSet S = b->set();
-  uint32_t* bits = at<uint32_t>(d_scratch, b->off_bits);
+  uint32_t* bits = at<uint32_t>(d_scratch, b->L.bits);
   daxgb::launch_classify_bits(0, S, b->aligned, bits, b->words, num_sms(), s);
   int st = check_launch("batch classify kernel");
   if (st) return st;
-  daxgb::launch_mc_scan(S, bits, at<uint32_t>(d_scratch, b->off_wt),
-                        at<uint32_t>(d_scratch, b->off_wv), at<uint32_t>(d_scratch, b->off_act),
-                        at<unsigned long long>(d_scratch, b->off_status),
-                        at<Info>(d_scratch, b->off_info), b->tiles, num_sms(), s);
-  if ((st = check_launch("batch row count/scan kernel"))) return st;
-  daxgb::launch_grid_offsets(S, at<uint32_t>(d_scratch, b->off_wt),
-                             at<uint32_t>(d_scratch, b->off_wv),
-                             at<long long>(d_scratch, b->off_goff), s);
+  const daxgb::WordOffsets o = b->L.offsets(d_scratch);
+  daxgb::launch_mc_scan(S, bits, o.wc, o.wt, o.wv, o.act, o.status, at<Info>(d_scratch, 0),
+                        num_sms(), s);
+  if ((st = check_launch("batch count/scan kernels"))) return st;
+  daxgb::launch_grid_offsets(S, b->L.offsets(d_scratch), at<long long>(d_scratch, b->off_goff), s);
   return check_launch("batch offsets kernel");
 }
 
@@ -516,13 +519,11 @@ int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* b, int merge, void* d_scratc
                                 size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
                                 int32_t* d_conn, int64_t tri_capacity, void* stream) {
   if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
-  if (scratch_bytes < b->total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
+  if (scratch_bytes < b->L.total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0))
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
-  daxgb::launch_mc_emit(b->set(), merge != 0, at<uint32_t>(d_scratch, b->off_bits),
-                        at<uint32_t>(d_scratch, b->off_wt), at<uint32_t>(d_scratch, b->off_wv),
-                        at<uint32_t>(d_scratch, b->off_act),
-                        at<Info>(d_scratch, b->off_info), d_verts, vert_capacity, d_conn,
+  daxgb::launch_mc_emit(b->set(), merge != 0, at<uint32_t>(d_scratch, b->L.bits),
+                        b->L.offsets(d_scratch), at<Info>(d_scratch, 0), d_verts, vert_capacity, d_conn,
                         tri_capacity, nullptr, nullptr, nullptr, num_sms(),
                         static_cast<cudaStream_t>(stream));
   return check_launch("batch generate kernel");

@@ -61,20 +61,28 @@ inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long
   return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
-// Marching cubes over row words: K2 (count + scan) writes per-word exclusive
-// triangle / vertex offsets wt, wv (uint32[rowwords + 1]) and the compacted
-// list of active words act (uint32[rowwords]); K3 emits from them.
+// Marching cubes over row words: K2a counts every row word into wc, K2b
+// scans them into per-word exclusive triangle / vertex offsets wt, wv
+// (uint32[rowwords + 1]; entry rowwords holds the totals) and the compacted
+// list of active words act.
+struct WordOffsets {
+  uint32_t* wc;   // [rowwords] packed counts (triangles << 16) | edges
+  uint32_t* wt;   // [rowwords + 1]
+  uint32_t* wv;   // [rowwords + 1]
+  uint32_t* act;  // [rowwords]
+  unsigned long long* status;  // [3][tiles] look-back state
+};
+
 int mc_scan_tiles(long long rowwords);
-void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wt, uint32_t* wv,
-                    uint32_t* act, unsigned long long* status, Info* info, int tiles, int num_sms,
-                    cudaStream_t s);
-void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const uint32_t* wt,
-                    const uint32_t* wv, const uint32_t* act, Info* info, float* verts,
-                    long long vcap, int32_t* conn, long long tcap, int32_t* ra, int32_t* rb,
-                    float* rw, int num_sms, cudaStream_t s);
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32_t* wt,
+                    uint32_t* wv, uint32_t* act, unsigned long long* status, Info* info,
+                    int num_sms, cudaStream_t s);
+void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
+                    Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
+                    int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s);
 // goff[2g], goff[2g+1]: first triangle / merged vertex of grid g; then totals.
-void launch_grid_offsets(const GridSet& S, const uint32_t* wt, const uint32_t* wv,
-                         long long* goff, cudaStream_t s);
+void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff,
+                         cudaStream_t s);
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s);
 
@@ -87,7 +95,7 @@ void launch_thr_emit(const Grid& g, const float* f, const uint32_t* bits, const 
                      cudaStream_t s);
 
 void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32_t* bits,
-                          const uint32_t* wv, const float* dverts, const float* dgrad,
+                          const WordOffsets* o, const float* dverts, const float* dgrad,
                           float* out, int num_sms, cudaStream_t s);
 
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s);

@@ -89,121 +89,322 @@ __device__ __forceinline__ void crossing_masks(const Grid& g, const uint32_t* bi
 }
 
 // ---------------------------------------------------------------------------
-// K2: counts per row word + three-chain look-back scan.
+// K2: counts per row word, then a single-pass scan.
+//   K2a (k_mc_count): one thread per word; writes the packed counts
+//       wc[w] = (triangles << 16) | crossing edges (both < 2^16: a word has
+//       32 points and 32 cells).  No synchronisation.
+//   K2b (k_mc_scan): single-pass decoupled look-back scan of wc (tiles of
+//       4096 words, 16 per thread), writing per-word exclusive triangle and
+//       vertex offsets wt / wv (uint32[rowwords + 1]) and the compacted list
+//       act of active words (uint32[A]).
 
-// Triangle and crossing-edge counts of word m of row r.  Eight word fetches
-// per 32 points: (a, a+x) of the four rows (j..j+1, k..k+1).
-__device__ __forceinline__ void mc_word_counts(const Grid& g, const uint32_t* bits, long long r,
-                                               int m, int& t, int& v) {
-  const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-  const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+// The eight corner words of word m of row r (a, a+x of rows (j..j+1,
+// k..k+1)) and the masks that decide which of them are meaningful.
+struct WordBits {
+  CornerWords w;
+  uint32_t pmask, xmask;
+  bool hy, hz;
+};
+
+__device__ __forceinline__ WordBits load_word_bits(const Grid& g, const uint32_t* bits, unsigned r,
+                                                   int m) {
+  WordBits wb;
+  const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+  wb.hy = j < g.ny - 1;
+  wb.hz = k < g.nz - 1;
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-  const long long pos = r * g.nx + 32ll * m;
-  const uint32_t pmask = low_mask(g.nx - 32 * m);
-  const uint32_t xmask = low_mask(g.nx - 1 - 32 * m);
-  CornerWords w{};
-  bits_at2(bits, pos, w.a, w.a1);
-  if (hy) bits_at2(bits, pos + dy, w.b, w.b1);
-  if (hz) bits_at2(bits, pos + dz, w.c, w.c1);
-  if (hy && hz) bits_at2(bits, pos + dy + dz, w.d, w.d1);
-  v = __popc((w.a ^ w.a1) & xmask);
+  const long long pos = (long long)r * g.nx + 32ll * m;
+  wb.pmask = low_mask(g.nx - 32 * m);
+  wb.xmask = low_mask(g.nx - 1 - 32 * m);
+  wb.w = CornerWords{};
+  bits_at2(bits, pos, wb.w.a, wb.w.a1);
+  if (wb.hy) bits_at2(bits, pos + dy, wb.w.b, wb.w.b1);
+  if (wb.hz) bits_at2(bits, pos + dz, wb.w.c, wb.w.c1);
+  if (wb.hy && wb.hz) bits_at2(bits, pos + dy + dz, wb.w.d, wb.w.d1);
+  return wb;
+}
+
+__device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int& si, unsigned& r,
+                                            int& m) {
+  si = S.count == 1 ? 0 : slot_of_rowword(S, gw);
+  const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+  const unsigned lw = (unsigned)(gw - sl.rw0);
+  r = lw / (unsigned)sl.g.wr;
+  m = (int)(lw - r * (unsigned)sl.g.wr);
+}
+
+// Counts of one word from its eight corner words.
+__device__ __forceinline__ uint32_t packed_counts(const CornerWords& w, bool hy, bool hz,
+                                                  uint32_t pmask, uint32_t xmask,
+                                                  const unsigned char* nf) {
+  int v = __popc((w.a ^ w.a1) & xmask);
   if (hy) v += __popc((w.a ^ w.b) & pmask);
   if (hz) v += __popc((w.a ^ w.c) & pmask);
-  t = 0;
-  if (hy && hz) {
-    uint32_t act = active_cells(w, xmask);
-    while (act) {
-      const int q = __ffs(act) - 1;
-      act &= act - 1;
-      t += mc_num_tris(case_of(w, q));
+  int t = 0;
+  if (hy && hz)
+    for (uint32_t u = active_cells(w, xmask); u; u &= u - 1) t += nf[case_of(w, __ffs(u) - 1)];
+  return ((uint32_t)t << 16) | (uint32_t)v;
+}
+
+// Four consecutive 32-bit windows of a row (x = 32m .. 32m+127) and their +x
+// neighbours, from five word fetches.
+__device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, long long pos,
+                                             uint32_t (&a)[4], uint32_t (&a1)[4]) {
+  const long long w = pos >> 5;
+  const unsigned sh = (unsigned)(pos & 31);
+  uint32_t x[5];
+#pragma unroll
+  for (int e = 0; e < 5; ++e) x[e] = __ldg(bits + w + e);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    a[e] = __funnelshift_r(x[e], x[e + 1], sh);
+    a1[e] = (a[e] >> 1) | (((x[e + 1] >> sh) & 1u) << 31);
+  }
+}
+
+constexpr int kCountWords = 4;  // consecutive row words per thread in K2a
+
+__global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __restrict__ bits,
+                                                  uint32_t* __restrict__ wc) {
+  __shared__ unsigned char s_nf[256];  // NumFaces, indexed by divergent case ids
+  s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x * kCountWords;
+  for (long long g0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kCountWords;
+       g0 < S.rowwords; g0 += stride) {
+    int si, m;
+    unsigned r;
+    locate_word(S, g0, si, r, m);
+    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+    const Grid& g = sl.g;
+    uint32_t out[kCountWords] = {0, 0, 0, 0};
+    const bool cells = g.nx >= 2 && g.ny >= 2 && g.nz >= 2;
+    if (cells && m + kCountWords <= g.wr && g0 + kCountWords <= S.rowwords &&
+        (S.count == 1 || g0 + kCountWords <= sl.rw0 + (long long)g.R * g.wr)) {
+      // fast path: the four words lie in one row
+      const uint32_t* gb = bits + sl.word0;
+      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+      const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+      const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+      const long long pos = (long long)r * g.nx + 32ll * m;
+      uint32_t a[4], a1[4], b[4] = {0, 0, 0, 0}, b1[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0},
+               c1[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0}, d1[4] = {0, 0, 0, 0};
+      row_windows4(gb, pos, a, a1);
+      if (hy) row_windows4(gb, pos + dy, b, b1);
+      if (hz) row_windows4(gb, pos + dz, c, c1);
+      if (hy && hz) row_windows4(gb, pos + dy + dz, d, d1);
+#pragma unroll
+      for (int e = 0; e < kCountWords; ++e) {
+        const CornerWords w{a[e], a1[e], b[e], b1[e], c[e], c1[e], d[e], d1[e]};
+        out[e] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + e)),
+                               low_mask(g.nx - 1 - 32 * (m + e)), s_nf);
+      }
+    } else {
+      // words that straddle a row or grid end: one at a time
+#pragma unroll
+      for (int e = 0; e < kCountWords; ++e) {
+        const long long gw = g0 + e;
+        if (gw >= S.rowwords) break;
+        int se, me;
+        unsigned re;
+        locate_word(S, gw, se, re, me);
+        const GridSlot& sle = S.count == 1 ? S.one : S.slots[se];
+        if (sle.g.nx >= 2 && sle.g.ny >= 2 && sle.g.nz >= 2) {
+          const WordBits wb = load_word_bits(sle.g, bits + sle.word0, re, me);
+          out[e] = packed_counts(wb.w, wb.hy, wb.hz, wb.pmask, wb.xmask, s_nf);
+        }
+      }
+    }
+    if (g0 + kCountWords <= S.rowwords) {
+      *reinterpret_cast<uint4*>(wc + g0) = make_uint4(out[0], out[1], out[2], out[3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < kCountWords; ++e)
+        if (g0 + e < S.rowwords) wc[g0 + e] = out[e];
     }
   }
 }
 
-constexpr int kWordsPerThread = 4;
-constexpr int kWordsPerTile = 256 * kWordsPerThread;
-
-__device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int& si, long long& r,
-                                            int& m) {
-  si = S.count == 1 ? 0 : slot_of_rowword(S, gw);
-  const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-  const long long lw = gw - sl.rw0;
-  r = lw / sl.g.wr;
-  m = (int)(lw - r * sl.g.wr);
+// Look-back by one warp over N independent status chains (status + c *
+// stride + tile), same flag protocol and bounded waiting as warp_lookback.
+template <int N>
+__device__ __forceinline__ void warp_lookback_n(unsigned long long* st, int stride, int tile,
+                                                const long long (&agg)[N], int* err,
+                                                long long (&ex)[N]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < N; ++c) ex[c] = 0;
+  if (lane == 0) {
+    const unsigned long long f = tile == 0 ? kFlagInc : kFlagAgg;
+#pragma unroll
+    for (int c = 0; c < N; ++c) st_release(st + c * stride + tile, f | (unsigned long long)agg[c]);
+  }
+  if (tile == 0) return;
+  bool done[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) done[c] = false;
+  int p = tile - 1, spins = 0;
+  while (true) {
+    bool all = true;
+#pragma unroll
+    for (int c = 0; c < N; ++c) all = all && done[c];
+    if (all) break;
+    const int idx = p - lane;
+    unsigned long long w[N];
+    int first[N];
+    bool missing = false;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      w[c] = (!done[c] && idx >= 0) ? ld_acquire(st + c * stride + idx) : kFlagInc;
+      const unsigned inc = __ballot_sync(kFull, (w[c] >> 62) == 2u);
+      const unsigned none = __ballot_sync(kFull, (w[c] >> 62) == 0u);
+      first[c] = inc ? __ffs(inc) - 1 : 32;
+      const unsigned need = first[c] >= 31 ? kFull : ((2u << first[c]) - 1u);
+      missing = missing || (none & need);
+    }
+    if (missing) {
+      if (++spins > kSpinLimit) {
+        if (lane == 0) atomicOr(err, kErrTimeout);
+        break;
+      }
+      if (spins > 16) __nanosleep(32);
+      continue;
+    }
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      long long v = (lane <= first[c] && idx >= 0) ? (long long)(w[c] & kValMask) : 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+      if (!done[c]) ex[c] += v;
+      done[c] = done[c] || first[c] < 32;
+    }
+    p -= 32;
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < N; ++c)
+      st_release(st + c * stride + tile, kFlagInc | (unsigned long long)(ex[c] + agg[c]));
+  }
 }
 
-__global__ void __launch_bounds__(256) k_mc_scan(GridSet S, const uint32_t* __restrict__ bits,
+constexpr int kScanItems = 16;                 // words per thread
+constexpr int kScanTile = 256 * kScanItems;    // words per tile
+
+__global__ void __launch_bounds__(256) k_mc_scan(long long rowwords,
+                                                 const uint32_t* __restrict__ wc,
                                                  uint32_t* __restrict__ wt,
                                                  uint32_t* __restrict__ wv,
                                                  uint32_t* __restrict__ act,
                                                  unsigned long long* __restrict__ status,
                                                  Info* __restrict__ info, int tiles) {
   __shared__ int s_tile;
-  const int tid = threadIdx.x;
-  while (true) {
-    if (tid == 0) s_tile = (int)atomicAdd(&info->ticket, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    __syncthreads();
-    if (tile >= tiles) break;
-    const long long w0 = (long long)tile * kWordsPerTile + (long long)tid * kWordsPerThread;
-    int tc[kWordsPerThread], vc[kWordsPerThread];
+  __shared__ uint32_t s_wt[8], s_wv[8], s_wa[8];
+  __shared__ long long s_ex[3];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = (int)atomicAdd(&info->ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const long long w0 = (long long)tile * kScanTile + (long long)tid * kScanItems;
+  uint32_t c[kScanItems];
+  const bool full = w0 + kScanItems <= rowwords;
+  if (full) {
 #pragma unroll
-    for (int e = 0; e < kWordsPerThread; ++e) {
-      tc[e] = vc[e] = 0;
-      const long long gw = w0 + e;
-      if (gw < S.rowwords) {
-        int si, m;
-        long long r;
-        locate_word(S, gw, si, r, m);
-        const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-        if (sl.g.nx >= 2 && sl.g.ny >= 2 && sl.g.nz >= 2)
-          mc_word_counts(sl.g, bits + sl.word0, r, m, tc[e], vc[e]);
-      }
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const uint4 u = __ldcs(reinterpret_cast<const uint4*>(wc + w0) + q);
+      c[4 * q] = u.x;
+      c[4 * q + 1] = u.y;
+      c[4 * q + 2] = u.z;
+      c[4 * q + 3] = u.w;
     }
-    long long mine[3] = {0, 0, 0};
+  } else {
 #pragma unroll
-    for (int e = 0; e < kWordsPerThread; ++e) {
-      mine[0] += tc[e];
-      mine[1] += vc[e];
-      mine[2] += (tc[e] | vc[e]) ? 1 : 0;
-    }
-    long long ex[3], agg[3], base[3];
-    block_exclusive_scan<3>(mine, ex, agg);
-    block_lookback<3>(status, tiles, tile, agg, &info->error, base);
-    long long ot = base[0] + ex[0], ov = base[1] + ex[1], oa = base[2] + ex[2];
+    for (int e = 0; e < kScanItems; ++e) c[e] = w0 + e < rowwords ? wc[w0 + e] : 0u;
+  }
+  uint32_t st = 0, sv = 0, sa = 0;
 #pragma unroll
-    for (int e = 0; e < kWordsPerThread; ++e) {
-      const long long gw = w0 + e;
-      if (gw < S.rowwords) {
-        wt[gw] = (uint32_t)ot;
-        wv[gw] = (uint32_t)ov;
-        if (tc[e] | vc[e]) act[oa++] = (uint32_t)gw;
-      }
-      ot += tc[e];
-      ov += vc[e];
+  for (int e = 0; e < kScanItems; ++e) {
+    st += c[e] >> 16;
+    sv += c[e] & 0xffffu;
+    sa += c[e] ? 1u : 0u;
+  }
+  // block exclusive scan of (st, sv, sa), 32-bit (a tile holds < 2^20 of each)
+  uint32_t it = st, iv = sv, ia = sa;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ut = __shfl_up_sync(kFull, it, o), uv = __shfl_up_sync(kFull, iv, o),
+                   ua = __shfl_up_sync(kFull, ia, o);
+    if (lane >= o) { it += ut; iv += uv; ia += ua; }
+  }
+  if (lane == 31) { s_wt[warp] = it; s_wv[warp] = iv; s_wa[warp] = ia; }
+  __syncthreads();
+  uint32_t bt = 0, bv = 0, ba = 0, tt = 0, tv = 0, ta = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    if (w < warp) { bt += s_wt[w]; bv += s_wv[w]; ba += s_wa[w]; }
+    tt += s_wt[w];
+    tv += s_wv[w];
+    ta += s_wa[w];
+  }
+  if (warp == 0) {
+    const long long agg[3] = {(long long)tt, (long long)tv, (long long)ta};
+    long long ex[3];
+    warp_lookback_n<3>(status, tiles, tile, agg, &info->error, ex);
+    if (lane == 0) {
+      s_ex[0] = ex[0];
+      s_ex[1] = ex[1];
+      s_ex[2] = ex[2];
     }
-    if (tile == tiles - 1 && tid == 0) {
-      const long long T = base[0] + agg[0], V = base[1] + agg[1], A = base[2] + agg[2];
-      wt[S.rowwords] = (uint32_t)T;
-      wv[S.rowwords] = (uint32_t)V;
-      info->total_a = T;
-      info->total_b = V;
-      info->total_c = A;
-      if (T > 2147483647ll || V > 2147483647ll) atomicOr(&info->error, kErrOverflow);
+  }
+  __syncthreads();
+  // offsets are stored as uint32; a total above 2^31 - 1 is reported below
+  uint32_t ot = (uint32_t)s_ex[0] + bt + it - st;
+  uint32_t ov = (uint32_t)s_ex[1] + bv + iv - sv;
+  long long oa = s_ex[2] + ba + ia - sa;
+#pragma unroll
+  for (int q = 0; q < kScanItems / 4; ++q) {
+    uint32_t t4[4], v4[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const uint32_t ce = c[4 * q + e];
+      t4[e] = ot;
+      v4[e] = ov;
+      ot += ce >> 16;
+      ov += ce & 0xffffu;
+      if (ce) act[oa++] = (uint32_t)(w0 + 4 * q + e);
     }
+    if (full) {
+      reinterpret_cast<uint4*>(wt + w0)[q] = make_uint4(t4[0], t4[1], t4[2], t4[3]);
+      reinterpret_cast<uint4*>(wv + w0)[q] = make_uint4(v4[0], v4[1], v4[2], v4[3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (w0 + 4 * q + e < rowwords) {
+          wt[w0 + 4 * q + e] = t4[e];
+          wv[w0 + 4 * q + e] = v4[e];
+        }
+    }
+  }
+  if (tile == tiles - 1 && tid == 0) {
+    const long long T = s_ex[0] + tt, V = s_ex[1] + tv;
+    wt[rowwords] = (uint32_t)T;
+    wv[rowwords] = (uint32_t)V;
+    info->total_a = T;
+    info->total_b = V;
+    info->total_c = s_ex[2] + ta;
+    if (T > 2147483647ll || V > 2147483647ll) atomicOr(&info->error, kErrOverflow);
   }
 }
 
-void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wt, uint32_t* wv,
-                    uint32_t* act, unsigned long long* status, Info* info, int tiles, int num_sms,
-                    cudaStream_t s) {
-  const int blocks = resident_blocks(k_mc_scan, 256, 0, num_sms, tiles);
-  k_mc_scan<<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, status, info, tiles);
-}
+int mc_scan_tiles(long long rowwords) { return (int)((rowwords + kScanTile - 1) / kScanTile); }
 
-int mc_scan_tiles(long long rowwords) {
-  return (int)((rowwords + kWordsPerTile - 1) / kWordsPerTile);
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32_t* wt,
+                    uint32_t* wv, uint32_t* act, unsigned long long* status, Info* info,
+                    int num_sms, cudaStream_t s) {
+  const long long want = (S.rowwords + 256 * kCountWords - 1) / (256 * kCountWords);
+  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, want);
+  k_mc_count<<<b1, 256, 0, s>>>(S, bits, wc);
+  const int tiles = mc_scan_tiles(S.rowwords);
+  k_mc_scan<<<tiles, 256, 0, s>>>(S.rowwords, wc, wt, wv, act, status, info, tiles);
 }
 
 // ---------------------------------------------------------------------------
@@ -234,6 +435,14 @@ __device__ __forceinline__ void emit_vertex(const Grid& g, const float* __restri
   if (rw) rw[vid] = w;
 }
 
+// Global offsets of word gw (gw may equal rowwords: then the totals).
+__device__ __forceinline__ long long word_t(const WordOffsets& o, long long gw) {
+  return (long long)__ldg(o.wt + gw);
+}
+__device__ __forceinline__ long long word_v(const WordOffsets& o, long long gw) {
+  return (long long)__ldg(o.wv + gw);
+}
+
 // Crossing masks of one owner word plus its global vertex offset.
 struct OwnerWord {
   uint32_t X, Y, Z;
@@ -241,18 +450,19 @@ struct OwnerWord {
 };
 
 __device__ __forceinline__ OwnerWord owner_word(const Grid& g, const uint32_t* bits,
-                                                const uint32_t* wv_grid, int jq, int kq, int wq) {
+                                                const WordOffsets& o, long long rw0, int jq,
+                                                int kq, int wq) {
   const long long rq = (long long)kq * g.ny + jq;
   const long long pos = rq * g.nx + 32ll * wq;
   uint32_t a, a1;
   bits_at2(bits, pos, a, a1);
   const uint32_t pm = low_mask(g.nx - 32 * wq);
-  OwnerWord o;
-  o.X = (a ^ a1) & low_mask(g.nx - 1 - 32 * wq);
-  o.Y = jq < g.ny - 1 ? (a ^ bits_at(bits, pos + g.nx)) & pm : 0u;
-  o.Z = kq < g.nz - 1 ? (a ^ bits_at(bits, pos + (long long)g.nx * g.ny)) & pm : 0u;
-  o.base = __ldg(wv_grid + rq * g.wr + wq);
-  return o;
+  OwnerWord ow;
+  ow.X = (a ^ a1) & low_mask(g.nx - 1 - 32 * wq);
+  ow.Y = jq < g.ny - 1 ? (a ^ bits_at(bits, pos + g.nx)) & pm : 0u;
+  ow.Z = kq < g.nz - 1 ? (a ^ bits_at(bits, pos + (long long)g.nx * g.ny)) & pm : 0u;
+  ow.base = word_v(o, rw0 + rq * g.wr + wq);
+  return ow;
 }
 
 __device__ __forceinline__ long long owner_rank_id(const OwnerWord& o, int b, int axis) {
@@ -263,83 +473,175 @@ __device__ __forceinline__ long long owner_rank_id(const OwnerWord& o, int b, in
   return id;
 }
 
-template <bool MERGE>
-__global__ void __launch_bounds__(256) k_mc_emit(GridSet S, const uint32_t* __restrict__ bits,
-                                                 const uint32_t* __restrict__ wt,
-                                                 const uint32_t* __restrict__ wv,
-                                                 const uint32_t* __restrict__ act,
-                                                 Info* __restrict__ info,
-                                                 float* __restrict__ verts, long long vcap,
-                                                 int32_t* __restrict__ conn, long long tcap,
-                                                 int32_t* __restrict__ ra, int32_t* __restrict__ rb,
-                                                 float* __restrict__ rw) {
+// K3: two kernels over the A active words (A on the device, the words in
+// the compacted list act).  k_mc_emit_vertices writes the merged
+// vertices a word's points own; k_mc_emit_triangles writes its cells'
+// triangles (and, unmerged, their corner vertices).  Splitting the roles
+// keeps each thread's chain of dependent memory round trips short and each
+// kernel's register count low.
+__device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long vcap, bool merge,
+                                           long long& A) {
   const long long T = info->total_a;
-  const long long V = MERGE ? info->total_b : 3 * T;
-  const long long A = info->total_c;
+  const long long V = merge ? info->total_b : 3 * T;
+  A = info->total_c;
   if (T > tcap || V > vcap || (info->error & (kErrOverflow | kErrTimeout))) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
       atomicOr(&info->error, kErrCapacity);
-    return;
+    return false;
   }
+  return true;
+}
+
+constexpr int kVertexBatch = 4;
+
+__global__ void __launch_bounds__(256) k_mc_emit_vertices(GridSet S,
+                                                          const uint32_t* __restrict__ bits,
+                                                          WordOffsets o,
+                                                          Info* __restrict__ info,
+                                                          float* __restrict__ verts, long long vcap,
+                                                          long long tcap,
+                                                          int32_t* __restrict__ ra,
+                                                          int32_t* __restrict__ rb,
+                                                          float* __restrict__ rw) {
+  long long A;
+  if (!emit_guard(info, tcap, vcap, true, A)) return;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long ai = (long long)blockIdx.x * blockDim.x + threadIdx.x; ai < A; ai += stride) {
-    const long long gw = __ldg(act + ai);
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < A; it += stride) {
+    const long long gw = __ldg(o.act + it);
+    const long long v0 = word_v(o, gw), v1 = word_v(o, gw + 1);
+    if (v1 == v0) continue;
     int si, m;
-    long long r;
+    unsigned r;
     locate_word(S, gw, si, r, m);
     const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
     const Grid& g = sl.g;
     const uint32_t* gb = bits + sl.word0;
-    const uint32_t* wvg = wv + sl.rw0;
     const float* f = sl.field;
     const float iso = sl.iso;
-    const long long t0 = __ldg(wt + gw), t1 = __ldg(wt + gw + 1);
-    const long long v0 = __ldg(wv + gw), v1 = __ldg(wv + gw + 1);
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
     const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-    const long long pos = r * g.nx + 32ll * m;
-    const uint32_t pmask = low_mask(g.nx - 32 * m);
-    const uint32_t xmask = low_mask(g.nx - 1 - 32 * m);
+    const long long pos = (long long)r * g.nx + 32ll * m;
     const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
-    CornerWords w{};
-    bits_at2(gb, pos, w.a, w.a1);
-    if (hy) bits_at2(gb, pos + dy, w.b, w.b1);
-    if (hz) bits_at2(gb, pos + dz, w.c, w.c1);
-    if (hy && hz) bits_at2(gb, pos + dy + dz, w.d, w.d1);
-    if (MERGE && v1 > v0) {
-      const uint32_t X = (w.a ^ w.a1) & xmask;
-      const uint32_t Y = hy ? (w.a ^ w.b) & pmask : 0u;
-      const uint32_t Z = hz ? (w.a ^ w.c) & pmask : 0u;
-      long long vid = v0;
-      for (uint32_t u = X | Y | Z; u; u &= u - 1) {
+    const uint32_t pmask = low_mask(g.nx - 32 * m);
+    uint32_t a, a1, b = 0, c = 0;
+    bits_at2(gb, pos, a, a1);
+    if (hy) b = bits_at(gb, pos + dy);
+    if (hz) c = bits_at(gb, pos + dz);
+    uint32_t ux = (a ^ a1) & low_mask(g.nx - 1 - 32 * m);
+    uint32_t uy = hy ? (a ^ b) & pmask : 0u;
+    uint32_t uz = hz ? (a ^ c) & pmask : 0u;
+    // edges in (point, axis) order, in batches whose field loads are all
+    // issued before any arithmetic
+    long long vid = v0;
+    while (ux | uy | uz) {
+      int ei[kVertexBatch], ea[kVertexBatch];
+      int nb = 0;
+#pragma unroll
+      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
+        const uint32_t u = ux | uy | uz;
+        if (u == 0) break;
         const int q = __ffs(u) - 1;
-        const int i = 32 * m + q;
-        if ((X >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 0, vid++, verts, ra, rb, rw);
-        if ((Y >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 1, vid++, verts, ra, rb, rw);
-        if ((Z >> q) & 1u) emit_vertex(g, f, iso, i, j, k, 2, vid++, verts, ra, rb, rw);
+        const uint32_t bit = 1u << q;
+        int ax;
+        if (ux & bit) { ax = 0; ux &= ~bit; }
+        else if (uy & bit) { ax = 1; uy &= ~bit; }
+        else { ax = 2; uz &= ~bit; }
+        ei[nb] = 32 * m + q;
+        ea[nb] = ax;
+        ++nb;
+      }
+      float fa[kVertexBatch], fb[kVertexBatch];
+#pragma unroll
+      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
+        if (s2 < nb) {
+          const long long pa = (long long)r * g.nx + ei[s2];
+          fa[s2] = __ldg(f + pa);
+          fb[s2] = __ldg(f + pa + (ea[s2] == 0 ? 1ll : (ea[s2] == 1 ? dy : dz)));
+        }
+      }
+#pragma unroll
+      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
+        if (s2 < nb) {
+          const int i = ei[s2], ax = ea[s2];
+          const float w = __fdiv_rn(__fsub_rn(iso, fa[s2]), __fsub_rn(fb[s2], fa[s2]));
+          const float xa = coord(g.ox, g.sx, i, g.mx), ya = coord(g.oy, g.sy, j, g.my),
+                      za = coord(g.oz, g.sz, k, g.mz);
+          const float xb = ax == 0 ? coord(g.ox, g.sx, i + 1, g.mx) : xa;
+          const float yb = ax == 1 ? coord(g.oy, g.sy, j + 1, g.my) : ya;
+          const float zb = ax == 2 ? coord(g.oz, g.sz, k + 1, g.mz) : za;
+          verts[3 * vid + 0] = lerp_rn(xa, xb, w);
+          verts[3 * vid + 1] = lerp_rn(ya, yb, w);
+          verts[3 * vid + 2] = lerp_rn(za, zb, w);
+          const long long pa = (long long)r * g.nx + i;
+          if (ra) ra[vid] = (int32_t)pa;
+          if (rb) rb[vid] = (int32_t)(pa + (ax == 0 ? 1ll : (ax == 1 ? dy : dz)));
+          if (rw) rw[vid] = w;
+          ++vid;
+        }
       }
     }
+  }
+}
+
+template <bool MERGE>
+__global__ void __launch_bounds__(256) k_mc_emit_triangles(GridSet S,
+                                                           const uint32_t* __restrict__ bits,
+                                                           WordOffsets o,
+                                                           Info* __restrict__ info,
+                                                           float* __restrict__ verts,
+                                                           long long vcap,
+                                                           int32_t* __restrict__ conn,
+                                                           long long tcap,
+                                                           int32_t* __restrict__ ra,
+                                                           int32_t* __restrict__ rb,
+                                                           float* __restrict__ rw) {
+  // case and edge tables in shared memory: lanes index them divergently
+  __shared__ uint64_t s_case[256];
+  __shared__ unsigned char s_edge[12];
+  s_case[threadIdx.x] = kMcCase[threadIdx.x];
+  if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
+  __syncthreads();
+  long long A;
+  if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < A; it += stride) {
+    const long long gw = __ldg(o.act + it);
+    const long long t0 = word_t(o, gw), t1 = word_t(o, gw + 1);
     if (t1 == t0) continue;
+    int si, m;
+    unsigned r;
+    locate_word(S, gw, si, r, m);
+    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+    const Grid& g = sl.g;
+    const uint32_t* gb = bits + sl.word0;
+    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+    const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+    const long long pos = (long long)r * g.nx + 32ll * m;
+    CornerWords w{};
+    bits_at2(gb, pos, w.a, w.a1);
+    bits_at2(gb, pos + dy, w.b, w.b1);
+    bits_at2(gb, pos + dz, w.c, w.c1);
+    bits_at2(gb, pos + dy + dz, w.d, w.d1);
     // first vertex of this grid in the concatenated output (0 for one grid)
-    const long long vbase0 = S.count == 1 ? 0 : (MERGE ? (long long)__ldg(wv + sl.rw0)
-                                                       : 3ll * __ldg(wt + sl.rw0));
+    const long long vbase0 =
+        S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
     OwnerWord ow[4];
     if (MERGE) {
 #pragma unroll
       for (int qi = 0; qi < 4; ++qi)
-        ow[qi] = owner_word(g, gb, wvg, j + (qi & 1), k + (qi >> 1), m);
+        ow[qi] = owner_word(g, gb, o, sl.rw0, j + (qi & 1), k + (qi >> 1), m);
     }
     long long tri = t0;
-    for (uint32_t u = active_cells(w, xmask); u; u &= u - 1) {
+    for (uint32_t u = active_cells(w, low_mask(g.nx - 1 - 32 * m)); u; u &= u - 1) {
       const int q = __ffs(u) - 1;
       const int i = 32 * m + q;
-      const uint64_t cw = kMcCase[case_of(w, q)];
+      const uint64_t cw = s_case[case_of(w, q)];
       const int nt = (int)(cw >> 60);
       for (int tt = 0; tt < nt; ++tt, ++tri) {
 #pragma unroll
         for (int corner = 0; corner < 3; ++corner) {
           const int e = mc_edge(cw, 3 * tt + corner);
-          const int info_e = kEdgeOwner[e];
+          const int info_e = s_edge[e];
           const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
           const int axis = info_e >> 3;
           if (MERGE) {
@@ -348,14 +650,14 @@ __global__ void __launch_bounds__(256) k_mc_emit(GridSet S, const uint32_t* __re
             if ((ii >> 5) == m) {
               vid = owner_rank_id(ow[dj + 2 * dk], ii & 31, axis);
             } else {  // the owner point is the first point of the next word
-              const OwnerWord o = owner_word(g, gb, wvg, j + dj, k + dk, m + 1);
-              vid = owner_rank_id(o, 0, axis);
+              const OwnerWord ox = owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1);
+              vid = owner_rank_id(ox, 0, axis);
             }
             conn[3 * tri + corner] = (int32_t)(vid - vbase0);
           } else {
             const long long vid = 3 * tri + corner;
             conn[vid] = (int32_t)(vid - vbase0);
-            emit_vertex(g, f, iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
+            emit_vertex(g, sl.field, sl.iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
           }
         }
       }
@@ -363,37 +665,37 @@ __global__ void __launch_bounds__(256) k_mc_emit(GridSet S, const uint32_t* __re
   }
 }
 
-void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const uint32_t* wt,
-                    const uint32_t* wv, const uint32_t* act, Info* info, float* verts,
-                    long long vcap, int32_t* conn, long long tcap, int32_t* ra, int32_t* rb,
-                    float* rw, int num_sms, cudaStream_t s) {
-  // the active count lives on the device: launch one resident wave, grid-stride
+void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
+                    Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
+                    int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s) {
+  // the active count lives on the device: one resident wave, grid-stride
   const long long want = (S.rowwords + 255) / 256;
   if (merge) {
-    const int blocks = resident_blocks(k_mc_emit<true>, 256, 0, num_sms, want);
-    k_mc_emit<true><<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, info, verts, vcap, conn, tcap,
-                                           ra, rb, rw);
+    const int bv = resident_blocks(k_mc_emit_vertices, 256, 0, num_sms, want);
+    k_mc_emit_vertices<<<bv, 256, 0, s>>>(S, bits, o, info, verts, vcap, tcap, ra, rb, rw);
+    const int bt = resident_blocks(k_mc_emit_triangles<true>, 256, 0, num_sms, want);
+    k_mc_emit_triangles<true><<<bt, 256, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap,
+                                                 ra, rb, rw);
   } else {
-    const int blocks = resident_blocks(k_mc_emit<false>, 256, 0, num_sms, want);
-    k_mc_emit<false><<<blocks, 256, 0, s>>>(S, bits, wt, wv, act, info, verts, vcap, conn, tcap,
-                                            ra, rb, rw);
+    const int bt = resident_blocks(k_mc_emit_triangles<false>, 256, 0, num_sms, want);
+    k_mc_emit_triangles<false><<<bt, 256, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap,
+                                                  ra, rb, rw);
   }
 }
 
 // Per-grid offsets: goff[2g], goff[2g+1] = first triangle / merged vertex of
 // grid g; goff[2G], goff[2G+1] = totals.
-__global__ void k_grid_offsets(GridSet S, const uint32_t* __restrict__ wt,
-                               const uint32_t* __restrict__ wv, long long* __restrict__ goff) {
+__global__ void k_grid_offsets(GridSet S, WordOffsets o, long long* __restrict__ goff) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= S.count; i += gridDim.x * blockDim.x) {
     const long long w = i < S.count ? load_slot(S, i).rw0 : S.rowwords;
-    goff[2 * i] = wt[w];
-    goff[2 * i + 1] = wv[w];
+    goff[2 * i] = word_t(o, w);
+    goff[2 * i + 1] = word_v(o, w);
   }
 }
 
-void launch_grid_offsets(const GridSet& S, const uint32_t* wt, const uint32_t* wv,
-                         long long* goff, cudaStream_t s) {
-  k_grid_offsets<<<(S.count + 256) / 256, 256, 0, s>>>(S, wt, wv, goff);
+void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff,
+                         cudaStream_t s) {
+  k_grid_offsets<<<(S.count + 256) / 256, 256, 0, s>>>(S, o, goff);
 }
 
 // CompactPointField: out[v] = Lerp(in[first], in[second], weight).
