@@ -88,6 +88,7 @@ SIGNATURES = {
     "dax_gb300_mc_batch_capture": ([vp, i32, vp, sz, vp, i64, vp, i64, ctypes.POINTER(vp)], i32),
     "dax_gb300_graph_launch": ([vp, vp], i32),
     "dax_gb300_graph_destroy": ([vp], i32),
+    "dax_gb300_mc_noalloc": ([gp, vp, f32, i32, vp, i64, vp, i64, vp, vp], i32),
 }
 
 

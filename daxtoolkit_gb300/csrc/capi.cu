@@ -208,6 +208,10 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
 
 }  // namespace
 
+namespace daxgb {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace daxgb
+
 // Batched marching cubes plan (host side of dax_gb300_mc_batch).
 struct dax_gb300_mc_batch {
   int count = 0;

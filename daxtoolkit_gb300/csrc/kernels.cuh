@@ -2,11 +2,15 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
 
 namespace daxgb {
+
+// Sets the message dax_gb300_last_error() returns on this thread.
+void set_last_error(const std::string& msg);
 
 // Bits words allocated for P points: whole 128-point chunks plus padding
 // that unaligned 64-bit fetches may touch.

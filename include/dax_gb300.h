@@ -142,6 +142,31 @@ int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t*
                                       const float* d_rec_weight, int64_t n, const float* d_in,
                                       float* d_out, void* stream);
 
+/* Marching cubes that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory where they need
+ * the isosurface -- code that runs inside a memory budget reserved up front
+ * (its own pool owns the device), code that must not take allocator locks or
+ * risk an out-of-memory failure on a latency-critical path, and plugin hosts
+ * that hand a plugin only the buffers they pass in.  Same results as
+ * dax_gb300_mc_count + dax_gb300_mc_generate (merge as there), but the
+ * scratch is a 32 MiB array compiled into this library, held by every GPU
+ * that loads it until the process exits; grids whose scratch
+ * (dax_gb300_mc_scratch_bytes) exceeds 32 MiB -- about 360^3 points -- are
+ * rejected with DAX_GB300_ERROR_UNSUPPORTED before any work is queued.  Calls
+ * no cudaMalloc, cudaFree or other allocating routine.  All calls on a
+ * device share that one array, and each call leaves its contents behind
+ * (the count pass clears what must start at zero): calls whose work overlaps
+ * on the GPU -- on different streams, or from different host threads -- race
+ * and must be serialised by the caller.  The first call on each device looks
+ * up the array's device address; make that first call outside any stream
+ * capture.  d_totals (device int64[3]) receives the triangle count, the
+ * vertex count of the merged output, and the device error bits (0 = ok; 2 =
+ * an output capacity was too small and nothing was written).
+ * Asynchronous. */
+int dax_gb300_mc_noalloc(const dax_gb300_uniform_grid* grid, const float* d_field, float isovalue,
+                         int merge, float* d_verts, int64_t vert_capacity, int32_t* d_conn,
+                         int64_t tri_capacity, int64_t* d_totals, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Batched marching cubes: many grids, one launch per pass                   */
 /* ------------------------------------------------------------------------ */
