@@ -50,6 +50,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the adjoint / batched / threshold / gradient measurements")
     return p.parse_args()
 
 
@@ -198,6 +200,130 @@ def run_reference(args, rank, world):
         "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _event_ms(fn, reps, stream):
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
+    """The rest of the headline metric: forward+adjoint against forward on the
+    same 512^3 field; the 64-grid batched pipeline (one CUDA-graph replay)
+    against the plain per-grid loop; threshold [0.3, 0.7] and CellGradient.
+    All device-timed with CUDA events (the plain loop and the batched replay
+    include the host read of the output sizes each iteration, which a caller
+    needs to use the result)."""
+    import torch
+    from daxtoolkit_gb300 import capi, cont, synthetic
+    L = capi.lib()
+    s = ctypes.c_void_p(stream.cuda_stream)
+    ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    g = grid.desc()
+    nx, ny, nz = dims
+    P, C = nx * ny * nz, (nx - 1) * (ny - 1) * (nz - 1)
+    out = {}
+
+    # --- forward (merged MC + CellGradient) vs forward + adjoint -----------
+    nbytes = L.dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
+    T, V = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(T), ctypes.byref(V), s)
+    T, V = T.value, V.value
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+    grad = torch.empty((C, 3), dtype=torch.float32, device=dev)
+    dverts = torch.randn((V, 3), dtype=torch.float32, device=dev)
+    dgrad = torch.randn((C, 3), dtype=torch.float32, device=dev)
+    dfield = torch.empty_like(field)
+
+    def fwd():
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
+        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(field), iso, 1, ptr(scratch),
+                  nbytes, ptr(verts), V, ptr(conn), T, None, None, None, s)
+        capi.call("dax_gb300_cell_gradient", ctypes.byref(g), ptr(field), ptr(grad), s)
+
+    def bwd():  # recomputes the count pass instead of keeping it
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
+        capi.call("dax_gb300_field_adjoint", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes,
+                  ptr(dverts), ptr(dgrad), ptr(dfield), s)
+
+    t_f = _event_ms(fwd, reps, stream)
+    t_fb = _event_ms(lambda: (fwd(), bwd()), reps, stream)
+    out["adjoint"] = {"workload": "merged MC + CellGradient forward, adjoint of both, %d^3" % nx,
+                      "fwd_ms": t_f, "fwd_adj_ms": t_fb, "ratio": t_fb / t_f, "target_ratio": 3.0}
+
+    # --- CellGradient and threshold ----------------------------------------
+    t_g = _event_ms(lambda: capi.call("dax_gb300_cell_gradient", ctypes.byref(g), ptr(field),
+                                      ptr(grad), s), reps, stream)
+    gb = (4 * P + 12 * C) / (t_g / 1e3) / 1e9
+    out["cell_gradient"] = {"ms": t_g, "cells_per_s": C / (t_g / 1e3), "achieved_gbs": gb,
+                            "frac": gb / peak, "algorithmic_bytes": 4 * P + 12 * C}
+    tb = L.dax_gb300_threshold_scratch_bytes(ctypes.byref(g))
+    tscr = torch.empty(tb, dtype=torch.uint8, device=dev)
+    capi.call("dax_gb300_threshold_count", ctypes.byref(g), ptr(field), 0.3, 0.7, ptr(tscr), tb, s)
+    K, U = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_threshold_totals", ptr(tscr), ctypes.byref(K), ctypes.byref(U), s)
+    K, U = K.value, U.value
+    tconn = torch.empty((K, 8), dtype=torch.int32, device=dev)
+    tcoords = torch.empty((U, 3), dtype=torch.float32, device=dev)
+    tfield = torch.empty(U, dtype=torch.float32, device=dev)
+
+    def thr():
+        capi.call("dax_gb300_threshold_count", ctypes.byref(g), ptr(field), 0.3, 0.7, ptr(tscr), tb, s)
+        capi.call("dax_gb300_threshold_generate", ctypes.byref(g), ptr(field), 0.3, 0.7, ptr(tscr),
+                  tb, ptr(tconn), K, ptr(tcoords), ptr(tfield), U, s)
+
+    t_t = _event_ms(thr, reps, stream)
+    tbytes = 4 * P + 32 * K + 16 * U
+    out["threshold"] = {"range": [0.3, 0.7], "kept_cells": K, "used_points": U, "ms": t_t,
+                        "cells_per_s": C / (t_t / 1e3),
+                        "achieved_gbs": tbytes / (t_t / 1e3) / 1e9,
+                        "frac": tbytes / (t_t / 1e3) / 1e9 / peak,
+                        "algorithmic_bytes": tbytes, "formula": "4P + 32K + 16U"}
+    del scratch, tscr, grad, dgrad, dfield, tconn, tcoords, tfield
+
+    # --- 64 uneven grids: batched graph replay vs per-grid loop -------------
+    gdims = synthetic.batch_grid_dims(64, 32, 192, 777)
+    isos = synthetic.batch_isovalues(64, 0.3, 0.6, 777)
+    grids, fields = [], []
+    for k, d in enumerate(gdims):
+        grids.append(cont.UniformGrid(d, spacing=tuple(1.0 / (x - 1) for x in d)))
+        fields.append(synthetic.blob_field(d, 4, seed=1000 + k, noise=0.05, device=dev))
+    cells = sum((d[0] - 1) * (d[1] - 1) * (d[2] - 1) for d in gdims)
+
+    def plain():
+        for gr, f, v in zip(grids, fields, isos):
+            cont.marching_cubes(gr, f, v, merge=True)
+
+    batch = cont.MarchingCubesBatch(grids, fields, isos)
+    bv, bc, toff, voff = batch.run(merge=True)
+    gv = torch.empty_like(bv)
+    gc = torch.empty_like(bc)
+    batch.capture(gv, gc, merge=True)
+
+    def batched():
+        batch.replay()
+        batch.totals()
+
+    t_plain = _event_ms(plain, 5, stream)
+    t_batch = _event_ms(batched, 20, stream)
+    ok = bool(torch.equal(gv, bv) and torch.equal(gc, bc))
+    out["batched"] = {"grids": 64, "grid_dims": "each U{32..192}, seed 777", "cells": cells,
+                      "triangles": toff[-1], "plain_loop_ms": t_plain, "batched_graph_ms": t_batch,
+                      "speedup": t_plain / t_batch, "target_speedup": 3.0,
+                      "batched_cells_per_s": cells / (t_batch / 1e3),
+                      "graph_replay_matches_batch_run": ok}
+    return out
 
 
 def config_dict(n):
@@ -371,9 +497,13 @@ def main():
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 4 * P,
                 "d2h_bytes_per_step": 12 * V + 12 * T, "ms_per_step": 1e3 * t_e2e,
                 "steps": e2e_steps},
-        "gpu_launches": 3 * args.steps,
+        # K1, K2a, K2b and the two K3 emit kernels per step (the scratch
+        # clear is a memset, not a kernel)
+        "gpu_launches": 5 * args.steps,
         "clocks": clocks,
     }
+    if not args.no_extras:
+        line.update(extra_measurements(field, grid, dims, iso, peak, stream, dev))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fh = field.cpu().numpy()
         cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)
