@@ -6,9 +6,17 @@
 // order without fused multiply-add, and x6 - x0 the difference of the two
 // implicit corner coordinates (not the spacing: both are rounded floats).
 //
-// One thread per cell in cell-id order.  Reads 4 B/point from HBM (the 8
-// corner loads of neighbouring cells hit L1/L2), writes 12 B/cell: the write
-// dominates, so the kernel is HBM-write bound.
+// A warp marches along z over a tile of 31 cells in x by kGradBand cell
+// rows in y and kSeg cell planes.  Each step loads one point plane of the
+// tile (kGradBand + 1 rows of 32 points, coalesced; lane 31's points are the
+// +x corners of lane 30's cells, and every +x neighbour comes from the next
+// lane) and keeps the previous plane in registers, so every field value is
+// read from HBM once (plus the band's halo row and the segment's halo
+// plane).  Each lane writes its cell's 12 bytes as one 8-byte store on the
+// 8-byte-aligned half plus one 4-byte store.  (Staging a row through shared
+// memory into fully coalesced stores measured slower on GB300: the warp
+// synchronisation behind the correctly rounded divides costs more than the
+// partial sectors save.)  Algorithmic traffic: 4 B/point + 12 B/cell.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -23,49 +31,95 @@ __device__ __forceinline__ float dw(unsigned neg_mask, int v) {
   return ((neg_mask >> v) & 1u) ? -0.25f : 0.25f;
 }
 
-__global__ void __launch_bounds__(256) k_cell_gradient(Grid g, const float* __restrict__ f,
-                                                       float* __restrict__ out) {
-  const int cx = g.nx - 1, cy = g.ny - 1;
-  const long long C = (long long)cx * cy * (g.nz - 1);
-  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
-       c += (long long)gridDim.x * blockDim.x) {
-    const long long row = c / cx;
-    const int i = (int)(c - row * cx);
-    const int j = (int)(row % cy);
-    const int k = (int)(row / cy);
-    const long long p0 = i + (long long)g.nx * (j + (long long)g.ny * k);
-    float v[8];
-    v[0] = __ldg(f + p0);
-    v[1] = __ldg(f + p0 + 1);
-    v[2] = __ldg(f + p0 + dy + 1);
-    v[3] = __ldg(f + p0 + dy);
-    v[4] = __ldg(f + p0 + dz);
-    v[5] = __ldg(f + p0 + dz + 1);
-    v[6] = __ldg(f + p0 + dz + dy + 1);
-    v[7] = __ldg(f + p0 + dz + dy);
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+// One point plane of a warp's tile: rows j0 .. j0 + kGradBand of point column i
+// (zero outside the grid).
+__device__ __forceinline__ void load_point_plane(const Grid& g, const float* __restrict__ f, int i,
+                                                 int j0, int k, float (&F)[kGradBand + 1]) {
 #pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      sx = __fadd_rn(sx, __fmul_rn(v[n], dw(kNegX, n)));
-      sy = __fadd_rn(sy, __fmul_rn(v[n], dw(kNegY, n)));
-      sz = __fadd_rn(sz, __fmul_rn(v[n], dw(kNegZ, n)));
-    }
-    const float wx = __fsub_rn(coord(g.ox, g.sx, i + 1, g.mx), coord(g.ox, g.sx, i, g.mx));
-    const float wy = __fsub_rn(coord(g.oy, g.sy, j + 1, g.my), coord(g.oy, g.sy, j, g.my));
-    const float wz = __fsub_rn(coord(g.oz, g.sz, k + 1, g.mz), coord(g.oz, g.sz, k, g.mz));
-    out[3 * c + 0] = __fdiv_rn(sx, wx);
-    out[3 * c + 1] = __fdiv_rn(sy, wy);
-    out[3 * c + 2] = __fdiv_rn(sz, wz);
+  for (int t = 0; t <= kGradBand; ++t) {
+    const int j = j0 + t;
+    const long long p = (long long)i + (long long)g.nx * (j + (long long)g.ny * k);
+    F[t] = (j < g.ny && i < g.nx) ? __ldg(f + p) : 0.0f;
   }
 }
 
+__global__ void __launch_bounds__(kMarchWarps * 32, kGradMinBlocks)
+    k_cell_gradient(Grid g, const float* __restrict__ f, float* __restrict__ out, MarchTiles mt) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long task = (long long)blockIdx.x * kMarchWarps + wib;
+  if (task >= mt.tasks) return;  // the whole warp leaves; no block barrier follows
+  const int xw = (int)(task % mt.nxw);
+  const long long t2 = task / mt.nxw;
+  const int band = (int)(t2 % mt.nband), seg = (int)(t2 / mt.nband);
+  const int cx = g.nx - 1, cy = g.ny - 1, cz = g.nz - 1;
+  // lanes 0..30 own cell columns i; lane 31 only supplies point column i
+  const int i = kMarchCols * xw + lane;
+  const bool own = lane < kMarchCols && i < cx;
+  const int j0 = band * kGradBand;
+  const int k0 = seg * kSeg, k1 = min(k0 + kSeg, cz);
+  const float wx =
+      own ? __fsub_rn(coord(g.ox, g.sx, i + 1, g.mx), coord(g.ox, g.sx, i, g.mx)) : 1.0f;
+
+  float F0[kGradBand + 1], F1[kGradBand + 1];
+  load_point_plane(g, f, i, j0, k0, F0);
+  for (int kc = k0; kc < k1; ++kc) {
+    load_point_plane(g, f, i, j0, kc + 1, F1);
+    const float wz = __fsub_rn(coord(g.oz, g.sz, kc + 1, g.mz), coord(g.oz, g.sz, kc, g.mz));
+    // row t of both planes at columns i and i + 1, carried from row to row
+    float a0 = F0[0], b0 = F1[0];
+    float a0n = __shfl_down_sync(kFull, a0, 1), b0n = __shfl_down_sync(kFull, b0, 1);
+#pragma unroll
+    for (int t = 0; t < kGradBand; ++t) {
+      const int jc = j0 + t;
+      if (jc >= cy) break;  // uniform across the warp
+      const float a1 = F0[t + 1], b1 = F1[t + 1];
+      const float a1n = __shfl_down_sync(kFull, a1, 1), b1n = __shfl_down_sync(kFull, b1, 1);
+      if (own) {
+        const float v[8] = {a0, a0n, a1n, a1, b0, b0n, b1n, b1};
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          sx = __fadd_rn(sx, __fmul_rn(v[n], dw(kNegX, n)));
+          sy = __fadd_rn(sy, __fmul_rn(v[n], dw(kNegY, n)));
+          sz = __fadd_rn(sz, __fmul_rn(v[n], dw(kNegZ, n)));
+        }
+        const float wy = __fsub_rn(coord(g.oy, g.sy, jc + 1, g.my), coord(g.oy, g.sy, jc, g.my));
+        const long long c = (long long)i + (long long)cx * (jc + (long long)cy * kc);
+        float* o = out + 3 * c;
+        const float gx = __fdiv_rn(sx, wx), gy = __fdiv_rn(sy, wy), gz = __fdiv_rn(sz, wz);
+        if ((c & 1) == 0) {  // byte offset 12 c is 8-byte aligned
+          *reinterpret_cast<float2*>(o) = make_float2(gx, gy);
+          o[2] = gz;
+        } else {             // byte offset 12 c + 4 is 8-byte aligned
+          o[0] = gx;
+          *reinterpret_cast<float2*>(o + 1) = make_float2(gy, gz);
+        }
+      }
+      a0 = a1;
+      a0n = a1n;
+      b0 = b1;
+      b0n = b1n;
+    }
+#pragma unroll
+    for (int t = 0; t <= kGradBand; ++t) F0[t] = F1[t];
+  }
+}
+
+MarchTiles march_tiles(int nx, int ny, int nz, int band) {
+  MarchTiles mt;
+  mt.nxw = (nx + kMarchCols - 1) / kMarchCols;
+  mt.nband = (ny + band - 1) / band;
+  mt.nseg = (nz + kSeg - 1) / kSeg;
+  mt.tasks = (long long)mt.nxw * mt.nband * mt.nseg;
+  return mt;
+}
+
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s) {
-  const long long C = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1);
-  const long long want = (C + 255) / 256;
-  const long long cap = (long long)num_sms * 16;
-  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
-  k_cell_gradient<<<blocks, 256, 0, s>>>(g, f, out);
+  (void)num_sms;
+  const MarchTiles mt = march_tiles(g.nx - 1, g.ny - 1, g.nz - 1, kGradBand);  // cell tiles
+  if (mt.tasks < 1) return;
+  const long long blocks = (mt.tasks + kMarchWarps - 1) / kMarchWarps;
+  k_cell_gradient<<<(unsigned)blocks, kMarchWarps * 32, 0, s>>>(g, f, out, mt);
 }
 
 }  // namespace daxgb

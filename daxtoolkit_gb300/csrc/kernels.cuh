@@ -98,6 +98,28 @@ void launch_thr_emit(const Grid& g, const float* f, const uint32_t* bits, const 
                      long long kcap, float* coords, float* fout, long long ucap, int num_sms,
                      cudaStream_t s);
 
+// z-marching stencil kernels (CellGradient and its adjoint): one warp per
+// tile of kMarchCols columns in x (the 32nd lane supplies the +x/-x
+// neighbour column), a band of rows in y and kSeg planes in z, marched
+// along z; kMarchWarps warps (independent tiles) per block.  Band heights
+// and register budgets (blocks per SM) were chosen by timing on GB300.
+constexpr int kMarchCols = 31;
+constexpr int kSeg = 32;
+constexpr int kMarchWarps = 8;
+constexpr int kGradBand = 4;        // cell rows per CellGradient tile
+constexpr int kGradMinBlocks = 4;
+constexpr int kAdjBand = 8;         // point rows per adjoint tile
+constexpr int kAdjMinBlocks = 3;
+
+struct MarchTiles {
+  int nxw, nband, nseg;  // tiles along x, y, z
+  long long tasks;       // nxw * nband * nseg, x fastest
+};
+// Tiles covering an nx x ny x nz box of cells or points, `band` rows each.
+MarchTiles march_tiles(int nx, int ny, int nz, int band);
+
+// dL/dfield from dL/d(merged vertices) (needs the count pass's bits and
+// word offsets) and/or dL/d(cell gradients); out is fully written.
 void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32_t* bits,
                           const WordOffsets* o, const float* dverts, const float* dgrad,
                           float* out, int num_sms, cudaStream_t s);

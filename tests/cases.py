@@ -112,4 +112,14 @@ def gradient_cases():
     d = (33, 17, 5)
     out.append(("odd_33x17x5_offset", d, (-1.5, 2.25, 0.125), (0.3, 0.7, 1.1), (3, -2, 7),
                 random_blobs(d, 3, 12)))
+    # ragged tiles in every direction (69 cells in x, 18 rows, 40 planes) and a
+    # far origin, so the cell widths differ by rounding from column to column
+    d = (70, 19, 41)
+    out.append(("ragged_70x19x41_far", d, (1000.0, -4.1, 250.0), (0.013, 0.7, 0.05), (-5, 2, 100),
+                random_blobs(d, 4, 17, noise=0.1)))
+    # exact tiles: 32 cells in x, 8 rows, 33 planes (one plane past a segment)
+    d = (33, 9, 34)
+    out.append(("exact_tiles_33x9x34", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 3, 18)))
+    out.append(("single_cell", (2, 2, 2), (0.5, 0.5, 0.5), (2.0, 3.0, 4.0), (0, 0, 0),
+                np.arange(8, dtype=np.float32) ** 2))
     return out
