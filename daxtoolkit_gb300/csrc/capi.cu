@@ -1,8 +1,11 @@
 // C ABI over the sm_103a kernels (declared in include/dax_gb300.h).
 //
-// Scratch layout (one buffer, caller-owned, 256-byte aligned sections):
-//   [Info][look-back status: 2 x tiles x u64][row_a: (R+1) x i64]
-//   [row_b: (R+1) x i64][bits: bit_words(P) x u32][used: R x wr x u32 (threshold)]
+// Scratch layout (one buffer, caller-owned, 256-byte aligned sections), with
+// W = R x wr row words:
+//   marching cubes: [Info][look-back status: 3 x tiles x u64][wc: W x u32]
+//                   [wt: (W+1) x u32][wv: (W+1) x u32][act: W x u32]
+//                   [bits: bit_words(P) x u32]
+//   threshold:      the same, then [kept: W x u32][used: W x u32]
 // Only the Info block and the status words are cleared per call (a few KB);
 // every other byte is fully rewritten by the kernels before it is read.
 #include <cstdio>
@@ -111,23 +114,20 @@ McLayout mc_layout(const Grid& g) {
   return mc_layout_words(g.R * g.wr, daxgb::bit_words(g.P), sizeof(Info));
 }
 
-// Threshold scratch: [Info][status 2 x tiles][row_a][row_b][bits][used].
+// Threshold scratch: the marching-cubes sections, then the per-word kept-cell
+// and used-point masks.
 struct Layout {
-  int tiles;
-  size_t info, status, row_a, row_b, bits, used, total, clear;
+  McLayout m;
+  size_t kept, used, total;
 };
 
 Layout layout(const Grid& g) {
   Layout L;
-  L.tiles = (int)((g.R + daxgb::kRowsPerTile - 1) / daxgb::kRowsPerTile);
-  L.info = 0;
-  L.status = align256(sizeof(Info));
-  L.row_a = align256(L.status + 2 * (size_t)L.tiles * 8);
-  L.clear = L.row_a;
-  L.row_b = align256(L.row_a + (size_t)(g.R + 1) * 8);
-  L.bits = align256(L.row_b + (size_t)(g.R + 1) * 8);
-  L.used = align256(L.bits + (size_t)daxgb::bit_words(g.P) * 4);
-  L.total = align256(L.used + (size_t)g.R * g.wr * 4);
+  const long long W = g.R * g.wr;
+  L.m = mc_layout_words(W, daxgb::bit_words(g.P), sizeof(Info));
+  L.kept = L.m.total;
+  L.used = align256(L.kept + 4 * (size_t)W);
+  L.total = align256(L.used + 4 * (size_t)W);
   return L;
 }
 
@@ -195,15 +195,17 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
     return check_launch("count/scan kernels");
   }
   const Layout L = layout(g);
-  cudaError_t e = cudaMemsetAsync(scratch, 0, L.clear, s);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, L.m.clear, s);
   if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
-  uint32_t* bits = at<uint32_t>(scratch, L.bits);
+  uint32_t* bits = at<uint32_t>(scratch, L.m.bits);
   daxgb::launch_classify_bits(1, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
   if ((st = check_launch("classify kernel"))) return st;
-  daxgb::launch_thr_rows(g, bits, at<uint32_t>(scratch, L.used), at<long long>(scratch, L.row_a),
-                         at<long long>(scratch, L.row_b), at<unsigned long long>(scratch, L.status),
-                         at<Info>(scratch, L.info), L.tiles, s);
-  return check_launch("row count/scan kernel");
+  const daxgb::WordOffsets o = L.m.offsets(scratch);
+  daxgb::launch_thr_count(g, bits, at<uint32_t>(scratch, L.kept), at<uint32_t>(scratch, L.used),
+                          o.wc, sms, s);
+  daxgb::launch_word_scan(g.R * g.wr, o.wc, o.wt, o.wv, o.act, o.status,
+                          at<Info>(scratch, L.m.info), s);
+  return check_launch("threshold count/scan kernels");
 }
 
 }  // namespace
@@ -217,7 +219,7 @@ struct dax_gb300_mc_batch {
   int count = 0;
   std::vector<daxgb::GridSlot> slots;
   daxgb::GridSlot* d_slots = nullptr;
-  long long rows = 0, chunks = 0, words = 0, blocks = 0, rowwords = 0;
+  long long rows = 0, chunks = 0, words = 0, rowwords = 0;
   int max_wr = 1;
   bool aligned = true;
   size_t off_goff = 0;
@@ -229,7 +231,6 @@ struct dax_gb300_mc_batch {
     S.count = count;
     S.rows = rows;
     S.chunks = chunks;
-    S.blocks = blocks;
     S.rowwords = rowwords;
     if (count == 1) S.one = slots[0];
     return S;
@@ -379,9 +380,8 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
   const Layout L = layout(g);
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_threshold_scratch_bytes()");
-  daxgb::launch_thr_emit(g, d_field, at<uint32_t>(d_scratch, L.bits),
-                         at<uint32_t>(d_scratch, L.used), at<long long>(d_scratch, L.row_a),
-                         at<long long>(d_scratch, L.row_b), at<Info>(d_scratch, L.info), d_conn,
+  daxgb::launch_thr_emit(g, d_field, L.m.offsets(d_scratch), at<uint32_t>(d_scratch, L.kept),
+                         at<uint32_t>(d_scratch, L.used), at<Info>(d_scratch, L.m.info), d_conn,
                          cell_capacity, d_coords, d_field_out, point_capacity, num_sms(),
                          static_cast<cudaStream_t>(stream));
   return check_launch("threshold generate kernel");
@@ -446,10 +446,8 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
     sl.chunk0 = b->chunks;
     sl.word0 = 4 * b->chunks;
     sl.row0 = b->rows;
-    sl.blk0 = b->blocks;
     sl.rw0 = b->rowwords;
     b->rowwords += g.R * g.wr;
-    b->blocks += (long long)g.nz * ((g.ny + daxgb::kRowsPerEmitBlock - 1) / daxgb::kRowsPerEmitBlock);
     b->chunks += (g.P + 127) / 128;
     b->rows += g.R;
     if (g.wr > b->max_wr) b->max_wr = g.wr;

@@ -16,17 +16,6 @@ void set_last_error(const std::string& msg);
 // that unaligned 64-bit fetches may touch.
 inline long long bit_words(long long P) { return ((P + 127) / 128) * 4 + 8; }
 
-constexpr int kRowsPerTile = 256;      // rows per look-back tile in K2
-constexpr int kRowsPerEmitBlock = 8;   // rows per block in K3 (one warp each)
-
-// Lanes that cooperate on one point row in K2/K3: the power of two >= the
-// row's word count, at most a warp.
-inline int lanes_per_row(int wr) {
-  int g = 1;
-  while (g < wr && g < 32) g <<= 1;
-  return g;
-}
-
 // A GridSet holding one grid (no device table).
 inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
   GridSet S{};
@@ -34,7 +23,6 @@ inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
   S.count = 1;
   S.rows = g.R;
   S.chunks = (g.P + 127) / 128;
-  S.blocks = (long long)g.nz * ((g.ny + kRowsPerEmitBlock - 1) / kRowsPerEmitBlock);
   S.rowwords = g.R * g.wr;
   S.one.g = g;
   S.one.field = field;
@@ -43,7 +31,6 @@ inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
   S.one.chunk0 = 0;
   S.one.word0 = 0;
   S.one.row0 = 0;
-  S.one.blk0 = 0;
   S.one.rw0 = 0;
   return S;
 }
@@ -78,6 +65,10 @@ struct WordOffsets {
 };
 
 int mc_scan_tiles(long long rowwords);
+// K2b alone: scan packed per-word counts wc (a << 16 | b) into wt (a), wv (b),
+// act (words with either) and info's totals.
+void launch_word_scan(long long rowwords, const uint32_t* wc, uint32_t* wt, uint32_t* wv,
+                      uint32_t* act, unsigned long long* status, Info* info, cudaStream_t s);
 void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32_t* wt,
                     uint32_t* wv, uint32_t* act, unsigned long long* status, Info* info,
                     int num_sms, cudaStream_t s);
@@ -90,13 +81,13 @@ void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s);
 
-void launch_thr_rows(const Grid& g, const uint32_t* bits, uint32_t* used, long long* row_k,
-                     long long* row_u, unsigned long long* status, Info* info, int tiles,
-                     cudaStream_t s);
-void launch_thr_emit(const Grid& g, const float* f, const uint32_t* bits, const uint32_t* used,
-                     const long long* row_k, const long long* row_u, Info* info, int32_t* conn,
-                     long long kcap, float* coords, float* fout, long long ucap, int num_sms,
-                     cudaStream_t s);
+// Threshold over row words: per word the kept-cell and used-point masks and
+// the packed counts (kept << 16) | used for launch_word_scan; then the emit.
+void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint32_t* used,
+                      uint32_t* wc, int num_sms, cudaStream_t s);
+void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const uint32_t* kept,
+                     const uint32_t* used, Info* info, int32_t* conn, long long kcap,
+                     float* coords, float* fout, long long ucap, int num_sms, cudaStream_t s);
 
 // z-marching stencil kernels (CellGradient and its adjoint): one warp per
 // tile of kMarchCols columns in x (the 32nd lane supplies the +x/-x

@@ -403,8 +403,13 @@ void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32
   const long long want = (S.rowwords + 256 * kCountWords - 1) / (256 * kCountWords);
   const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, want);
   k_mc_count<<<b1, 256, 0, s>>>(S, bits, wc);
-  const int tiles = mc_scan_tiles(S.rowwords);
-  k_mc_scan<<<tiles, 256, 0, s>>>(S.rowwords, wc, wt, wv, act, status, info, tiles);
+  launch_word_scan(S.rowwords, wc, wt, wv, act, status, info, s);
+}
+
+void launch_word_scan(long long rowwords, const uint32_t* wc, uint32_t* wt, uint32_t* wv,
+                      uint32_t* act, unsigned long long* status, Info* info, cudaStream_t s) {
+  const int tiles = mc_scan_tiles(rowwords);
+  k_mc_scan<<<tiles, 256, 0, s>>>(rowwords, wc, wt, wv, act, status, info, tiles);
 }
 
 // ---------------------------------------------------------------------------
