@@ -2,12 +2,12 @@
 //
 // Scratch layout (one buffer, caller-owned, 256-byte aligned sections), with
 // W = R x wr row words:
-//   marching cubes: [Info][look-back status: 3 x tiles x u64][wc: W x u32]
+//   marching cubes: [Info][tile totals: 3 x tiles x u32][wc: W x u32]
 //                   [wt: (W+1) x u32][wv: (W+1) x u32][act: W x u32]
 //                   [bits: bit_words(P) x u32]
 //   threshold:      the same, then [kept: W x u32][used: W x u32]
-// Only the Info block and the status words are cleared per call (a few KB);
-// every other byte is fully rewritten by the kernels before it is read.
+// Nothing is cleared per call: every byte, the Info block included, is
+// written by the count pass before anything reads it.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -86,22 +86,21 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Marching-cubes scratch: [Info][status 3 x tiles][wc][wt][wv][act][bits].
+// Marching-cubes scratch: [Info][tile totals 3 x tiles][wc][wt][wv][act][bits].
 struct McLayout {
   long long rowwords;
   int tiles;
-  size_t info, status, wc, wt, wv, act, bits, total, clear;
+  size_t info, tile, wc, wt, wv, act, bits, total;
   daxgb::WordOffsets offsets(void* base) const;
 };
 
 McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head) {
   McLayout L;
   L.rowwords = rowwords;
-  L.tiles = daxgb::mc_scan_tiles(rowwords);
+  L.tiles = daxgb::word_scan_tiles(rowwords);
   L.info = 0;
-  L.status = align256(head);
-  L.clear = align256(L.status + 3 * 8 * (size_t)L.tiles);
-  L.wc = L.clear;
+  L.tile = align256(head);
+  L.wc = align256(L.tile + 3 * 4 * (size_t)L.tiles);
   L.wt = align256(L.wc + 4 * (size_t)rowwords);
   L.wv = align256(L.wt + 4 * (size_t)(rowwords + 1));
   L.act = align256(L.wv + 4 * (size_t)(rowwords + 1));
@@ -142,7 +141,7 @@ daxgb::WordOffsets McLayout::offsets(void* base) const {
   o.wt = at<uint32_t>(base, wt);
   o.wv = at<uint32_t>(base, wv);
   o.act = at<uint32_t>(base, act);
-  o.status = at<unsigned long long>(base, status);
+  o.tile = at<uint32_t>(base, tile);
   return o;
 }
 
@@ -184,27 +183,22 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
   const daxgb::GridSet S = daxgb::single_set(g, field, a, b);
   if (mode == 0) {
     const McLayout L = mc_layout(g);
-    cudaError_t e = cudaMemsetAsync(scratch, 0, L.clear, s);
-    if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
     uint32_t* bits = at<uint32_t>(scratch, L.bits);
     daxgb::launch_classify_bits(0, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
     if ((st = check_launch("classify kernel"))) return st;
     const daxgb::WordOffsets o = L.offsets(scratch);
-    daxgb::launch_mc_scan(S, bits, o.wc, o.wt, o.wv, o.act, o.status, at<Info>(scratch, L.info),
-                          sms, s);
+    daxgb::launch_mc_scan(S, bits, o, at<Info>(scratch, L.info), sms, s);
     return check_launch("count/scan kernels");
   }
   const Layout L = layout(g);
-  cudaError_t e = cudaMemsetAsync(scratch, 0, L.m.clear, s);
-  if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
   uint32_t* bits = at<uint32_t>(scratch, L.m.bits);
   daxgb::launch_classify_bits(1, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
   if ((st = check_launch("classify kernel"))) return st;
   const daxgb::WordOffsets o = L.m.offsets(scratch);
   daxgb::launch_thr_count(g, bits, at<uint32_t>(scratch, L.kept), at<uint32_t>(scratch, L.used),
-                          o.wc, sms, s);
-  daxgb::launch_word_scan(g.R * g.wr, o.wc, o.wt, o.wv, o.act, o.status,
-                          at<Info>(scratch, L.m.info), s);
+                          o.wc, o.tile, sms, s);
+  daxgb::launch_word_scan(g.R * g.wr, o.wc, o.tile, o.wt, o.wv, o.act, at<Info>(scratch, L.m.info),
+                          s);
   return check_launch("threshold count/scan kernels");
 }
 
@@ -486,16 +480,13 @@ int dax_gb300_mc_batch_count(dax_gb300_mc_batch* b, void* d_scratch, size_t scra
   if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
   if (scratch_bytes < b->L.total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(d_scratch, 0, b->L.clear, s);
-  if (e != cudaSuccess) return cuda_fail(e, "clearing scratch");
   const daxgb::GridSet S = b->set();
   uint32_t* bits = at<uint32_t>(d_scratch, b->L.bits);
   daxgb::launch_classify_bits(0, S, b->aligned, bits, b->words, num_sms(), s);
   int st = check_launch("batch classify kernel");
   if (st) return st;
   const daxgb::WordOffsets o = b->L.offsets(d_scratch);
-  daxgb::launch_mc_scan(S, bits, o.wc, o.wt, o.wv, o.act, o.status, at<Info>(d_scratch, 0),
-                        num_sms(), s);
+  daxgb::launch_mc_scan(S, bits, o, at<Info>(d_scratch, 0), num_sms(), s);
   if ((st = check_launch("batch count/scan kernels"))) return st;
   daxgb::launch_grid_offsets(S, b->L.offsets(d_scratch), at<long long>(d_scratch, b->off_goff), s);
   return check_launch("batch offsets kernel");

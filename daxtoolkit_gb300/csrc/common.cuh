@@ -155,4 +155,30 @@ __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long 
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Block-wide sums of three per-thread values (256 threads); all threads get
+// the totals.  s holds 3 x 8 scratch words.
+__device__ __forceinline__ void block_sum3(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t* s) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(kFull, a, o);
+    b += __shfl_xor_sync(kFull, b, o);
+    c += __shfl_xor_sync(kFull, c, o);
+  }
+  if (lane == 0) {
+    s[warp] = a;
+    s[8 + warp] = b;
+    s[16 + warp] = c;
+  }
+  __syncthreads();
+  a = b = c = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    a += s[w];
+    b += s[8 + w];
+    c += s[16 + w];
+  }
+  __syncthreads();
+}
+
 }  // namespace daxgb

@@ -52,25 +52,27 @@ inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long
   return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
-// Marching cubes over row words: K2a counts every row word into wc, K2b
-// scans them into per-word exclusive triangle / vertex offsets wt, wv
-// (uint32[rowwords + 1]; entry rowwords holds the totals) and the compacted
-// list of active words act.
+// Row-word count passes write packed per-word counts wc = (a << 16) | b and,
+// per tile of kScanTile words, the totals of a, of b and of non-zero words
+// (tile[0 / 1 / 2][tiles]); launch_word_scan turns them into per-word
+// exclusive offsets wt (a), wv (b) (uint32[rowwords + 1]; entry rowwords
+// holds the totals), the compacted list act of the non-zero words, and the
+// totals and error word in Info.
+constexpr int kScanItems = 16;               // words per thread in a tile
+constexpr int kScanTile = 256 * kScanItems;  // words per tile
 struct WordOffsets {
-  uint32_t* wc;   // [rowwords] packed counts (triangles << 16) | edges
-  uint32_t* wt;   // [rowwords + 1]
-  uint32_t* wv;   // [rowwords + 1]
-  uint32_t* act;  // [rowwords]
-  unsigned long long* status;  // [3][tiles] look-back state
+  uint32_t* wc;    // [rowwords] packed counts
+  uint32_t* wt;    // [rowwords + 1]
+  uint32_t* wv;    // [rowwords + 1]
+  uint32_t* act;   // [rowwords]
+  uint32_t* tile;  // [3][tiles] per-tile totals
 };
 
-int mc_scan_tiles(long long rowwords);
-// K2b alone: scan packed per-word counts wc (a << 16 | b) into wt (a), wv (b),
-// act (words with either) and info's totals.
-void launch_word_scan(long long rowwords, const uint32_t* wc, uint32_t* wt, uint32_t* wv,
-                      uint32_t* act, unsigned long long* status, Info* info, cudaStream_t s);
-void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32_t* wt,
-                    uint32_t* wv, uint32_t* act, unsigned long long* status, Info* info,
+int word_scan_tiles(long long rowwords);
+void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
+                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s);
+// Marching cubes K2a (counts: triangles, crossing edges) + K2b.
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
                     int num_sms, cudaStream_t s);
 void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
                     Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
@@ -81,10 +83,11 @@ void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s);
 
-// Threshold over row words: per word the kept-cell and used-point masks and
-// the packed counts (kept << 16) | used for launch_word_scan; then the emit.
+// Threshold over row words: per word the kept-cell and used-point masks, the
+// packed counts (kept << 16) | used and the tile totals for
+// launch_word_scan; then the emit.
 void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint32_t* used,
-                      uint32_t* wc, int num_sms, cudaStream_t s);
+                      uint32_t* wc, uint32_t* tile_tot, int num_sms, cudaStream_t s);
 void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const uint32_t* kept,
                      const uint32_t* used, Info* info, int32_t* conn, long long kcap,
                      float* coords, float* fout, long long ucap, int num_sms, cudaStream_t s);

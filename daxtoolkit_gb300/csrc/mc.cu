@@ -4,26 +4,29 @@
 // i = 32m .. 32m+31 of that row (and the cells whose first point they are);
 // row words are numbered r * wr + m, which is point order.
 //
-// K2 (k_mc_scan): for every row word
+// K2a (k_mc_count): for every row word
 //     T = triangles of its cells            = sum NumFaces[case(i)]
 //     V = crossing edges its points own      = edges (p, p + e_axis) whose end
 //         points classify differently, axis x < y < z
 //     A = 1 if T or V is non-zero
-//   and a single-pass decoupled look-back scan (three chains) over tiles of
-//   1024 words turns them into exclusive offsets per word plus a compacted
-//   list of the active words.  V counts exactly the vertices of the merged
-//   output: a cell's triangle-table row references exactly its sign-change
-//   edges, every grid edge belongs to a cell, and the reference's merged
-//   order, ascending (first id, second id), is ascending (owner point, axis)
-//   on a uniform grid -- point order, then axis.  So the reference's
-//   Sort/Unique/LowerBounds (dax/cont/DispatcherGenerateInterpolatedCells.h:
-//   276-291) becomes a rank: offset of the owner word + popcount.
+//   plus per-tile totals; K2b (k_word_scan) turns them into exclusive
+//   offsets per word and a compacted list of the active words
+//   (reduce-then-scan: no block waits on another).  V counts exactly the
+//   vertices of the merged output: a cell's triangle-table row references
+//   exactly its sign-change edges, every grid edge belongs to a cell, and
+//   the reference's merged order, ascending (first id, second id), is
+//   ascending (owner point, axis) on a uniform grid -- point order, then
+//   axis.  So the reference's Sort/Unique/LowerBounds
+//   (dax/cont/DispatcherGenerateInterpolatedCells.h:276-291) becomes a rank:
+//   offset of the owner word + popcount.
 //
-// K3 (k_mc_emit): one thread per ACTIVE word (from the compacted list):
-//   recompute cases from the bits, write the word's vertices at its V offset
-//   and its cells' triangles at its T offset; a triangle corner's vertex id
-//   is the V offset of the edge's owner word plus the edge's rank inside it.
-//   Field values are read only at crossing-edge end points.
+// K3 (k_mc_emit): warps take 32 active words at a time and deal their active
+//   cells to the lanes; a cell writes its triangles at its word's T offset
+//   plus the counts of the word's earlier active cells, a triangle corner's
+//   vertex id is the V offset of the edge's owner word plus the edge's rank
+//   inside it, and each merged vertex is written by the one cell that is its
+//   owner point's own.  Field values are read only at crossing-edge end
+//   points.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mc_case.cuh"
@@ -89,14 +92,7 @@ __device__ __forceinline__ void crossing_masks(const Grid& g, const uint32_t* bi
 }
 
 // ---------------------------------------------------------------------------
-// K2: counts per row word, then a single-pass scan.
-//   K2a (k_mc_count): one thread per word; writes the packed counts
-//       wc[w] = (triangles << 16) | crossing edges (both < 2^16: a word has
-//       32 points and 32 cells).  No synchronisation.
-//   K2b (k_mc_scan): single-pass decoupled look-back scan of wc (tiles of
-//       4096 words, 16 per thread), writing per-word exclusive triangle and
-//       vertex offsets wt / wv (uint32[rowwords + 1]) and the compacted list
-//       act of active words (uint32[A]).
+// K2: counts per row word, then the scan.
 
 // The eight corner words of word m of row r (a, a+x of rows (j..j+1,
 // k..k+1)) and the masks that decide which of them are meaningful.
@@ -162,148 +158,128 @@ __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, 
   }
 }
 
-constexpr int kCountWords = 4;  // consecutive row words per thread in K2a
+constexpr int kCountWords = 4;  // consecutive row words per count group
 
+// K2a: one 256-thread block per tile of kScanTile row words (grid-stride
+// over tiles).  Thread t counts the 4-word groups t + 256 e (e = 0..3) of
+// the tile, so a warp's groups are consecutive; the block then writes the
+// tile's totals (triangles, crossing edges, active words) to
+// tile_tot[0 / 1 / 2][tile] for the scan.
 __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __restrict__ bits,
-                                                  uint32_t* __restrict__ wc) {
+                                                  uint32_t* __restrict__ wc,
+                                                  uint32_t* __restrict__ tile_tot, int tiles) {
   __shared__ unsigned char s_nf[256];  // NumFaces, indexed by divergent case ids
+  __shared__ uint32_t s_red[24];
   s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
   __syncthreads();
-  const long long stride = (long long)gridDim.x * blockDim.x * kCountWords;
-  for (long long g0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kCountWords;
-       g0 < S.rowwords; g0 += stride) {
-    int si, m;
-    unsigned r;
-    locate_word(S, g0, si, r, m);
-    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-    const Grid& g = sl.g;
-    uint32_t out[kCountWords] = {0, 0, 0, 0};
-    const bool cells = g.nx >= 2 && g.ny >= 2 && g.nz >= 2;
-    if (cells && m + kCountWords <= g.wr && g0 + kCountWords <= S.rowwords &&
-        (S.count == 1 || g0 + kCountWords <= sl.rw0 + (long long)g.R * g.wr)) {
-      // fast path: the four words lie in one row
-      const uint32_t* gb = bits + sl.word0;
-      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-      const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
-      const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-      const long long pos = (long long)r * g.nx + 32ll * m;
-      uint32_t a[4], a1[4], b[4] = {0, 0, 0, 0}, b1[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0},
-               c1[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0}, d1[4] = {0, 0, 0, 0};
-      row_windows4(gb, pos, a, a1);
-      if (hy) row_windows4(gb, pos + dy, b, b1);
-      if (hz) row_windows4(gb, pos + dz, c, c1);
-      if (hy && hz) row_windows4(gb, pos + dy + dz, d, d1);
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    uint32_t st = 0, sv = 0, sa = 0;
+#pragma unroll 1
+    for (int e = 0; e < kScanItems / kCountWords; ++e) {
+      const long long g0 = (long long)tile * kScanTile + (long long)(threadIdx.x + 256 * e) * kCountWords;
+      if (g0 >= S.rowwords) break;
+      int si, m;
+      unsigned r;
+      locate_word(S, g0, si, r, m);
+      const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+      const Grid& g = sl.g;
+      uint32_t out[kCountWords] = {0, 0, 0, 0};
+      const bool cells = g.nx >= 2 && g.ny >= 2 && g.nz >= 2;
+      if (cells && m + kCountWords <= g.wr && g0 + kCountWords <= S.rowwords &&
+          (S.count == 1 || g0 + kCountWords <= sl.rw0 + (long long)g.R * g.wr)) {
+        // fast path: the four words lie in one row
+        const uint32_t* gb = bits + sl.word0;
+        const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+        const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+        const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+        const long long pos = (long long)r * g.nx + 32ll * m;
+        uint32_t a[4], a1[4], b[4] = {0, 0, 0, 0}, b1[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0},
+                 c1[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0}, d1[4] = {0, 0, 0, 0};
+        row_windows4(gb, pos, a, a1);
+        if (hy) row_windows4(gb, pos + dy, b, b1);
+        if (hz) row_windows4(gb, pos + dz, c, c1);
+        if (hy && hz) row_windows4(gb, pos + dy + dz, d, d1);
 #pragma unroll
-      for (int e = 0; e < kCountWords; ++e) {
-        const CornerWords w{a[e], a1[e], b[e], b1[e], c[e], c1[e], d[e], d1[e]};
-        out[e] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + e)),
-                               low_mask(g.nx - 1 - 32 * (m + e)), s_nf);
-      }
-    } else {
-      // words that straddle a row or grid end: one at a time
+        for (int q = 0; q < kCountWords; ++q) {
+          const CornerWords w{a[q], a1[q], b[q], b1[q], c[q], c1[q], d[q], d1[q]};
+          out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + q)),
+                                 low_mask(g.nx - 1 - 32 * (m + q)), s_nf);
+        }
+      } else {
+        // words that straddle a row or grid end: one at a time
 #pragma unroll
-      for (int e = 0; e < kCountWords; ++e) {
-        const long long gw = g0 + e;
-        if (gw >= S.rowwords) break;
-        int se, me;
-        unsigned re;
-        locate_word(S, gw, se, re, me);
-        const GridSlot& sle = S.count == 1 ? S.one : S.slots[se];
-        if (sle.g.nx >= 2 && sle.g.ny >= 2 && sle.g.nz >= 2) {
-          const WordBits wb = load_word_bits(sle.g, bits + sle.word0, re, me);
-          out[e] = packed_counts(wb.w, wb.hy, wb.hz, wb.pmask, wb.xmask, s_nf);
+        for (int q = 0; q < kCountWords; ++q) {
+          const long long gw = g0 + q;
+          if (gw >= S.rowwords) break;
+          int sq, mq;
+          unsigned rq;
+          locate_word(S, gw, sq, rq, mq);
+          const GridSlot& slq = S.count == 1 ? S.one : S.slots[sq];
+          if (slq.g.nx >= 2 && slq.g.ny >= 2 && slq.g.nz >= 2) {
+            const WordBits wb = load_word_bits(slq.g, bits + slq.word0, rq, mq);
+            out[q] = packed_counts(wb.w, wb.hy, wb.hz, wb.pmask, wb.xmask, s_nf);
+          }
         }
       }
-    }
-    if (g0 + kCountWords <= S.rowwords) {
-      *reinterpret_cast<uint4*>(wc + g0) = make_uint4(out[0], out[1], out[2], out[3]);
-    } else {
+      if (g0 + kCountWords <= S.rowwords) {
+        *reinterpret_cast<uint4*>(wc + g0) = make_uint4(out[0], out[1], out[2], out[3]);
+      } else {
 #pragma unroll
-      for (int e = 0; e < kCountWords; ++e)
-        if (g0 + e < S.rowwords) wc[g0 + e] = out[e];
-    }
-  }
-}
-
-// Look-back by one warp over N independent status chains (status + c *
-// stride + tile), same flag protocol and bounded waiting as warp_lookback.
-template <int N>
-__device__ __forceinline__ void warp_lookback_n(unsigned long long* st, int stride, int tile,
-                                                const long long (&agg)[N], int* err,
-                                                long long (&ex)[N]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int c = 0; c < N; ++c) ex[c] = 0;
-  if (lane == 0) {
-    const unsigned long long f = tile == 0 ? kFlagInc : kFlagAgg;
-#pragma unroll
-    for (int c = 0; c < N; ++c) st_release(st + c * stride + tile, f | (unsigned long long)agg[c]);
-  }
-  if (tile == 0) return;
-  bool done[N];
-#pragma unroll
-  for (int c = 0; c < N; ++c) done[c] = false;
-  int p = tile - 1, spins = 0;
-  while (true) {
-    bool all = true;
-#pragma unroll
-    for (int c = 0; c < N; ++c) all = all && done[c];
-    if (all) break;
-    const int idx = p - lane;
-    unsigned long long w[N];
-    int first[N];
-    bool missing = false;
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      w[c] = (!done[c] && idx >= 0) ? ld_acquire(st + c * stride + idx) : kFlagInc;
-      const unsigned inc = __ballot_sync(kFull, (w[c] >> 62) == 2u);
-      const unsigned none = __ballot_sync(kFull, (w[c] >> 62) == 0u);
-      first[c] = inc ? __ffs(inc) - 1 : 32;
-      const unsigned need = first[c] >= 31 ? kFull : ((2u << first[c]) - 1u);
-      missing = missing || (none & need);
-    }
-    if (missing) {
-      if (++spins > kSpinLimit) {
-        if (lane == 0) atomicOr(err, kErrTimeout);
-        break;
+        for (int q = 0; q < kCountWords; ++q)
+          if (g0 + q < S.rowwords) wc[g0 + q] = out[q];
       }
-      if (spins > 16) __nanosleep(32);
-      continue;
+#pragma unroll
+      for (int q = 0; q < kCountWords; ++q) {
+        st += out[q] >> 16;
+        sv += out[q] & 0xffffu;
+        sa += out[q] ? 1u : 0u;
+      }
     }
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      long long v = (lane <= first[c] && idx >= 0) ? (long long)(w[c] & kValMask) : 0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-      if (!done[c]) ex[c] += v;
-      done[c] = done[c] || first[c] < 32;
+    block_sum3(st, sv, sa, s_red);
+    if (threadIdx.x == 0) {
+      tile_tot[tile] = st;
+      tile_tot[tiles + tile] = sv;
+      tile_tot[2 * tiles + tile] = sa;
     }
-    p -= 32;
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int c = 0; c < N; ++c)
-      st_release(st + c * stride + tile, kFlagInc | (unsigned long long)(ex[c] + agg[c]));
   }
 }
 
-constexpr int kScanItems = 16;                 // words per thread
-constexpr int kScanTile = 256 * kScanItems;    // words per tile
-
-__global__ void __launch_bounds__(256) k_mc_scan(long long rowwords,
-                                                 const uint32_t* __restrict__ wc,
-                                                 uint32_t* __restrict__ wt,
-                                                 uint32_t* __restrict__ wv,
-                                                 uint32_t* __restrict__ act,
-                                                 unsigned long long* __restrict__ status,
-                                                 Info* __restrict__ info, int tiles) {
-  __shared__ int s_tile;
-  __shared__ uint32_t s_wt[8], s_wv[8], s_wa[8];
-  __shared__ long long s_ex[3];
+// K2b: scan of the packed per-word counts wc = (a << 16) | b with the tile
+// totals tile_tot[0 / 1 / 2][tiles] (sums of a, of b and of non-zero words)
+// written by the count pass: reduce-then-scan, so no block waits on
+// another.  Block `tile` sums the totals of the tiles before it, scans its
+// own kScanTile words and writes the exclusive offsets wt (a) and wv (b),
+// the compacted list act of its non-zero words, and -- the last tile -- the
+// totals, the end entries wt[rowwords] / wv[rowwords] and the error word.
+__global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
+                                                   const uint32_t* __restrict__ wc,
+                                                   const uint32_t* __restrict__ tile_tot,
+                                                   int tiles, uint32_t* __restrict__ wt,
+                                                   uint32_t* __restrict__ wv,
+                                                   uint32_t* __restrict__ act,
+                                                   Info* __restrict__ info) {
+  __shared__ uint32_t s_red[24];
+  __shared__ unsigned long long s_pre[3 * 8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_tile = (int)atomicAdd(&info->ticket, 1u);
-  __syncthreads();
-  const int tile = s_tile;
+  const int tile = blockIdx.x;
+  // exclusive prefix over the tiles before this one (64-bit: totals may pass 2^32)
+  unsigned long long pt = 0, pv = 0, pa = 0;
+  for (int x = tid; x < tile; x += 256) {
+    pt += __ldg(tile_tot + x);
+    pv += __ldg(tile_tot + tiles + x);
+    pa += __ldg(tile_tot + 2 * tiles + x);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pt += __shfl_xor_sync(kFull, pt, o);
+    pv += __shfl_xor_sync(kFull, pv, o);
+    pa += __shfl_xor_sync(kFull, pa, o);
+  }
+  if (lane == 0) {
+    s_pre[warp] = pt;
+    s_pre[8 + warp] = pv;
+    s_pre[16 + warp] = pa;
+  }
   const long long w0 = (long long)tile * kScanTile + (long long)tid * kScanItems;
   uint32_t c[kScanItems];
   const bool full = w0 + kScanItems <= rowwords;
@@ -335,31 +311,24 @@ __global__ void __launch_bounds__(256) k_mc_scan(long long rowwords,
                    ua = __shfl_up_sync(kFull, ia, o);
     if (lane >= o) { it += ut; iv += uv; ia += ua; }
   }
-  if (lane == 31) { s_wt[warp] = it; s_wv[warp] = iv; s_wa[warp] = ia; }
+  if (lane == 31) { s_red[warp] = it; s_red[8 + warp] = iv; s_red[16 + warp] = ia; }
   __syncthreads();
   uint32_t bt = 0, bv = 0, ba = 0, tt = 0, tv = 0, ta = 0;
+  unsigned long long et = 0, ev = 0, ea = 0;
 #pragma unroll
   for (int w = 0; w < 8; ++w) {
-    if (w < warp) { bt += s_wt[w]; bv += s_wv[w]; ba += s_wa[w]; }
-    tt += s_wt[w];
-    tv += s_wv[w];
-    ta += s_wa[w];
+    if (w < warp) { bt += s_red[w]; bv += s_red[8 + w]; ba += s_red[16 + w]; }
+    tt += s_red[w];
+    tv += s_red[8 + w];
+    ta += s_red[16 + w];
+    et += s_pre[w];
+    ev += s_pre[8 + w];
+    ea += s_pre[16 + w];
   }
-  if (warp == 0) {
-    const long long agg[3] = {(long long)tt, (long long)tv, (long long)ta};
-    long long ex[3];
-    warp_lookback_n<3>(status, tiles, tile, agg, &info->error, ex);
-    if (lane == 0) {
-      s_ex[0] = ex[0];
-      s_ex[1] = ex[1];
-      s_ex[2] = ex[2];
-    }
-  }
-  __syncthreads();
   // offsets are stored as uint32; a total above 2^31 - 1 is reported below
-  uint32_t ot = (uint32_t)s_ex[0] + bt + it - st;
-  uint32_t ov = (uint32_t)s_ex[1] + bv + iv - sv;
-  long long oa = s_ex[2] + ba + ia - sa;
+  uint32_t ot = (uint32_t)et + bt + it - st;
+  uint32_t ov = (uint32_t)ev + bv + iv - sv;
+  long long oa = (long long)ea + ba + ia - sa;
 #pragma unroll
   for (int q = 0; q < kScanItems / 4; ++q) {
     uint32_t t4[4], v4[4];
@@ -385,35 +354,36 @@ __global__ void __launch_bounds__(256) k_mc_scan(long long rowwords,
     }
   }
   if (tile == tiles - 1 && tid == 0) {
-    const long long T = s_ex[0] + tt, V = s_ex[1] + tv;
+    const long long T = (long long)(et + tt), V = (long long)(ev + tv);
     wt[rowwords] = (uint32_t)T;
     wv[rowwords] = (uint32_t)V;
     info->total_a = T;
     info->total_b = V;
-    info->total_c = s_ex[2] + ta;
-    if (T > 2147483647ll || V > 2147483647ll) atomicOr(&info->error, kErrOverflow);
+    info->total_c = (long long)(ea + ta);
+    info->error = (T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0;
   }
 }
 
-int mc_scan_tiles(long long rowwords) { return (int)((rowwords + kScanTile - 1) / kScanTile); }
-
-void launch_mc_scan(const GridSet& S, const uint32_t* bits, uint32_t* wc, uint32_t* wt,
-                    uint32_t* wv, uint32_t* act, unsigned long long* status, Info* info,
-                    int num_sms, cudaStream_t s) {
-  const long long want = (S.rowwords + 256 * kCountWords - 1) / (256 * kCountWords);
-  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, want);
-  k_mc_count<<<b1, 256, 0, s>>>(S, bits, wc);
-  launch_word_scan(S.rowwords, wc, wt, wv, act, status, info, s);
+int word_scan_tiles(long long rowwords) {
+  return (int)((rowwords + kScanTile - 1) / kScanTile);
 }
 
-void launch_word_scan(long long rowwords, const uint32_t* wc, uint32_t* wt, uint32_t* wv,
-                      uint32_t* act, unsigned long long* status, Info* info, cudaStream_t s) {
-  const int tiles = mc_scan_tiles(rowwords);
-  k_mc_scan<<<tiles, 256, 0, s>>>(rowwords, wc, wt, wv, act, status, info, tiles);
+void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
+                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s) {
+  const int tiles = word_scan_tiles(rowwords);
+  k_word_scan<<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info);
+}
+
+void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
+                    int num_sms, cudaStream_t s) {
+  const int tiles = word_scan_tiles(S.rowwords);
+  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles);
+  k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
+  launch_word_scan(S.rowwords, o.wc, o.tile, o.wt, o.wv, o.act, info, s);
 }
 
 // ---------------------------------------------------------------------------
-// K3: emit, one thread per active row word.
+// K3: emit.
 
 // Vertex on the edge owned by point (i, j, k) along `axis`:
 // weight = (iso - f[A]) / (f[B] - f[A]) (dax/worklet/MarchingCubes.h:160-161),
@@ -478,12 +448,7 @@ __device__ __forceinline__ long long owner_rank_id(const OwnerWord& o, int b, in
   return id;
 }
 
-// K3: two kernels over the A active words (A on the device, the words in
-// the compacted list act).  k_mc_emit_vertices writes the merged
-// vertices a word's points own; k_mc_emit_triangles writes its cells'
-// triangles (and, unmerged, their corner vertices).  Splitting the roles
-// keeps each thread's chain of dependent memory round trips short and each
-// kernel's register count low.
+// Capacity and error check before any output is written; A = active words.
 __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long vcap, bool merge,
                                            long long& A) {
   const long long T = info->total_a;
@@ -497,149 +462,164 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
   return true;
 }
 
-constexpr int kVertexBatch = 4;
+// One warp's staging of 32 active words, structure-of-arrays so that lane L
+// writes column L without bank conflicts: per word the corner bit words, the
+// crossing masks and first vertex ids of the four owner rows q = dj + 2 dk
+// (rows (j + dj, k + dk) at word m), the active-cell mask, the first
+// triangle, the global row word and the grid slot.
+enum EmitField {
+  kFWin = 0,     // 8: a, a1, b, b1, c, c1, d, d1
+  kFOx = 8,      // 4
+  kFOy = 12,     // 4
+  kFOz = 16,     // 4
+  kFOv = 20,     // 4
+  kFAm = 24,
+  kFT0 = 25,
+  kFWord = 26,
+  kFSlot = 27,
+  kFields = 28
+};
+constexpr int kEmitWarps = 8;
 
-__global__ void __launch_bounds__(256) k_mc_emit_vertices(GridSet S,
-                                                          const uint32_t* __restrict__ bits,
-                                                          WordOffsets o,
-                                                          Info* __restrict__ info,
-                                                          float* __restrict__ verts, long long vcap,
-                                                          long long tcap,
-                                                          int32_t* __restrict__ ra,
-                                                          int32_t* __restrict__ rb,
-                                                          float* __restrict__ rw) {
-  long long A;
-  if (!emit_guard(info, tcap, vcap, true, A)) return;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < A; it += stride) {
-    const long long gw = __ldg(o.act + it);
-    const long long v0 = word_v(o, gw), v1 = word_v(o, gw + 1);
-    if (v1 == v0) continue;
-    int si, m;
-    unsigned r;
-    locate_word(S, gw, si, r, m);
-    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-    const Grid& g = sl.g;
-    const uint32_t* gb = bits + sl.word0;
-    const float* f = sl.field;
-    const float iso = sl.iso;
-    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-    const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-    const long long pos = (long long)r * g.nx + 32ll * m;
-    const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
-    const uint32_t pmask = low_mask(g.nx - 32 * m);
-    uint32_t a, a1, b = 0, c = 0;
-    bits_at2(gb, pos, a, a1);
-    if (hy) b = bits_at(gb, pos + dy);
-    if (hz) c = bits_at(gb, pos + dz);
-    uint32_t ux = (a ^ a1) & low_mask(g.nx - 1 - 32 * m);
-    uint32_t uy = hy ? (a ^ b) & pmask : 0u;
-    uint32_t uz = hz ? (a ^ c) & pmask : 0u;
-    // edges in (point, axis) order, in batches whose field loads are all
-    // issued before any arithmetic
-    long long vid = v0;
-    while (ux | uy | uz) {
-      int ei[kVertexBatch], ea[kVertexBatch];
-      int nb = 0;
-#pragma unroll
-      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
-        const uint32_t u = ux | uy | uz;
-        if (u == 0) break;
-        const int q = __ffs(u) - 1;
-        const uint32_t bit = 1u << q;
-        int ax;
-        if (ux & bit) { ax = 0; ux &= ~bit; }
-        else if (uy & bit) { ax = 1; uy &= ~bit; }
-        else { ax = 2; uz &= ~bit; }
-        ei[nb] = 32 * m + q;
-        ea[nb] = ax;
-        ++nb;
-      }
-      float fa[kVertexBatch], fb[kVertexBatch];
-#pragma unroll
-      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
-        if (s2 < nb) {
-          const long long pa = (long long)r * g.nx + ei[s2];
-          fa[s2] = __ldg(f + pa);
-          fb[s2] = __ldg(f + pa + (ea[s2] == 0 ? 1ll : (ea[s2] == 1 ? dy : dz)));
-        }
-      }
-#pragma unroll
-      for (int s2 = 0; s2 < kVertexBatch; ++s2) {
-        if (s2 < nb) {
-          const int i = ei[s2], ax = ea[s2];
-          const float w = __fdiv_rn(__fsub_rn(iso, fa[s2]), __fsub_rn(fb[s2], fa[s2]));
-          const float xa = coord(g.ox, g.sx, i, g.mx), ya = coord(g.oy, g.sy, j, g.my),
-                      za = coord(g.oz, g.sz, k, g.mz);
-          const float xb = ax == 0 ? coord(g.ox, g.sx, i + 1, g.mx) : xa;
-          const float yb = ax == 1 ? coord(g.oy, g.sy, j + 1, g.my) : ya;
-          const float zb = ax == 2 ? coord(g.oz, g.sz, k + 1, g.mz) : za;
-          verts[3 * vid + 0] = lerp_rn(xa, xb, w);
-          verts[3 * vid + 1] = lerp_rn(ya, yb, w);
-          verts[3 * vid + 2] = lerp_rn(za, zb, w);
-          const long long pa = (long long)r * g.nx + i;
-          if (ra) ra[vid] = (int32_t)pa;
-          if (rb) rb[vid] = (int32_t)(pa + (ax == 0 ? 1ll : (ax == 1 ? dy : dz)));
-          if (rw) rw[vid] = w;
-          ++vid;
-        }
-      }
-    }
-  }
-}
+__device__ __forceinline__ uint32_t window(const uint32_t* st, int f, int s) { return st[f * 32 + s]; }
 
 template <bool MERGE>
-__global__ void __launch_bounds__(256) k_mc_emit_triangles(GridSet S,
-                                                           const uint32_t* __restrict__ bits,
-                                                           WordOffsets o,
-                                                           Info* __restrict__ info,
-                                                           float* __restrict__ verts,
-                                                           long long vcap,
-                                                           int32_t* __restrict__ conn,
-                                                           long long tcap,
-                                                           int32_t* __restrict__ ra,
-                                                           int32_t* __restrict__ rb,
-                                                           float* __restrict__ rw) {
+__global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
+                                                            const uint32_t* __restrict__ bits,
+                                                            WordOffsets o,
+                                                            Info* __restrict__ info,
+                                                            float* __restrict__ verts,
+                                                            long long vcap,
+                                                            int32_t* __restrict__ conn,
+                                                            long long tcap,
+                                                            int32_t* __restrict__ ra,
+                                                            int32_t* __restrict__ rb,
+                                                            float* __restrict__ rw) {
   // case and edge tables in shared memory: lanes index them divergently
   __shared__ uint64_t s_case[256];
   __shared__ unsigned char s_edge[12];
+  __shared__ uint32_t s_stage[kEmitWarps][kFields * 32];
+  __shared__ int s_pre[kEmitWarps][33];
   s_case[threadIdx.x] = kMcCase[threadIdx.x];
   if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
   __syncthreads();
   long long A;
   if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < A; it += stride) {
-    const long long gw = __ldg(o.act + it);
-    const long long t0 = word_t(o, gw), t1 = word_t(o, gw + 1);
-    if (t1 == t0) continue;
-    int si, m;
-    unsigned r;
-    locate_word(S, gw, si, r, m);
-    const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-    const Grid& g = sl.g;
-    const uint32_t* gb = bits + sl.word0;
-    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-    const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-    const long long pos = (long long)r * g.nx + 32ll * m;
-    CornerWords w{};
-    bits_at2(gb, pos, w.a, w.a1);
-    bits_at2(gb, pos + dy, w.b, w.b1);
-    bits_at2(gb, pos + dz, w.c, w.c1);
-    bits_at2(gb, pos + dy + dz, w.d, w.d1);
-    // first vertex of this grid in the concatenated output (0 for one grid)
-    const long long vbase0 =
-        S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
-    OwnerWord ow[4];
-    if (MERGE) {
-#pragma unroll
-      for (int qi = 0; qi < 4; ++qi)
-        ow[qi] = owner_word(g, gb, o, sl.rw0, j + (qi & 1), k + (qi >> 1), m);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t* st = s_stage[wib];
+  int* pre = s_pre[wib];
+  const long long warp0 = (long long)blockIdx.x * kEmitWarps + wib;
+  const long long nwarps = (long long)gridDim.x * kEmitWarps;
+  for (long long a0 = warp0 * 32; a0 < A; a0 += nwarps * 32) {
+    // ---- lane = word: gather the word's bits, masks and offsets ----------
+    uint32_t am = 0;
+    if (a0 + lane < A) {
+      const uint32_t gw = __ldg(o.act + a0 + lane);
+      int si, m;
+      unsigned r;
+      locate_word(S, gw, si, r, m);
+      const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+      const Grid& g = sl.g;
+      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+      if (j < g.ny - 1 && k < g.nz - 1) {  // the row has cells
+        const uint32_t* gb = bits + sl.word0;
+        const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+        const long long pos = (long long)r * g.nx + 32ll * m;
+        CornerWords w;
+        bits_at2(gb, pos, w.a, w.a1);
+        bits_at2(gb, pos + dy, w.b, w.b1);
+        bits_at2(gb, pos + dz, w.c, w.c1);
+        bits_at2(gb, pos + dy + dz, w.d, w.d1);
+        const uint32_t xmask = low_mask(g.nx - 1 - 32 * m), pmask = low_mask(g.nx - 32 * m);
+        am = active_cells(w, xmask);
+        st[(kFWin + 0) * 32 + lane] = w.a;
+        st[(kFWin + 1) * 32 + lane] = w.a1;
+        st[(kFWin + 2) * 32 + lane] = w.b;
+        st[(kFWin + 3) * 32 + lane] = w.b1;
+        st[(kFWin + 4) * 32 + lane] = w.c;
+        st[(kFWin + 5) * 32 + lane] = w.c1;
+        st[(kFWin + 6) * 32 + lane] = w.d;
+        st[(kFWin + 7) * 32 + lane] = w.d1;
+        st[kFT0 * 32 + lane] = __ldg(o.wt + gw);
+        st[kFWord * 32 + lane] = gw;
+        st[kFSlot * 32 + lane] = (uint32_t)si;
+        if (MERGE && am) {
+          // owner rows (j, k), (j+1, k), (j, k+1), (j+1, k+1); the masks are
+          // those the count pass counted (X: +x, Y: +y, Z: +z crossing edges)
+          const bool y2 = j + 1 < g.ny - 1, z2 = k + 1 < g.nz - 1;
+          const uint32_t b2 = y2 ? bits_at(gb, pos + 2 * dy) : 0u;
+          const uint32_t c2 = z2 ? bits_at(gb, pos + 2 * dz) : 0u;
+          const uint32_t d2y = y2 ? bits_at(gb, pos + 2 * dy + dz) : 0u;
+          const uint32_t d2z = z2 ? bits_at(gb, pos + dy + 2 * dz) : 0u;
+          st[(kFOx + 0) * 32 + lane] = (w.a ^ w.a1) & xmask;
+          st[(kFOy + 0) * 32 + lane] = (w.a ^ w.b) & pmask;
+          st[(kFOz + 0) * 32 + lane] = (w.a ^ w.c) & pmask;
+          st[(kFOx + 1) * 32 + lane] = (w.b ^ w.b1) & xmask;
+          st[(kFOy + 1) * 32 + lane] = y2 ? (w.b ^ b2) & pmask : 0u;
+          st[(kFOz + 1) * 32 + lane] = (w.b ^ w.d) & pmask;
+          st[(kFOx + 2) * 32 + lane] = (w.c ^ w.c1) & xmask;
+          st[(kFOy + 2) * 32 + lane] = (w.c ^ w.d) & pmask;
+          st[(kFOz + 2) * 32 + lane] = z2 ? (w.c ^ c2) & pmask : 0u;
+          st[(kFOx + 3) * 32 + lane] = (w.d ^ w.d1) & xmask;
+          st[(kFOy + 3) * 32 + lane] = y2 ? (w.d ^ d2y) & pmask : 0u;
+          st[(kFOz + 3) * 32 + lane] = z2 ? (w.d ^ d2z) & pmask : 0u;
+          const uint32_t rwy = (uint32_t)g.wr, rwz = (uint32_t)g.wr * (uint32_t)g.ny;
+          st[(kFOv + 0) * 32 + lane] = __ldg(o.wv + gw);
+          st[(kFOv + 1) * 32 + lane] = __ldg(o.wv + gw + rwy);
+          st[(kFOv + 2) * 32 + lane] = __ldg(o.wv + gw + rwz);
+          st[(kFOv + 3) * 32 + lane] = __ldg(o.wv + gw + rwy + rwz);
+        }
+      }
     }
-    long long tri = t0;
-    for (uint32_t u = active_cells(w, low_mask(g.nx - 1 - 32 * m)); u; u &= u - 1) {
+    st[kFAm * 32 + lane] = am;
+    // ---- deal the warp's active cells to the lanes ----------------------
+    const int n = __popc(am);
+    int incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += v;
+    }
+    pre[lane + 1] = incl;
+    if (lane == 0) pre[0] = 0;
+    const int total = __shfl_sync(kFull, incl, 31);
+    __syncwarp();
+    for (int c = lane; c < total; c += 32) {
+      int s = 0;  // the last word whose prefix is <= c
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (pre[s + step] <= c) s += step;
+      // walk the word's active cells up to the c - pre[s]-th, summing their
+      // triangle counts (the cell's first triangle)
+      CornerWords w;
+      w.a = window(st, kFWin + 0, s);
+      w.a1 = window(st, kFWin + 1, s);
+      w.b = window(st, kFWin + 2, s);
+      w.b1 = window(st, kFWin + 3, s);
+      w.c = window(st, kFWin + 4, s);
+      w.c1 = window(st, kFWin + 5, s);
+      w.d = window(st, kFWin + 6, s);
+      w.d1 = window(st, kFWin + 7, s);
+      uint32_t u = window(st, kFAm, s);
+      long long tri = window(st, kFT0, s);
+      for (int t = c - pre[s]; t > 0; --t) {
+        tri += (int)(s_case[case_of(w, __ffs(u) - 1)] >> 60);
+        u &= u - 1;
+      }
       const int q = __ffs(u) - 1;
+      const uint32_t gw = window(st, kFWord, s);
+      const int si = (int)window(st, kFSlot, s);
+      const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+      const Grid& g = sl.g;
+      const uint32_t* gb = bits + sl.word0;
+      const unsigned lw = gw - (unsigned)sl.rw0;
+      const unsigned r = lw / (unsigned)g.wr;
+      const int m = (int)(lw - r * (unsigned)g.wr);
+      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
       const int i = 32 * m + q;
+      // first vertex of this grid in the concatenated output (0 for one grid)
+      const long long vbase0 =
+          S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
       const uint64_t cw = s_case[case_of(w, q)];
       const int nt = (int)(cw >> 60);
       for (int tt = 0; tt < nt; ++tt, ++tri) {
@@ -650,13 +630,17 @@ __global__ void __launch_bounds__(256) k_mc_emit_triangles(GridSet S,
           const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
           const int axis = info_e >> 3;
           if (MERGE) {
-            const int ii = i + di;
+            const int qq = dj + 2 * dk, ii = q + di;
             long long vid;
-            if ((ii >> 5) == m) {
-              vid = owner_rank_id(ow[dj + 2 * dk], ii & 31, axis);
+            if (ii < 32) {
+              OwnerWord ow;
+              ow.X = window(st, kFOx + qq, s);
+              ow.Y = window(st, kFOy + qq, s);
+              ow.Z = window(st, kFOz + qq, s);
+              ow.base = window(st, kFOv + qq, s);
+              vid = owner_rank_id(ow, ii, axis);
             } else {  // the owner point is the first point of the next word
-              const OwnerWord ox = owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1);
-              vid = owner_rank_id(ox, 0, axis);
+              vid = owner_rank_id(owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1), 0, axis);
             }
             conn[3 * tri + corner] = (int32_t)(vid - vbase0);
           } else {
@@ -666,25 +650,56 @@ __global__ void __launch_bounds__(256) k_mc_emit_triangles(GridSet S,
           }
         }
       }
+      if (MERGE) {
+        // merged vertices owned by the corners whose own cell this is: the
+        // first point always, a far corner only on the grid's last cell
+        // layer along each axis where it lies beyond
+        const bool ex = i == g.nx - 2, ey = j == g.ny - 2, ez = k == g.nz - 2;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const int di = cc & 1, dj = (cc >> 1) & 1, dk = cc >> 2;
+          if ((di && !ex) || (dj && !ey) || (dk && !ez)) continue;
+          const int qq = dj + 2 * dk, ii = q + di;
+          OwnerWord ow;
+          int bit;
+          if (ii < 32) {
+            ow.X = window(st, kFOx + qq, s);
+            ow.Y = window(st, kFOy + qq, s);
+            ow.Z = window(st, kFOz + qq, s);
+            ow.base = window(st, kFOv + qq, s);
+            bit = ii;
+          } else {
+            ow = owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1);
+            bit = 0;
+          }
+          const uint32_t own = (((ow.X >> bit) & 1u)) | (((ow.Y >> bit) & 1u) << 1) |
+                               (((ow.Z >> bit) & 1u) << 2);
+          if (!own) continue;
+#pragma unroll
+          for (int axis = 0; axis < 3; ++axis)
+            if ((own >> axis) & 1u)
+              emit_vertex(g, sl.field, sl.iso, i + di, j + dj, k + dk, axis,
+                          owner_rank_id(ow, bit, axis), verts, ra, rb, rw);
+        }
+      }
     }
+    __syncwarp();
   }
 }
 
 void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
                     Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
                     int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s) {
-  // the active count lives on the device: one resident wave, grid-stride
-  const long long want = (S.rowwords + 255) / 256;
+  // the active count lives on the device: one resident wave, warp-stride
+  const long long want = (S.rowwords + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
   if (merge) {
-    const int bv = resident_blocks(k_mc_emit_vertices, 256, 0, num_sms, want);
-    k_mc_emit_vertices<<<bv, 256, 0, s>>>(S, bits, o, info, verts, vcap, tcap, ra, rb, rw);
-    const int bt = resident_blocks(k_mc_emit_triangles<true>, 256, 0, num_sms, want);
-    k_mc_emit_triangles<true><<<bt, 256, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap,
-                                                 ra, rb, rw);
+    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want);
+    k_mc_emit<true><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
+                                                  rb, rw);
   } else {
-    const int bt = resident_blocks(k_mc_emit_triangles<false>, 256, 0, num_sms, want);
-    k_mc_emit_triangles<false><<<bt, 256, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap,
-                                                  ra, rb, rw);
+    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want);
+    k_mc_emit<false><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
+                                                   rb, rw);
   }
 }
 

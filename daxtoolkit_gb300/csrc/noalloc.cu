@@ -92,7 +92,7 @@ int dax_gb300_mc_noalloc(const dax_gb300_uniform_grid* grid, const float* d_fiel
   void* scratch = nullptr;
   int st = scratch_address(&scratch);
   if (st) return st;
-  // the count pass clears the part of the scratch that must start at zero
+  // the count pass writes every scratch byte the generate pass reads
   st = dax_gb300_mc_count(grid, d_field, isovalue, scratch, kNoAllocScratchBytes, stream);
   if (st) return st;
   st = dax_gb300_mc_generate(grid, d_field, isovalue, merge, scratch, kNoAllocScratchBytes, d_verts,

@@ -1,14 +1,16 @@
 // Cell threshold on the in-range bit stream (bit = lo <= f <= hi), on the
 // row-word pipeline marching cubes uses.
 //
-// K2a (k_thr_count): per row word w = (point row r = (j, k), word m)
+// K2a (k_thr_kept, k_thr_used): per row word w = (point row r = (j, k), word m)
 //     kept[w] = cells 32m .. 32m+31 of cell row r whose 8 corners are all in
 //               range (ThresholdFunction, dax/worklet/Threshold.h:30-66)
 //     used[w] = points 32m .. 32m+31 of point row r that are a corner of a
 //               kept cell (FillPointMask,
-//               dax/cont/DispatcherGenerateTopology.h:206-227)
-//     wc[w]   = popc(kept) << 16 | popc(used)
-// K2b (k_mc_scan, shared with marching cubes): per-word exclusive offsets
+//               dax/cont/DispatcherGenerateTopology.h:206-227): the OR of the
+//               kept masks of cell rows (j-1..j, k-1..k), each with its +x
+//               neighbour cell
+//     wc[w]   = popc(kept) << 16 | popc(used), and per-tile totals
+// K2b (k_word_scan, shared with marching cubes): per-word exclusive offsets
 //     wt (kept cells) and wv (used points), the compacted list act of the
 //     words with either, and the totals.
 // K3 (k_thr_emit): a warp loads 32 active words at once (lane = word), then
@@ -23,81 +25,86 @@
 
 namespace daxgb {
 
-namespace {
-
-// Cells of point row (j+dj, k+dk) whose two x-corners are in range: bit b
-// is cell 32m+b; *carry = the same for cell 32m-1 (m > 0).
-__device__ __forceinline__ uint32_t x_pairs(const Grid& g, const uint32_t* __restrict__ bits,
-                                            long long pos, int m, uint32_t* carry) {
-  uint32_t a, a1;
-  bits_at2(bits, pos, a, a1);
-  if (m > 0) {
-    const long long q = pos - 1;
-    *carry = ((__ldg(bits + (q >> 5)) >> (unsigned)(q & 31)) & a) & 1u;
-  } else {
-    *carry = 0u;
-  }
-  return a & a1;
+// Bit positions fit in 32 bits: grids hold fewer than 2^31 points, and the
+// largest position read, a point plus two planes, stays below 2^32.
+__device__ __forceinline__ uint32_t bits_at_u32(const uint32_t* __restrict__ bits, uint32_t pos) {
+  return __funnelshift_r(__ldg(bits + (pos >> 5)), __ldg(bits + (pos >> 5) + 1), pos & 31u);
 }
 
-}  // namespace
+// K2a, first pass: kept mask of every cell-row word (0 on rows without cells).
+__global__ void __launch_bounds__(256) k_thr_kept(Grid g, const uint32_t* __restrict__ bits,
+                                                  uint32_t* __restrict__ kept) {
+  const uint32_t W = (uint32_t)(g.R * g.wr);  // < 2^27 for grids below 2^31 points
+  const uint32_t wr = (uint32_t)g.wr, nx = (uint32_t)g.nx;
+  const uint32_t dy = nx, dz = nx * (uint32_t)g.ny;
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
+    const uint32_t r = w / wr, m = w - r * wr;
+    const uint32_t j = r % (uint32_t)g.ny, k = r / (uint32_t)g.ny;
+    uint32_t K = 0u;
+    if (j + 1 < (uint32_t)g.ny && k + 1 < (uint32_t)g.nz) {
+      const uint32_t pos = r * nx + 32u * m;
+      const uint32_t p0 = pos, p1 = pos + dy, p2 = pos + dz, p3 = pos + dy + dz;
+      K = bits_at_u32(bits, p0) & bits_at_u32(bits, p0 + 1) & bits_at_u32(bits, p1) &
+          bits_at_u32(bits, p1 + 1) & bits_at_u32(bits, p2) & bits_at_u32(bits, p2 + 1) &
+          bits_at_u32(bits, p3) & bits_at_u32(bits, p3 + 1) & low_mask(g.nx - 1 - 32 * (int)m);
+    }
+    kept[w] = K;
+  }
+}
 
-__global__ void __launch_bounds__(256) k_thr_count(Grid g, const uint32_t* __restrict__ bits,
-                                                   uint32_t* __restrict__ kept,
-                                                   uint32_t* __restrict__ used,
-                                                   uint32_t* __restrict__ wc) {
-  const long long W = g.R * g.wr;  // < 2^27 for grids below 2^31 points
-  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
-       w += (long long)gridDim.x * blockDim.x) {
-    const unsigned r = (unsigned)w / (unsigned)g.wr;
-    const int m = (int)((unsigned)w - r * (unsigned)g.wr);
-    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-    const long long pos = (long long)r * g.nx + 32ll * m;
-    // x-pairs of the 3 x 3 point rows around (j, k): px[dk + 1][dj + 1]
-    uint32_t px[3][3], pc[3][3];
+// K2a, second pass: one 256-thread block per tile of kScanTile words
+// (grid-stride over tiles): used masks, packed counts and tile totals.
+__global__ void __launch_bounds__(256) k_thr_used(Grid g, const uint32_t* __restrict__ kept,
+                                                  uint32_t* __restrict__ used,
+                                                  uint32_t* __restrict__ wc,
+                                                  uint32_t* __restrict__ tile_tot, int tiles) {
+  __shared__ uint32_t s_red[24];
+  const uint32_t W = (uint32_t)(g.R * g.wr);
+  const uint32_t wr = (uint32_t)g.wr, wy = wr, wz = wr * (uint32_t)g.ny;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    uint32_t sk = 0, su = 0, sa = 0;
+#pragma unroll 4
+    for (int e = 0; e < kScanItems; ++e) {
+      const uint32_t w = (uint32_t)tile * kScanTile + threadIdx.x + 256u * e;
+      if (w >= W) break;
+      const uint32_t r = w / wr, m = w - r * wr;
+      const uint32_t j = r % (uint32_t)g.ny, k = r / (uint32_t)g.ny;
+      const uint32_t own = __ldg(kept + w);
+      uint32_t u = 0u;
 #pragma unroll
-    for (int dk = -1; dk <= 1; ++dk) {
-#pragma unroll
-      for (int dj = -1; dj <= 1; ++dj) {
-        const int jj = j + dj, kk = k + dk;
-        if (jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) {
-          px[dk + 1][dj + 1] = 0u;
-          pc[dk + 1][dj + 1] = 0u;
-        } else {
-          px[dk + 1][dj + 1] = x_pairs(g, bits, pos + dj * dy + dk * dz, m, &pc[dk + 1][dj + 1]);
-        }
+      for (int c = 0; c < 4; ++c) {  // cell rows (j - (c & 1), k - (c >> 1))
+        const uint32_t cj = c & 1, ck = c >> 1;
+        if (j < cj || k < ck) continue;
+        const uint32_t wq = w - cj * wy - ck * wz;
+        const uint32_t K = c == 0 ? own : __ldg(kept + wq);
+        const uint32_t Kp = m > 0 ? __ldg(kept + wq - 1) : 0u;
+        u |= K | (K << 1) | (Kp >> 31);
       }
+      u &= low_mask(g.nx - 32 * (int)m);
+      used[w] = u;
+      const uint32_t pk = (uint32_t)__popc(own) << 16 | (uint32_t)__popc(u);
+      wc[w] = pk;
+      sk += pk >> 16;
+      su += pk & 0xffffu;
+      sa += pk ? 1u : 0u;
     }
-    // kept cells of the 4 cell rows (j + cj, k + ck), cj, ck in {-1, 0}
-    const uint32_t cmask = low_mask(g.nx - 1 - 32 * m);
-    uint32_t own = 0u, u = 0u;
-#pragma unroll
-    for (int ck = -1; ck <= 0; ++ck) {
-#pragma unroll
-      for (int cj = -1; cj <= 0; ++cj) {
-        const int jc = j + cj, kc = k + ck;
-        if (jc < 0 || jc >= g.ny - 1 || kc < 0 || kc >= g.nz - 1) continue;
-        const uint32_t K = px[ck + 1][cj + 1] & px[ck + 1][cj + 2] & px[ck + 2][cj + 1] &
-                           px[ck + 2][cj + 2] & cmask;
-        const uint32_t Kc = pc[ck + 1][cj + 1] & pc[ck + 1][cj + 2] & pc[ck + 2][cj + 1] &
-                            pc[ck + 2][cj + 2];
-        u |= K | (K << 1) | Kc;
-        if (cj == 0 && ck == 0) own = K;
-      }
+    block_sum3(sk, su, sa, s_red);
+    if (threadIdx.x == 0) {
+      tile_tot[tile] = sk;
+      tile_tot[tiles + tile] = su;
+      tile_tot[2 * tiles + tile] = sa;
     }
-    u &= low_mask(g.nx - 32 * m);
-    kept[w] = own;
-    used[w] = u;
-    wc[w] = ((uint32_t)__popc(own) << 16) | (uint32_t)__popc(u);
   }
 }
 
 void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint32_t* used,
-                      uint32_t* wc, int num_sms, cudaStream_t s) {
-  const long long want = (g.R * g.wr + 255) / 256;
-  const int blocks = resident_blocks(k_thr_count, 256, 0, num_sms, want);
-  k_thr_count<<<blocks, 256, 0, s>>>(g, bits, kept, used, wc);
+                      uint32_t* wc, uint32_t* tile_tot, int num_sms, cudaStream_t s) {
+  const long long W = g.R * g.wr;
+  const int b1 = resident_blocks(k_thr_kept, 256, 0, num_sms, (W + 255) / 256);
+  k_thr_kept<<<b1, 256, 0, s>>>(g, bits, kept);
+  const int tiles = word_scan_tiles(W);
+  const int b2 = resident_blocks(k_thr_used, 256, 0, num_sms, tiles);
+  k_thr_used<<<b2, 256, 0, s>>>(g, kept, used, wc, tile_tot, tiles);
 }
 
 // Per active word, what the emit loop needs: its masks and offsets, and for
