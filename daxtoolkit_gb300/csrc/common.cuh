@@ -91,10 +91,11 @@ __device__ __forceinline__ GridSlot load_slot(const GridSet& S, int i) {
 struct Info {
   long long total_a;      // triangles (MC) / kept cells (threshold)
   long long total_b;      // merged vertices (MC) / used points (threshold)
-  long long total_c;      // active row words (MC)
+  long long total_c;      // active row words
   int error;              // kErr* bits raised on the device
-  unsigned ticket;        // dynamic tile counter of the look-back scan
-  int pad[8];
+  unsigned ticket;        // next batch of active words for the MC emit warps
+  unsigned done;          // MC emit blocks finished (the last resets both)
+  int pad[7];
 };
 
 constexpr int kErrTimeout = 1;     // a look-back wait gave up

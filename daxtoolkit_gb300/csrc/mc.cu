@@ -361,6 +361,8 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
     info->total_b = V;
     info->total_c = (long long)(ea + ta);
     info->error = (T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0;
+    info->ticket = 0;
+    info->done = 0;
   }
 }
 
@@ -508,13 +510,18 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint32_t* st = s_stage[wib];
   int* pre = s_pre[wib];
-  const long long warp0 = (long long)blockIdx.x * kEmitWarps + wib;
-  const long long nwarps = (long long)gridDim.x * kEmitWarps;
-  for (long long a0 = warp0 * 32; a0 < A; a0 += nwarps * 32) {
+  while (true) {
+    // the next batch of 32 active words, taken dynamically (batches differ
+    // widely in cost)
+    long long a0 = 0;
+    if (lane == 0) a0 = 32ll * atomicAdd(&info->ticket, 1u);
+    a0 = __shfl_sync(kFull, a0, 0);
+    if (a0 >= A) break;
     // ---- lane = word: gather the word's bits, masks and offsets ----------
-    uint32_t am = 0;
+    uint32_t am = 0, t0 = 0;
     if (a0 + lane < A) {
       const uint32_t gw = __ldg(o.act + a0 + lane);
+      t0 = __ldg(o.wt + gw);
       int si, m;
       unsigned r;
       locate_word(S, gw, si, r, m);
@@ -540,7 +547,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
         st[(kFWin + 5) * 32 + lane] = w.c1;
         st[(kFWin + 6) * 32 + lane] = w.d;
         st[(kFWin + 7) * 32 + lane] = w.d1;
-        st[kFT0 * 32 + lane] = __ldg(o.wt + gw);
         st[kFWord * 32 + lane] = gw;
         st[kFSlot * 32 + lane] = (uint32_t)si;
         if (MERGE && am) {
@@ -572,9 +578,8 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
       }
     }
     st[kFAm * 32 + lane] = am;
-    // ---- deal the warp's active cells to the lanes ----------------------
-    const int n = __popc(am);
-    int incl = n;
+    // ---- deal the batch's active cells to the lanes, in batch order -----
+    int incl = __popc(am);
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int v = __shfl_up_sync(kFull, incl, d);
@@ -583,30 +588,43 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
     pre[lane + 1] = incl;
     if (lane == 0) pre[0] = 0;
     const int total = __shfl_sync(kFull, incl, 31);
+    // the batch's triangles are contiguous from its first word's offset
+    long long tri_next = __shfl_sync(kFull, t0, 0);
     __syncwarp();
-    for (int c = lane; c < total; c += 32) {
-      int s = 0;  // the last word whose prefix is <= c
+    for (int c0 = 0; c0 < total; c0 += 32) {
+      const int c = c0 + lane;
+      int s = 0, q = 0;
+      uint64_t cw = 0;
+      CornerWords w{};
+      if (c < total) {
+        // the last word whose prefix is <= c, and its (c - pre[s])-th active cell
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1)
-        if (pre[s + step] <= c) s += step;
-      // walk the word's active cells up to the c - pre[s]-th, summing their
-      // triangle counts (the cell's first triangle)
-      CornerWords w;
-      w.a = window(st, kFWin + 0, s);
-      w.a1 = window(st, kFWin + 1, s);
-      w.b = window(st, kFWin + 2, s);
-      w.b1 = window(st, kFWin + 3, s);
-      w.c = window(st, kFWin + 4, s);
-      w.c1 = window(st, kFWin + 5, s);
-      w.d = window(st, kFWin + 6, s);
-      w.d1 = window(st, kFWin + 7, s);
-      uint32_t u = window(st, kFAm, s);
-      long long tri = window(st, kFT0, s);
-      for (int t = c - pre[s]; t > 0; --t) {
-        tri += (int)(s_case[case_of(w, __ffs(u) - 1)] >> 60);
-        u &= u - 1;
+        for (int step = 16; step > 0; step >>= 1)
+          if (pre[s + step] <= c) s += step;
+        uint32_t u = window(st, kFAm, s);
+        for (int t = c - pre[s]; t > 0; --t) u &= u - 1;
+        q = __ffs(u) - 1;
+        w.a = window(st, kFWin + 0, s);
+        w.a1 = window(st, kFWin + 1, s);
+        w.b = window(st, kFWin + 2, s);
+        w.b1 = window(st, kFWin + 3, s);
+        w.c = window(st, kFWin + 4, s);
+        w.c1 = window(st, kFWin + 5, s);
+        w.d = window(st, kFWin + 6, s);
+        w.d1 = window(st, kFWin + 7, s);
+        cw = s_case[case_of(w, q)];
       }
-      const int q = __ffs(u) - 1;
+      // first triangle of each lane's cell: exclusive scan of the counts
+      const int nt = (int)(cw >> 60);
+      int ti = nt;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(kFull, ti, d);
+        if (lane >= d) ti += v;
+      }
+      long long tri = tri_next + ti - nt;
+      tri_next += __shfl_sync(kFull, ti, 31);
+      if (c >= total) continue;
       const uint32_t gw = window(st, kFWord, s);
       const int si = (int)window(st, kFSlot, s);
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
@@ -620,8 +638,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
       // first vertex of this grid in the concatenated output (0 for one grid)
       const long long vbase0 =
           S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
-      const uint64_t cw = s_case[case_of(w, q)];
-      const int nt = (int)(cw >> 60);
       for (int tt = 0; tt < nt; ++tt, ++tri) {
 #pragma unroll
         for (int corner = 0; corner < 3; ++corner) {
@@ -672,9 +688,8 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
             ow = owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1);
             bit = 0;
           }
-          const uint32_t own = (((ow.X >> bit) & 1u)) | (((ow.Y >> bit) & 1u) << 1) |
+          const uint32_t own = ((ow.X >> bit) & 1u) | (((ow.Y >> bit) & 1u) << 1) |
                                (((ow.Z >> bit) & 1u) << 2);
-          if (!own) continue;
 #pragma unroll
           for (int axis = 0; axis < 3; ++axis)
             if ((own >> axis) & 1u)
@@ -684,6 +699,17 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
       }
     }
     __syncwarp();
+  }
+  // the last block to finish resets the batch counter for the next launch
+  // on this scratch
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&info->done, 1u) == gridDim.x - 1) {
+      info->ticket = 0;
+      info->done = 0;
+      __threadfence();
+    }
   }
 }
 
