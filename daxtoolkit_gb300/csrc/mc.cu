@@ -467,8 +467,8 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
 // One warp's staging of 32 active words, structure-of-arrays so that lane L
 // writes column L without bank conflicts: per word the corner bit words, the
 // crossing masks and first vertex ids of the four owner rows q = dj + 2 dk
-// (rows (j + dj, k + dk) at word m), the active-cell mask, the first
-// triangle, the global row word and the grid slot.
+// (rows (j + dj, k + dk) at word m), the active-cell mask, the global row
+// word, the grid slot and the word's first point (i0 = 32 m, j, k).
 enum EmitField {
   kFWin = 0,     // 8: a, a1, b, b1, c, c1, d, d1
   kFOx = 8,      // 4
@@ -476,17 +476,50 @@ enum EmitField {
   kFOz = 16,     // 4
   kFOv = 20,     // 4
   kFAm = 24,
-  kFT0 = 25,
-  kFWord = 26,
-  kFSlot = 27,
-  kFields = 28
+  kFWord = 25,
+  kFSlot = 26,
+  kFI0 = 27,
+  kFJ = 28,
+  kFK = 29,
+  kFields = 30
 };
 constexpr int kEmitWarps = 8;
+constexpr int kCellChunk = 64;  // active cells tabulated per triangle pass
 
 __device__ __forceinline__ uint32_t window(const uint32_t* st, int f, int s) { return st[f * 32 + s]; }
 
+// Largest s in [0, 31] with pre[s] <= x, for a non-decreasing pre[0..31].
+__device__ __forceinline__ int search32(const int* pre, int x) {
+  int s = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (pre[s + step] <= x) s += step;
+  return s;
+}
+
+// Position of the n-th (0-based) set bit of u; n < popc(u).
+__device__ __forceinline__ int nth_bit(uint32_t u, int n) {
+  int p = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (__popc(u & ((1u << (p + step)) - 1u)) <= n) p += step;
+  return p;
+}
+
+// Exclusive warp scan of v; *total receives the warp's sum.
+__device__ __forceinline__ int warp_exclusive(int v, int lane, int* total) {
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  *total = __shfl_sync(kFull, x, 31);
+  return x - v;
+}
+
 template <bool MERGE>
-__global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
+__global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
                                                             const uint32_t* __restrict__ bits,
                                                             WordOffsets o,
                                                             Info* __restrict__ info,
@@ -501,7 +534,10 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
   __shared__ uint64_t s_case[256];
   __shared__ unsigned char s_edge[12];
   __shared__ uint32_t s_stage[kEmitWarps][kFields * 32];
-  __shared__ int s_pre[kEmitWarps][33];
+  __shared__ int s_pre[kEmitWarps][33];    // active cells before word s
+  __shared__ int s_prev[kEmitWarps][33];   // owned vertices before word s
+  __shared__ uint32_t s_cell[kEmitWarps][kCellChunk];     // word | bit << 5 | case << 10
+  __shared__ int s_tpre[kEmitWarps][kCellChunk + 1];      // triangles before cell
   s_case[threadIdx.x] = kMcCase[threadIdx.x];
   if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
   __syncthreads();
@@ -510,6 +546,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint32_t* st = s_stage[wib];
   int* pre = s_pre[wib];
+  int* pv = s_prev[wib];
+  uint32_t* cell = s_cell[wib];
+  int* tpre = s_tpre[wib];
   while (true) {
     // the next batch of 32 active words, taken dynamically (batches differ
     // widely in cost)
@@ -519,6 +558,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
     if (a0 >= A) break;
     // ---- lane = word: gather the word's bits, masks and offsets ----------
     uint32_t am = 0, t0 = 0;
+    int nv = 0;
     if (a0 + lane < A) {
       const uint32_t gw = __ldg(o.act + a0 + lane);
       t0 = __ldg(o.wt + gw);
@@ -528,16 +568,32 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
       const Grid& g = sl.g;
       const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-      if (j < g.ny - 1 && k < g.nz - 1) {  // the row has cells
-        const uint32_t* gb = bits + sl.word0;
-        const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-        const long long pos = (long long)r * g.nx + 32ll * m;
-        CornerWords w;
-        bits_at2(gb, pos, w.a, w.a1);
-        bits_at2(gb, pos + dy, w.b, w.b1);
-        bits_at2(gb, pos + dz, w.c, w.c1);
+      const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+      const uint32_t* gb = bits + sl.word0;
+      const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+      const long long pos = (long long)r * g.nx + 32ll * m;
+      const uint32_t xmask = low_mask(g.nx - 1 - 32 * m), pmask = low_mask(g.nx - 32 * m);
+      CornerWords w{};
+      bits_at2(gb, pos, w.a, w.a1);
+      if (hy) bits_at2(gb, pos + dy, w.b, w.b1);
+      if (hz) bits_at2(gb, pos + dz, w.c, w.c1);
+      st[kFWord * 32 + lane] = gw;
+      st[kFSlot * 32 + lane] = (uint32_t)si;
+      st[kFI0 * 32 + lane] = (uint32_t)(32 * m);
+      st[kFJ * 32 + lane] = (uint32_t)j;
+      st[kFK * 32 + lane] = (uint32_t)k;
+      if (MERGE) {  // the crossing edges the word's own points own
+        const uint32_t X = (w.a ^ w.a1) & xmask;
+        const uint32_t Y = hy ? (w.a ^ w.b) & pmask : 0u;
+        const uint32_t Z = hz ? (w.a ^ w.c) & pmask : 0u;
+        st[(kFOx + 0) * 32 + lane] = X;
+        st[(kFOy + 0) * 32 + lane] = Y;
+        st[(kFOz + 0) * 32 + lane] = Z;
+        st[(kFOv + 0) * 32 + lane] = __ldg(o.wv + gw);
+        nv = __popc(X) + __popc(Y) + __popc(Z);
+      }
+      if (hy && hz) {  // the row has cells
         bits_at2(gb, pos + dy + dz, w.d, w.d1);
-        const uint32_t xmask = low_mask(g.nx - 1 - 32 * m), pmask = low_mask(g.nx - 32 * m);
         am = active_cells(w, xmask);
         st[(kFWin + 0) * 32 + lane] = w.a;
         st[(kFWin + 1) * 32 + lane] = w.a1;
@@ -547,19 +603,13 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
         st[(kFWin + 5) * 32 + lane] = w.c1;
         st[(kFWin + 6) * 32 + lane] = w.d;
         st[(kFWin + 7) * 32 + lane] = w.d1;
-        st[kFWord * 32 + lane] = gw;
-        st[kFSlot * 32 + lane] = (uint32_t)si;
         if (MERGE && am) {
-          // owner rows (j, k), (j+1, k), (j, k+1), (j+1, k+1); the masks are
-          // those the count pass counted (X: +x, Y: +y, Z: +z crossing edges)
+          // owner rows (j+1, k), (j, k+1), (j+1, k+1) of the cells' far corners
           const bool y2 = j + 1 < g.ny - 1, z2 = k + 1 < g.nz - 1;
           const uint32_t b2 = y2 ? bits_at(gb, pos + 2 * dy) : 0u;
           const uint32_t c2 = z2 ? bits_at(gb, pos + 2 * dz) : 0u;
           const uint32_t d2y = y2 ? bits_at(gb, pos + 2 * dy + dz) : 0u;
           const uint32_t d2z = z2 ? bits_at(gb, pos + dy + 2 * dz) : 0u;
-          st[(kFOx + 0) * 32 + lane] = (w.a ^ w.a1) & xmask;
-          st[(kFOy + 0) * 32 + lane] = (w.a ^ w.b) & pmask;
-          st[(kFOz + 0) * 32 + lane] = (w.a ^ w.c) & pmask;
           st[(kFOx + 1) * 32 + lane] = (w.b ^ w.b1) & xmask;
           st[(kFOy + 1) * 32 + lane] = y2 ? (w.b ^ b2) & pmask : 0u;
           st[(kFOz + 1) * 32 + lane] = (w.b ^ w.d) & pmask;
@@ -570,7 +620,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
           st[(kFOy + 3) * 32 + lane] = y2 ? (w.d ^ d2y) & pmask : 0u;
           st[(kFOz + 3) * 32 + lane] = z2 ? (w.d ^ d2z) & pmask : 0u;
           const uint32_t rwy = (uint32_t)g.wr, rwz = (uint32_t)g.wr * (uint32_t)g.ny;
-          st[(kFOv + 0) * 32 + lane] = __ldg(o.wv + gw);
           st[(kFOv + 1) * 32 + lane] = __ldg(o.wv + gw + rwy);
           st[(kFOv + 2) * 32 + lane] = __ldg(o.wv + gw + rwz);
           st[(kFOv + 3) * 32 + lane] = __ldg(o.wv + gw + rwy + rwz);
@@ -578,67 +627,92 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
       }
     }
     st[kFAm * 32 + lane] = am;
-    // ---- deal the batch's active cells to the lanes, in batch order -----
-    int incl = __popc(am);
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int v = __shfl_up_sync(kFull, incl, d);
-      if (lane >= d) incl += v;
-    }
-    pre[lane + 1] = incl;
-    if (lane == 0) pre[0] = 0;
-    const int total = __shfl_sync(kFull, incl, 31);
+    int total_c, total_v;
+    pre[lane + 1] = warp_exclusive(__popc(am), lane, &total_c) + __popc(am);
+    pv[lane + 1] = warp_exclusive(nv, lane, &total_v) + nv;
+    if (lane == 0) pre[0] = pv[0] = 0;
     // the batch's triangles are contiguous from its first word's offset
-    long long tri_next = __shfl_sync(kFull, t0, 0);
+    long long tri_base = __shfl_sync(kFull, t0, 0);
     __syncwarp();
-    for (int c0 = 0; c0 < total; c0 += 32) {
-      const int c = c0 + lane;
-      int s = 0, q = 0;
-      uint64_t cw = 0;
-      CornerWords w{};
-      if (c < total) {
-        // the last word whose prefix is <= c, and its (c - pre[s])-th active cell
+    if (MERGE) {
+      // ---- lane = merged vertex: each owned crossing edge of the words'
+      // own points, in (point, axis) order -----------------------------------
+      for (int v = lane; v < total_v; v += 32) {
+        const int s = search32(pv, v);
+        const int rnk = v - pv[s];
+        OwnerWord ow;
+        ow.X = window(st, kFOx, s);
+        ow.Y = window(st, kFOy, s);
+        ow.Z = window(st, kFOz, s);
+        ow.base = window(st, kFOv, s);
+        // the owner point: the last bit b whose earlier points own <= rnk edges
+        int b = 0;
 #pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (pre[s + step] <= c) s += step;
-        uint32_t u = window(st, kFAm, s);
-        for (int t = c - pre[s]; t > 0; --t) u &= u - 1;
-        q = __ffs(u) - 1;
-        w.a = window(st, kFWin + 0, s);
-        w.a1 = window(st, kFWin + 1, s);
-        w.b = window(st, kFWin + 2, s);
-        w.b1 = window(st, kFWin + 3, s);
-        w.c = window(st, kFWin + 4, s);
-        w.c1 = window(st, kFWin + 5, s);
-        w.d = window(st, kFWin + 6, s);
-        w.d1 = window(st, kFWin + 7, s);
-        cw = s_case[case_of(w, q)];
+        for (int step = 16; step > 0; step >>= 1) {
+          const uint32_t lm = (1u << (b + step)) - 1u;
+          if (__popc(ow.X & lm) + __popc(ow.Y & lm) + __popc(ow.Z & lm) <= rnk) b += step;
+        }
+        const uint32_t lm = (1u << b) - 1u;
+        const int left = rnk - (__popc(ow.X & lm) + __popc(ow.Y & lm) + __popc(ow.Z & lm));
+        const uint32_t own =
+            ((ow.X >> b) & 1u) | (((ow.Y >> b) & 1u) << 1) | (((ow.Z >> b) & 1u) << 2);
+        const int axis = nth_bit(own, left);
+        const GridSlot& sl = S.count == 1 ? S.one : S.slots[window(st, kFSlot, s)];
+        emit_vertex(sl.g, sl.field, sl.iso, (int)window(st, kFI0, s) + b, (int)window(st, kFJ, s),
+                    (int)window(st, kFK, s), axis, ow.base + rnk, verts, ra, rb, rw);
       }
-      // first triangle of each lane's cell: exclusive scan of the counts
-      const int nt = (int)(cw >> 60);
-      int ti = nt;
+    }
+    // ---- triangles, in chunks of kCellChunk active cells -----------------
+    for (int c0 = 0; c0 < total_c; c0 += kCellChunk) {
+      // lane = cell: its word, bit and case, and the chunk's triangle prefix
+      int chunk_tri = 0;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int v = __shfl_up_sync(kFull, ti, d);
-        if (lane >= d) ti += v;
+      for (int h = 0; h < kCellChunk / 32; ++h) {
+        const int c = c0 + 32 * h + lane;
+        int nt = 0;
+        uint32_t packed = 0;
+        if (c < total_c) {
+          const int s = search32(pre, c);
+          const int q = nth_bit(window(st, kFAm, s), c - pre[s]);
+          CornerWords w;
+          w.a = window(st, kFWin + 0, s);
+          w.a1 = window(st, kFWin + 1, s);
+          w.b = window(st, kFWin + 2, s);
+          w.b1 = window(st, kFWin + 3, s);
+          w.c = window(st, kFWin + 4, s);
+          w.c1 = window(st, kFWin + 5, s);
+          w.d = window(st, kFWin + 6, s);
+          w.d1 = window(st, kFWin + 7, s);
+          const int cs = case_of(w, q);
+          nt = (int)(s_case[cs] >> 60);
+          packed = (uint32_t)s | ((uint32_t)q << 5) | ((uint32_t)cs << 10);
+        }
+        int sum;
+        const int ex = warp_exclusive(nt, lane, &sum);
+        cell[32 * h + lane] = packed;
+        tpre[32 * h + lane] = chunk_tri + ex;
+        chunk_tri += sum;
       }
-      long long tri = tri_next + ti - nt;
-      tri_next += __shfl_sync(kFull, ti, 31);
-      if (c >= total) continue;
-      const uint32_t gw = window(st, kFWord, s);
-      const int si = (int)window(st, kFSlot, s);
-      const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-      const Grid& g = sl.g;
-      const uint32_t* gb = bits + sl.word0;
-      const unsigned lw = gw - (unsigned)sl.rw0;
-      const unsigned r = lw / (unsigned)g.wr;
-      const int m = (int)(lw - r * (unsigned)g.wr);
-      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
-      const int i = 32 * m + q;
-      // first vertex of this grid in the concatenated output (0 for one grid)
-      const long long vbase0 =
-          S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
-      for (int tt = 0; tt < nt; ++tt, ++tri) {
+      if (lane == 0) tpre[kCellChunk] = chunk_tri;
+      __syncwarp();
+      // lane = triangle of the chunk
+      for (int t = lane; t < chunk_tri; t += 32) {
+        int ci = 0;
+#pragma unroll
+        for (int step = kCellChunk / 2; step > 0; step >>= 1)
+          if (tpre[ci + step] <= t) ci += step;
+        const uint32_t packed = cell[ci];
+        const int s = (int)(packed & 31u), q = (int)((packed >> 5) & 31u), cs = (int)(packed >> 10);
+        const int tt = t - tpre[ci];
+        const uint64_t cw = s_case[cs];
+        const long long tri = tri_base + t;
+        const int si = (int)window(st, kFSlot, s);
+        const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
+        const int i = (int)window(st, kFI0, s) + q, j = (int)window(st, kFJ, s),
+                  k = (int)window(st, kFK, s);
+        // first vertex of this grid in the concatenated output (0 for one grid)
+        const long long vbase0 =
+            S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
 #pragma unroll
         for (int corner = 0; corner < 3; ++corner) {
           const int e = mc_edge(cw, 3 * tt + corner);
@@ -656,47 +730,21 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_mc_emit(GridSet S,
               ow.base = window(st, kFOv + qq, s);
               vid = owner_rank_id(ow, ii, axis);
             } else {  // the owner point is the first point of the next word
-              vid = owner_rank_id(owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1), 0, axis);
+              vid = owner_rank_id(owner_word(sl.g, bits + sl.word0, o, sl.rw0, j + dj, k + dk,
+                                             (i >> 5) + 1),
+                                  0, axis);
             }
             conn[3 * tri + corner] = (int32_t)(vid - vbase0);
           } else {
             const long long vid = 3 * tri + corner;
             conn[vid] = (int32_t)(vid - vbase0);
-            emit_vertex(g, sl.field, sl.iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
+            emit_vertex(sl.g, sl.field, sl.iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb,
+                        rw);
           }
         }
       }
-      if (MERGE) {
-        // merged vertices owned by the corners whose own cell this is: the
-        // first point always, a far corner only on the grid's last cell
-        // layer along each axis where it lies beyond
-        const bool ex = i == g.nx - 2, ey = j == g.ny - 2, ez = k == g.nz - 2;
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-          const int di = cc & 1, dj = (cc >> 1) & 1, dk = cc >> 2;
-          if ((di && !ex) || (dj && !ey) || (dk && !ez)) continue;
-          const int qq = dj + 2 * dk, ii = q + di;
-          OwnerWord ow;
-          int bit;
-          if (ii < 32) {
-            ow.X = window(st, kFOx + qq, s);
-            ow.Y = window(st, kFOy + qq, s);
-            ow.Z = window(st, kFOz + qq, s);
-            ow.base = window(st, kFOv + qq, s);
-            bit = ii;
-          } else {
-            ow = owner_word(g, gb, o, sl.rw0, j + dj, k + dk, m + 1);
-            bit = 0;
-          }
-          const uint32_t own = ((ow.X >> bit) & 1u) | (((ow.Y >> bit) & 1u) << 1) |
-                               (((ow.Z >> bit) & 1u) << 2);
-#pragma unroll
-          for (int axis = 0; axis < 3; ++axis)
-            if ((own >> axis) & 1u)
-              emit_vertex(g, sl.field, sl.iso, i + di, j + dj, k + dk, axis,
-                          owner_rank_id(ow, bit, axis), verts, ra, rb, rw);
-        }
-      }
+      tri_base += chunk_tri;
+      __syncwarp();
     }
     __syncwarp();
   }
