@@ -468,7 +468,9 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
 // writes column L without bank conflicts: per word the corner bit words, the
 // crossing masks and first vertex ids of the four owner rows q = dj + 2 dk
 // (rows (j + dj, k + dk) at word m), the active-cell mask, the global row
-// word, the grid slot and the word's first point (i0 = 32 m, j, k).
+// word, the grid slot, the word's first point (i0 = 32 m, j, k), and -- when
+// the word's last cell is active -- the owned edges and first vertex id of
+// point 32m + 32 of each owner row, which that cell's +x corners need.
 enum EmitField {
   kFWin = 0,     // 8: a, a1, b, b1, c, c1, d, d1
   kFOx = 8,      // 4
@@ -481,7 +483,9 @@ enum EmitField {
   kFI0 = 27,
   kFJ = 28,
   kFK = 29,
-  kFields = 30
+  kFNx = 30,     // point 32m + 32 of owner row q: X, Y, Z bits at 3q .. 3q + 2
+  kFNv = 31,     // 4: first vertex id of word m + 1 of owner row q
+  kFields = 35
 };
 constexpr int kEmitWarps = 8;
 constexpr int kCellChunk = 64;  // active cells tabulated per triangle pass
@@ -623,6 +627,16 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
           st[(kFOv + 1) * 32 + lane] = __ldg(o.wv + gw + rwy);
           st[(kFOv + 2) * 32 + lane] = __ldg(o.wv + gw + rwz);
           st[(kFOv + 3) * 32 + lane] = __ldg(o.wv + gw + rwy + rwz);
+          if (am >> 31) {  // the last cell's +x corners lie in word m + 1
+            uint32_t nx3 = 0;
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) {
+              const OwnerWord on = owner_word(g, gb, o, sl.rw0, j + (qq & 1), k + (qq >> 1), m + 1);
+              nx3 |= ((on.X & 1u) | ((on.Y & 1u) << 1) | ((on.Z & 1u) << 2)) << (3 * qq);
+              st[(kFNv + qq) * 32 + lane] = (uint32_t)on.base;
+            }
+            st[kFNx * 32 + lane] = nx3;
+          }
         }
       }
     }
@@ -730,9 +744,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
               ow.base = window(st, kFOv + qq, s);
               vid = owner_rank_id(ow, ii, axis);
             } else {  // the owner point is the first point of the next word
-              vid = owner_rank_id(owner_word(sl.g, bits + sl.word0, o, sl.rw0, j + dj, k + dk,
-                                             (i >> 5) + 1),
-                                  0, axis);
+              const uint32_t nb = window(st, kFNx, s) >> (3 * qq);
+              vid = (long long)window(st, kFNv + qq, s) + (axis >= 1 ? (nb & 1u) : 0u) +
+                    (axis >= 2 ? ((nb >> 1) & 1u) : 0u);
             }
             conn[3 * tri + corner] = (int32_t)(vid - vbase0);
           } else {
