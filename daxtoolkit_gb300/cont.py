@@ -34,14 +34,23 @@ def _stream(stream=None):
 
 
 def _require_field(field, grid):
-    if not isinstance(field, torch.Tensor) or not field.is_cuda:
-        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "field must be a CUDA tensor")
+    """A field is a CUDA tensor or a page-locked CPU tensor (the kernels then
+    read it over the host link through its device mapping)."""
+    if not isinstance(field, torch.Tensor) or not (field.is_cuda or field.is_pinned()):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "field must be a CUDA tensor or a page-locked CPU tensor")
     if field.dtype != torch.float32 or not field.is_contiguous():
         raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "field must be contiguous float32")
     if field.numel() != grid.GetNumberOfPoints():
         raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
                                         "field has %d values, grid has %d points"
                                         % (field.numel(), grid.GetNumberOfPoints()))
+
+
+def _out_device(field):
+    """Device of the outputs computed from `field`: its own, or the current
+    CUDA device for a page-locked CPU field."""
+    return field.device if field.is_cuda else torch.device("cuda", torch.cuda.current_device())
 
 
 class UniformGrid:
@@ -184,7 +193,7 @@ def marching_cubes(grid, field, isovalue, merge=True, records=False, scratch=Non
     capi.call("dax_gb300_mc_totals", _ptr(buf), ctypes.byref(T), ctypes.byref(Vm), s)
     T = T.value
     V = Vm.value if merge else 3 * T
-    dev = field.device
+    dev = _out_device(field)
     verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
     conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
     ra = rb = rw = None
@@ -202,7 +211,7 @@ def marching_cubes(grid, field, isovalue, merge=True, records=False, scratch=Non
 
 
 def interpolate_point_field(rec_first, rec_second, rec_weight, field, stream=None):
-    out = torch.empty(rec_first.numel(), dtype=torch.float32, device=field.device)
+    out = torch.empty(rec_first.numel(), dtype=torch.float32, device=_out_device(field))
     capi.call("dax_gb300_interpolate_point_field", _ptr(rec_first), _ptr(rec_second),
               _ptr(rec_weight), rec_first.numel(), _ptr(field), _ptr(out), _stream(stream))
     return out
@@ -220,7 +229,7 @@ def threshold(grid, field, lo, hi, compact_field=True, scratch=None, stream=None
     K, U = ctypes.c_int64(0), ctypes.c_int64(0)
     capi.call("dax_gb300_threshold_totals", _ptr(buf), ctypes.byref(K), ctypes.byref(U), s)
     K, U = K.value, U.value
-    dev = field.device
+    dev = _out_device(field)
     conn = torch.empty((K, 8), dtype=torch.int32, device=dev)
     coords = torch.empty((U, 3), dtype=torch.float32, device=dev)
     fout = torch.empty(U, dtype=torch.float32, device=dev) if compact_field else None
@@ -233,7 +242,8 @@ def cell_gradient(grid, field, out=None, stream=None):
     _require_field(field, grid)
     g = grid.desc()
     if out is None:
-        out = torch.empty((grid.GetNumberOfCells(), 3), dtype=torch.float32, device=field.device)
+        out = torch.empty((grid.GetNumberOfCells(), 3), dtype=torch.float32,
+                          device=_out_device(field))
     capi.call("dax_gb300_cell_gradient", ctypes.byref(g), _ptr(field), _ptr(out), _stream(stream))
     return out
 
@@ -251,12 +261,12 @@ class DispatcherMapCell:
         g = grid.desc()
         C = grid.GetNumberOfCells()
         if isinstance(w, MarchingCubesCount):
-            count = torch.empty(C, dtype=torch.int32, device=field.device)
+            count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
             capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field), w.IsoValue,
                       _ptr(count), None, _stream(stream))
             return count
         if isinstance(w, ThresholdCount):
-            count = torch.empty(C, dtype=torch.int32, device=field.device)
+            count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
             capi.call("dax_gb300_threshold_classify_count", ctypes.byref(g), _ptr(field),
                       w.ThresholdMin, w.ThresholdMax, _ptr(count), _stream(stream))
             return count
@@ -269,8 +279,8 @@ class DispatcherMapCell:
         """MarchingCubesCount with the per-cell case index as a second output."""
         g = grid.desc()
         C = grid.GetNumberOfCells()
-        count = torch.empty(C, dtype=torch.int32, device=field.device)
-        cases = torch.empty(C, dtype=torch.uint8, device=field.device)
+        count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
+        cases = torch.empty(C, dtype=torch.uint8, device=_out_device(field))
         capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field),
                   self.worklet.IsoValue, _ptr(count), _ptr(cases), _stream(stream))
         return count, cases

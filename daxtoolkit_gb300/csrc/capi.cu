@@ -150,6 +150,27 @@ int check_launch(const char* where) {
   return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, where);
 }
 
+// A field may be device memory or page-locked host memory (cudaHostAlloc,
+// cudaHostRegister); host memory is read by the kernels through its device
+// mapping, over the host link.  Pageable host memory is refused: the device
+// cannot address it through the CUDA runtime.
+int device_view(const float*& p, const char* what) {
+  if (!p) return DAX_GB300_SUCCESS;  // the callers report NULL themselves
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(DAX_GB300_ERROR_BAD_VALUE, std::string(what) + " pointer is not known to CUDA");
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return DAX_GB300_SUCCESS;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    p = static_cast<const float*>(a.devicePointer);
+    return DAX_GB300_SUCCESS;
+  }
+  return fail(DAX_GB300_ERROR_BAD_VALUE,
+              std::string(what) + " is pageable host memory: page-lock it or copy it to the device");
+}
+
 int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
   if (!scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch is NULL");
   Info h;
@@ -173,6 +194,7 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
   int st = make_grid(grid, g);
   if (st) return st;
   if (!field || !scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if ((st = device_view(field, "field"))) return st;
   const size_t need = mode == 0 ? mc_layout(g).total : layout(g).total;
   if (bytes < need) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than *_scratch_bytes()");
   if (!has_cells(g)) {  // no cells: totals stay 0
@@ -249,6 +271,7 @@ int dax_gb300_classify_points(const float* d_field, int64_t n, int mode, float a
                               uint32_t* d_bits, void* stream) {
   if (n <= 0) return DAX_GB300_SUCCESS;
   if (!d_field || !d_bits) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or bits");
+  if (int st = device_view(d_field, "field")) return st;
   if (mode != DAX_GB300_CLASSIFY_ABOVE && mode != DAX_GB300_CLASSIFY_IN_RANGE)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "unknown classification mode");
   Grid g{};
@@ -270,6 +293,7 @@ int dax_gb300_mc_classify_count(const dax_gb300_uniform_grid* grid, const float*
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_count) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or count");
+  if ((st = device_view(d_field, "field"))) return st;
   daxgb::launch_cell_count(0, g, d_field, isovalue, 0.0f, d_count, d_cases, num_sms(),
                            static_cast<cudaStream_t>(stream));
   return check_launch("mc classify-count kernel");
@@ -303,6 +327,7 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if ((st = device_view(d_field, "field"))) return st;
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
       tri_capacity < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
@@ -335,6 +360,7 @@ int dax_gb300_threshold_classify_count(const dax_gb300_uniform_grid* grid, const
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_count) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or count");
+  if ((st = device_view(d_field, "field"))) return st;
   daxgb::launch_cell_count(1, g, d_field, lo, hi, d_count, nullptr, num_sms(),
                            static_cast<cudaStream_t>(stream));
   return check_launch("threshold classify-count kernel");
@@ -368,6 +394,7 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if ((st = device_view(d_field, "field"))) return st;
   if ((!d_conn && cell_capacity > 0) || (!d_coords && point_capacity > 0) || cell_capacity < 0 ||
       point_capacity < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
@@ -388,6 +415,7 @@ int dax_gb300_cell_gradient(const dax_gb300_uniform_grid* grid, const float* d_f
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_gradient) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or gradient");
+  if ((st = device_view(d_field, "field"))) return st;
   daxgb::launch_cell_gradient(g, d_field, d_gradient, num_sms(), static_cast<cudaStream_t>(stream));
   return check_launch("cell gradient kernel");
 }
@@ -406,6 +434,7 @@ int dax_gb300_field_adjoint(const dax_gb300_uniform_grid* grid, const float* d_f
     return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing adjoint");
   }
   if (!d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field");
+  if ((st = device_view(d_field, "field"))) return st;
   const McLayout L = mc_layout(g);
   if (d_grad_vertices && (!d_scratch || scratch_bytes < L.total))
     return fail(DAX_GB300_ERROR_BAD_VALUE, "vertex adjoint needs the dax_gb300_mc_count scratch");
@@ -432,9 +461,11 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
     if (st) { delete b; return st; }
     if (!has_cells(g)) { delete b; return fail(DAX_GB300_ERROR_BAD_VALUE, "batch grid without cells"); }
     if (!d_fields[i]) { delete b; return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field in batch"); }
+    const float* fi = d_fields[i];
+    if ((st = device_view(fi, "batch field"))) { delete b; return st; }
     daxgb::GridSlot& sl = b->slots[i];
     sl.g = g;
-    sl.field = d_fields[i];
+    sl.field = fi;
     sl.iso = isovalues[i];
     sl.iso_hi = 0.0f;
     sl.chunk0 = b->chunks;
@@ -445,7 +476,7 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
     b->chunks += (g.P + 127) / 128;
     b->rows += g.R;
     if (g.wr > b->max_wr) b->max_wr = g.wr;
-    b->aligned = b->aligned && aligned16(d_fields[i]);
+    b->aligned = b->aligned && aligned16(fi);
   }
   b->words = 4 * b->chunks + 8;
   b->off_goff = align256(sizeof(Info));
