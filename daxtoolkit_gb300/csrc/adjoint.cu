@@ -190,9 +190,9 @@ __global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __res
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
        w += (long long)gridDim.x * blockDim.x) {
-    const unsigned r = (unsigned)w / (unsigned)g.wr;
-    const int m = (int)((unsigned)w - r * (unsigned)g.wr);
-    const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+    int m, j, k;
+    const unsigned r = split_word(g, (unsigned)w, m);
+    split_row(g, r, j, k);
     const long long pos = (long long)r * g.nx + 32ll * m;
     const uint32_t pm = low_mask(g.nx - 32 * m);
     uint32_t a, a1;

@@ -77,6 +77,8 @@ int make_grid(const dax_gb300_uniform_grid* in, Grid& g) {
   g.mz = in->extent_min[2];
   g.P = P;
   g.R = d[1] * d[2];
+  g.mwr = daxgb::div_multiplier((unsigned)g.wr);
+  g.mny = daxgb::div_multiplier((unsigned)g.ny);
   return DAX_GB300_SUCCESS;
 }
 

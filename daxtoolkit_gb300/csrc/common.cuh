@@ -30,7 +30,32 @@ struct Grid {
   int mx, my, mz;         // extent minimum (added to ijk for coordinates)
   long long P;            // points
   long long R;            // point rows = ny * nz
+  unsigned long long mwr, mny;  // division multipliers for wr and ny (div_by)
 };
+
+// n / d for 32-bit n and a divisor fixed per grid, from the multiplier
+// M = floor((2^64 - 1) / d) + 1 (0 for d = 1): q = high 64 bits of n * M.
+// Exact for every 32-bit n and 2 <= d < 2^32: n/d <= n*M/2^64 < n/d + 2^-32
+// and 2^-32 <= 1/d (T. Granlund, P. Montgomery, "Division by Invariant
+// Integers using Multiplication", PLDI 1994).
+__host__ __device__ inline unsigned long long div_multiplier(unsigned d) {
+  return d >= 2 ? ~0ull / d + 1ull : 0ull;
+}
+__device__ __forceinline__ unsigned div_by(unsigned n, unsigned long long M) {
+  return M ? (unsigned)__umul64hi((unsigned long long)n, M) : n;
+}
+// Row r and word m of a grid's row word lw (lw < R * wr < 2^32).
+__device__ __forceinline__ unsigned split_word(const Grid& g, unsigned lw, int& m) {
+  const unsigned r = div_by(lw, g.mwr);
+  m = (int)(lw - r * (unsigned)g.wr);
+  return r;
+}
+// (j, k) of point row r.
+__device__ __forceinline__ void split_row(const Grid& g, unsigned r, int& j, int& k) {
+  const unsigned kk = div_by(r, g.mny);
+  k = (int)kk;
+  j = (int)(r - kk * (unsigned)g.ny);
+}
 
 // One grid of a batch (device-resident table entry, or passed by value).
 struct GridSlot {

@@ -105,7 +105,8 @@ struct WordBits {
 __device__ __forceinline__ WordBits load_word_bits(const Grid& g, const uint32_t* bits, unsigned r,
                                                    int m) {
   WordBits wb;
-  const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+  int j, k;
+  split_row(g, r, j, k);
   wb.hy = j < g.ny - 1;
   wb.hz = k < g.nz - 1;
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
@@ -125,8 +126,7 @@ __device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int&
   si = S.count == 1 ? 0 : slot_of_rowword(S, gw);
   const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
   const unsigned lw = (unsigned)(gw - sl.rw0);
-  r = lw / (unsigned)sl.g.wr;
-  m = (int)(lw - r * (unsigned)sl.g.wr);
+  r = split_word(sl.g, lw, m);
 }
 
 // Counts of one word from its eight corner words.
@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
           (S.count == 1 || g0 + kCountWords <= sl.rw0 + (long long)g.R * g.wr)) {
         // fast path: the four words lie in one row
         const uint32_t* gb = bits + sl.word0;
-        const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+        int j, k;
+  split_row(g, r, j, k);
         const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
         const long long dy = g.nx, dz = (long long)g.nx * g.ny;
         const long long pos = (long long)r * g.nx + 32ll * m;
@@ -571,7 +572,8 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
       locate_word(S, gw, si, r, m);
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
       const Grid& g = sl.g;
-      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+      int j, k;
+  split_row(g, r, j, k);
       const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
       const uint32_t* gb = bits + sl.word0;
       const long long dy = g.nx, dz = (long long)g.nx * g.ny;

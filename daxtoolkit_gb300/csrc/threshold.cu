@@ -38,8 +38,10 @@ __global__ void __launch_bounds__(256) k_thr_kept(Grid g, const uint32_t* __rest
   const uint32_t wr = (uint32_t)g.wr, nx = (uint32_t)g.nx;
   const uint32_t dy = nx, dz = nx * (uint32_t)g.ny;
   for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
-    const uint32_t r = w / wr, m = w - r * wr;
-    const uint32_t j = r % (uint32_t)g.ny, k = r / (uint32_t)g.ny;
+    int mi, ji, ki;
+    const uint32_t r = split_word(g, w, mi);
+    split_row(g, r, ji, ki);
+    const uint32_t m = (uint32_t)mi, j = (uint32_t)ji, k = (uint32_t)ki;
     uint32_t K = 0u;
     if (j + 1 < (uint32_t)g.ny && k + 1 < (uint32_t)g.nz) {
       const uint32_t pos = r * nx + 32u * m;
@@ -67,8 +69,10 @@ __global__ void __launch_bounds__(256) k_thr_used(Grid g, const uint32_t* __rest
     for (int e = 0; e < kScanItems; ++e) {
       const uint32_t w = (uint32_t)tile * kScanTile + threadIdx.x + 256u * e;
       if (w >= W) break;
-      const uint32_t r = w / wr, m = w - r * wr;
-      const uint32_t j = r % (uint32_t)g.ny, k = r / (uint32_t)g.ny;
+      int mi, ji, ki;
+      const uint32_t r = split_word(g, w, mi);
+      split_row(g, r, ji, ki);
+      const uint32_t m = (uint32_t)mi, j = (uint32_t)ji, k = (uint32_t)ki;
       const uint32_t own = __ldg(kept + w);
       uint32_t u = 0u;
 #pragma unroll
@@ -148,7 +152,9 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       d.v0 = __ldg(wv + d.w);
       d.t0 = __ldg(wt + d.w);
       if (d.kw) {  // a kept cell implies rows j + 1 and k + 1 exist
-        const unsigned r = d.w / wr, m = d.w - r * wr;
+        int mi;
+        split_word(g, d.w, mi);
+        const unsigned m = (unsigned)mi;
         const uint32_t rows[4] = {d.w, d.w + wr, d.w + (unsigned)g.ny * wr,
                                   d.w + (unsigned)(g.ny + 1) * wr};
 #pragma unroll
@@ -169,8 +175,10 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       const uint32_t w = __shfl_sync(kFull, d.w, s);
       const uint32_t u = __shfl_sync(kFull, d.u, s);
       const uint32_t kw = __shfl_sync(kFull, d.kw, s);
-      const uint32_t r = w / wr, m = w - r * wr;
-      const int j = (int)(r % (unsigned)g.ny), k = (int)(r / (unsigned)g.ny);
+      int mi, j, k;
+      const uint32_t r = split_word(g, w, mi);
+      const uint32_t m = (uint32_t)mi;
+      split_row(g, r, j, k);
       const int i = 32 * (int)m + lane;
       const long long p = (long long)r * g.nx + i;
       const uint32_t v0 = __shfl_sync(kFull, d.v0, s);
