@@ -8,7 +8,12 @@ field resident in HBM.  The field (537 MB) is larger than L2 (129 MB), so no
 flush is needed between steps.
 
 Reported:
-  value        cells/s over all ranks, device-timed (CUDA events, field in HBM)
+  value        cells/s over all ranks, device-timed (CUDA events, field in HBM),
+               with --frames frames in flight (default 3): consecutive frames go
+               to separate streams, each with its own field copy, scratch and
+               outputs, so one frame's bandwidth-bound classification overlaps
+               the latency-bound count/scan/emit of the previous ones; the
+               one-frame-at-a-time time is reported beside it
   e2e          the same metric through the public API from pinned host memory:
                H2D field copy + marching_cubes() (count, host sizing, generate)
                + D2H of vertices and connectivity, every step
@@ -47,6 +52,8 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=512)
+    p.add_argument("--frames", type=int, default=3,
+                   help="frames in flight (one stream, scratch and output set each)")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -383,13 +390,47 @@ def main():
     verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
     conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
 
-    def step():
-        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(field), iso, ptr(scratch), nbytes, s)
-        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(field), iso, 1, ptr(scratch), nbytes,
-                  ptr(verts), V, ptr(conn), T, None, None, None, s)
+    # Frames in flight: each slot is one complete frame -- its own copy of the
+    # field (so no frame reuses another's cache lines), its own scratch and
+    # outputs and its own stream.  Consecutive frames go to consecutive slots,
+    # so the bandwidth-bound classification of one frame overlaps the
+    # latency-bound count, scan and emit of the frames before it.
+    F = max(1, args.frames)
+    slots = []
+    for f in range(F):
+        slots.append(dict(
+            field=field if f == 0 else field.clone(),
+            scratch=scratch if f == 0 else torch.empty_like(scratch),
+            verts=verts if f == 0 else torch.empty_like(verts),
+            conn=conn if f == 0 else torch.empty_like(conn),
+            stream=torch.cuda.Stream(device=dev)))
+    for sl in slots:
+        sl["s"] = ctypes.c_void_p(sl["stream"].cuda_stream)
 
-    for _ in range(max(3, args.warmup)):
-        step()
+    def frame(k, inflight=F):
+        sl = slots[k % inflight]
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(sl["field"]), iso, ptr(sl["scratch"]),
+                  nbytes, sl["s"])
+        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(sl["field"]), iso, 1,
+                  ptr(sl["scratch"]), nbytes, ptr(sl["verts"]), V, ptr(sl["conn"]), T, None, None,
+                  None, sl["s"])
+
+    def run_frames(count, inflight=F):
+        """Enqueue `count` frames between two events on the current stream."""
+        cur = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(cur)
+        for sl in slots:
+            sl["stream"].wait_stream(cur)
+        for k in range(count):
+            frame(k, inflight)
+        for sl in slots:
+            cur.wait_stream(sl["stream"])
+        b.record(cur)
+        return a, b
+
+    for k in range(max(3, args.warmup) * F):
+        frame(k)
     torch.cuda.synchronize()
 
     def barrier():
@@ -402,19 +443,23 @@ def main():
     time.sleep(0.3)
     barrier()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
+    e0, e1 = run_frames(args.steps)
     torch.cuda.synchronize()
     barrier()
     t_ms = e0.elapsed_time(e1)
     clocks = sampler.stop()
-    # device totals/errors after the timed region
-    T2, V2 = ctypes.c_int64(0), ctypes.c_int64(0)
-    capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(T2), ctypes.byref(V2), s)
-    assert (T2.value, V2.value) == (T, V)
+    # device totals/errors and outputs of every slot after the timed region
+    for sl in slots:
+        T2, V2 = ctypes.c_int64(0), ctypes.c_int64(0)
+        capi.call("dax_gb300_mc_totals", ptr(sl["scratch"]), ctypes.byref(T2), ctypes.byref(V2),
+                  sl["s"])
+        assert (T2.value, V2.value) == (T, V)
+        assert torch.equal(sl["verts"], verts) and torch.equal(sl["conn"], conn)
+    # one frame at a time: the single-frame latency
+    reps1 = max(5, min(args.steps, 300))
+    a1, b1 = run_frames(reps1, 1)
+    torch.cuda.synchronize()
+    ms_one = a1.elapsed_time(b1) / reps1
     if world > 1:
         import torch.distributed as dist
         tt = torch.tensor([t_ms], device=dev)
@@ -485,7 +530,11 @@ def main():
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": config_dict(n),
+        "data": "synthetic",
+        "config": dict(config_dict(n), frames_in_flight=F,
+                       frames_note="each in-flight frame has its own field copy, scratch, "
+                                   "outputs and stream; every frame is a complete pass"),
+        "ms_per_frame_one_in_flight": ms_one,
         "triangles": T, "merged_vertices": V,
         "triangles_per_s": world * T / (ms_per_step / 1e3),
         "roofline": {"bound": "hbm", "kernel": "k_classify_bits", "achieved": achieved,
