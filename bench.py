@@ -330,7 +330,70 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                       "speedup": t_plain / t_batch, "target_speedup": 3.0,
                       "batched_cells_per_s": cells / (t_batch / 1e3),
                       "graph_replay_matches_batch_run": ok}
+    out["primitives"] = primitive_measurements(peak, stream, dev)
     return out
+
+
+def primitive_measurements(peak, stream, dev, reps=10):
+    """The device adapter's generic primitives on large int32 inputs, device-
+    timed, with numpy on the host cores beside them (the reference's CPU
+    adapter runs std:: algorithms of the same kind).  Bytes per element are
+    the data each algorithm must touch at least once."""
+    import numpy as np
+    import torch
+    from daxtoolkit_gb300 import cont
+    A = cont.Algorithm
+    g = torch.Generator(device="cpu").manual_seed(4321)
+    res = {}
+
+    def gbs(nbytes, ms):
+        return nbytes / (ms / 1e3) / 1e9
+
+    def cpu_ms(fn, k=3):
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        return (time.perf_counter() - t0) / k * 1e3
+
+    # ScanInclusive over 1 G dax::Id values (read 4 B, write 4 B)
+    n = 1 << 30
+    x = torch.randint(0, 1000, (n,), dtype=torch.int32, device=dev)
+    y = torch.empty_like(x)
+    t = _event_ms(lambda: A.ScanInclusive(x, y), reps, stream)
+    xs = x[: 1 << 26].cpu().numpy()
+    tc = cpu_ms(lambda: np.cumsum(xs, dtype=np.int32)) * (n / (1 << 26))
+    res["scan_inclusive_i32"] = {"n": n, "ms": t, "gb_s": gbs(8 * n, t), "frac": gbs(8 * n, t) / peak,
+                                 "cpu_numpy_ms_scaled": tc}
+    del x, y
+    # SortByKey of 100 M (int32 key, int32 value) pairs (read and write 8 B)
+    n = 100_000_000
+    keys0 = torch.randint(-2 ** 31, 2 ** 31 - 1, (n,), dtype=torch.int32, generator=g).to(dev)
+    vals0 = torch.arange(n, dtype=torch.int32, device=dev)
+    keys, vals = keys0.clone(), vals0.clone()
+
+    def sort_once():
+        keys.copy_(keys0)
+        vals.copy_(vals0)
+        A.SortByKey(keys, vals)
+
+    t_copy = _event_ms(lambda: (keys.copy_(keys0), vals.copy_(vals0)), reps, stream)
+    t = _event_ms(sort_once, reps, stream) - t_copy
+    ok = bool(torch.all(keys[1:] >= keys[:-1]).item())
+    kc = keys0[: 1 << 24].cpu().numpy()
+    tc = cpu_ms(lambda: np.argsort(kc, kind="stable")) * (n / (1 << 24))
+    res["sort_by_key_i32_pairs"] = {"n": n, "ms": t, "keys_per_s": n / (t / 1e3),
+                                    "gb_s_min_traffic": gbs(16 * n, t), "sorted": ok,
+                                    "passes": 4, "cpu_numpy_stable_argsort_ms_scaled": tc}
+    # Unique of the sorted keys, StreamCompact of the values with a 30 % stencil
+    uk = keys.clone()
+    t_u = _event_ms(lambda: (uk.copy_(keys), A.Unique(uk)), reps, stream) - \
+        _event_ms(lambda: uk.copy_(keys), reps, stream)
+    stencil = (torch.rand(n, generator=g) < 0.3).to(torch.int32).to(dev)
+    t_c = _event_ms(lambda: A.StreamCompact(vals, stencil), reps, stream)
+    res["unique_i32"] = {"n": n, "ms": t_u, "gb_s_min_traffic": gbs(8 * n, t_u)}
+    res["stream_compact_i32"] = {"n": n, "kept": int(stencil.sum().item()), "ms": t_c,
+                                 "gb_s_min_traffic": gbs(8 * n + 4 * int(stencil.sum().item()), t_c)}
+    return res
 
 
 def config_dict(n):

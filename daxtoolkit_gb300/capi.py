@@ -89,7 +89,17 @@ SIGNATURES = {
     "dax_gb300_graph_launch": ([vp, vp], i32),
     "dax_gb300_graph_destroy": ([vp], i32),
     "dax_gb300_mc_noalloc": ([gp, vp, f32, i32, vp, i64, vp, i64, vp, vp], i32),
+    "dax_gb300_scan_scratch_bytes": ([i64], sz),
+    "dax_gb300_scan": ([vp, vp, i64, i32, i32, vp, sz, vp, vp], i32),
+    "dax_gb300_sort_scratch_bytes": ([i64, i32, i32], sz),
+    "dax_gb300_sort_by_key": ([vp, vp, i64, i32, i32, i32, vp, sz, vp], i32),
+    "dax_gb300_compact_scratch_bytes": ([i64, i32], sz),
+    "dax_gb300_unique": ([vp, i64, i32, vp, sz, ctypes.POINTER(i64), vp], i32),
+    "dax_gb300_stream_compact": ([vp, i32, vp, i32, i64, vp, vp, sz, ctypes.POINTER(i64), vp], i32),
+    "dax_gb300_bounds": ([vp, i64, vp, i64, i32, i32, vp, vp], i32),
 }
+
+TYPE_I32, TYPE_U32, TYPE_F32, TYPE_I64, TYPE_U64 = 0, 1, 2, 3, 4
 
 
 def header_symbols():

@@ -424,3 +424,167 @@ class MarchingCubesBatch:
 
     def replay(self, stream=None):
         capi.call("dax_gb300_graph_launch", self.graph, _stream(stream))
+
+
+# ---- generic primitives: dax::cont::internal::DeviceAdapterAlgorithm -------
+class SortLess:
+    """dax::math::SortLess: ascending order (the default)."""
+
+
+class SortGreater:
+    """dax::math::SortGreater: descending order."""
+
+
+_TYPES = {torch.int32: capi.TYPE_I32, torch.float32: capi.TYPE_F32, torch.int64: capi.TYPE_I64}
+if hasattr(torch, "uint32"):
+    _TYPES[torch.uint32] = capi.TYPE_U32
+if hasattr(torch, "uint64"):
+    _TYPES[torch.uint64] = capi.TYPE_U64
+
+
+def _elem_type(t, what):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or not t.is_contiguous():
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "%s must be a contiguous CUDA tensor"
+                                        % what)
+    if t.dtype not in _TYPES:
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "unsupported %s type %s"
+                                        % (what, t.dtype))
+    return _TYPES[t.dtype]
+
+
+def _row_bytes(t):
+    return t[0].numel() * t.element_size() if t.dim() > 1 else t.element_size()
+
+
+class Algorithm:
+    """The device adapter's generic algorithms (DeviceAdapterAlgorithm.h:44-331)
+    on torch CUDA tensors, with the reference's names and argument meanings."""
+
+    @staticmethod
+    def Copy(src, dst=None):
+        if dst is None:
+            return src.clone()
+        dst.resize_(src.shape).copy_(src)
+        return dst
+
+    @staticmethod
+    def _scan(inp, out, exclusive, stream):
+        t = _elem_type(inp, "array")
+        if out is None:
+            out = torch.empty_like(inp)
+        n = inp.numel()
+        nb = capi.lib().dax_gb300_scan_scratch_bytes(n)
+        scratch = torch.empty(nb, dtype=torch.uint8, device=inp.device)
+        total = torch.zeros(1, dtype=inp.dtype)
+        capi.call("dax_gb300_scan", _ptr(inp), _ptr(out), n, t, int(exclusive), _ptr(scratch), nb,
+                  ctypes.c_void_p(total.data_ptr()), _stream(stream))
+        return total.item(), out
+
+    @staticmethod
+    def ScanInclusive(inp, out=None, stream=None):
+        """Returns (total, out); out may be inp (in place)."""
+        return Algorithm._scan(inp, out, False, stream)
+
+    @staticmethod
+    def ScanExclusive(inp, out=None, stream=None):
+        return Algorithm._scan(inp, out, True, stream)
+
+    @staticmethod
+    def SortByKey(keys, values, comp=None, stream=None):
+        """Sorts keys in place (stable), carrying values ([n] or [n, k] rows of
+        up to 16 bytes).  Keys of shape [n, k] sort lexicographically, as the
+        reference's tuple keys do (first component most significant)."""
+        desc = isinstance(comp, SortGreater) or comp is SortGreater
+        if keys.dim() > 1:
+            return Algorithm._sort_rows(keys, values, desc, stream)
+        t = _elem_type(keys, "keys")
+        n = keys.numel()
+        vb = 0
+        if values is not None:
+            if not values.is_cuda or not values.is_contiguous() or values.shape[0] != n:
+                raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                                "values must be contiguous, one row per key")
+            vb = _row_bytes(values) if n else 0
+        nb = capi.lib().dax_gb300_sort_scratch_bytes(n, t, vb)
+        if nb == 0:
+            raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "value rows must be 4..16 bytes")
+        scratch = torch.empty(nb, dtype=torch.uint8, device=keys.device)
+        capi.call("dax_gb300_sort_by_key", _ptr(keys), _ptr(values) if vb else None, n, t, vb,
+                  int(desc), _ptr(scratch), nb, _stream(stream))
+        return keys, values
+
+    @staticmethod
+    def _sort_rows(keys, values, desc, stream):
+        n = keys.shape[0]
+        perm = torch.arange(n, dtype=torch.int32, device=keys.device)
+        for c in reversed(range(keys.shape[1])):  # least significant component first
+            col = keys[:, c][perm.long()].contiguous()
+            Algorithm.SortByKey(col, perm, SortGreater() if desc else None, stream)
+        idx = perm.long()
+        keys.copy_(keys[idx])
+        if values is not None:
+            values.copy_(values[idx])
+        return keys, values
+
+    @staticmethod
+    def Sort(array, comp=None, stream=None):
+        return Algorithm.SortByKey(array, None, comp, stream)[0]
+
+    @staticmethod
+    def Unique(array, stream=None):
+        """Keeps the first of every run of equal adjacent values; returns the
+        shrunk view of `array`."""
+        t = _elem_type(array, "array")
+        n = array.numel()
+        nb = capi.lib().dax_gb300_compact_scratch_bytes(n, array.element_size())
+        scratch = torch.empty(nb, dtype=torch.uint8, device=array.device)
+        cnt = ctypes.c_int64(0)
+        capi.call("dax_gb300_unique", _ptr(array), n, t, _ptr(scratch), nb, ctypes.byref(cnt),
+                  _stream(stream))
+        return array[:cnt.value]
+
+    @staticmethod
+    def _bounds(sorted_, values, out, upper, stream):
+        t = _elem_type(sorted_, "input")
+        if values.dtype != sorted_.dtype:
+            raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "values must match the input type")
+        if out is None:
+            out = torch.empty(values.numel(), dtype=torch.int32, device=values.device)
+        capi.call("dax_gb300_bounds", _ptr(sorted_), sorted_.numel(), _ptr(values), values.numel(),
+                  t, int(upper), _ptr(out), _stream(stream))
+        return out
+
+    @staticmethod
+    def LowerBounds(inp, values, out=None, comp=None, stream=None):
+        return Algorithm._bounds(inp, values, out, False, stream)
+
+    @staticmethod
+    def UpperBounds(inp, values, out=None, comp=None, stream=None):
+        return Algorithm._bounds(inp, values, out, True, stream)
+
+    @staticmethod
+    def StreamCompact(inp, stencil=None, stream=None):
+        """StreamCompact(input, stencil): the rows of input whose stencil entry
+        is non-zero.  StreamCompact(stencil): the int32 indices of the non-zero
+        entries."""
+        if stencil is None:
+            stencil, inp = inp, None
+        st = _elem_type(stencil, "stencil")
+        if st not in (capi.TYPE_I32, capi.TYPE_F32):
+            raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "stencil must be int32 or float32")
+        n = stencil.numel()
+        if inp is None:
+            out = torch.empty(n, dtype=torch.int32, device=stencil.device)
+            vb = 4
+        else:
+            if not inp.is_cuda or not inp.is_contiguous() or inp.shape[0] != n:
+                raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                                "input must be contiguous, one row per stencil entry")
+            out = torch.empty_like(inp)
+            vb = _row_bytes(inp) if n else 4
+        nb = capi.lib().dax_gb300_compact_scratch_bytes(n, 0)
+        scratch = torch.empty(nb, dtype=torch.uint8, device=stencil.device)
+        cnt = ctypes.c_int64(0)
+        capi.call("dax_gb300_stream_compact", _ptr(inp), vb, _ptr(stencil), st, n, _ptr(out),
+                  _ptr(scratch), nb, ctypes.byref(cnt), _stream(stream))
+        return out[:cnt.value]

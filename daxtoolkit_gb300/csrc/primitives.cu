@@ -1,0 +1,763 @@
+// Generic data-parallel primitives of the device adapter
+// (dax::cont::DeviceAdapterAlgorithm, dax/cont/internal/DeviceAdapterAlgorithm.h:44-331;
+// the reference's generic versions are dax/cont/internal/DeviceAdapterAlgorithmGeneral.h):
+// ScanInclusive / ScanExclusive, Sort / SortByKey, Unique, LowerBounds /
+// UpperBounds and StreamCompact, on the element types the Dax pipelines use
+// (dax::Id = int32, int64, unsigned, dax::Scalar = float) with values of up
+// to 16 bytes (a dax::Vector3 is 12).
+//
+// Every primitive works on tiles of kPTile elements (256 threads x 16):
+//   scan     reduce-then-scan: tile sums, one block scanning the sums, then
+//            each tile scanned with its prefix (in place allowed);
+//   sort     LSD radix sort, 8-bit digits, stable: per pass a per-tile digit
+//            histogram, a scan of the histograms in digit-major order, and a
+//            scatter that ranks each element among equal digits of its tile
+//            (warp match + per-warp counts) in element order;
+//   compact  per-tile counts of the kept elements, their scan, and an
+//            order-preserving scatter (Unique = compact of "differs from the
+//            previous element", StreamCompact = compact of "stencil != 0").
+#include <cstdint>
+#include <cstring>
+#include <string>
+
+#include "../../include/dax_gb300.h"
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace daxgb {
+
+namespace {
+
+constexpr int kPT = 256;
+constexpr int kPI = 16;
+constexpr int kPTile = kPT * kPI;
+
+int ptiles(long long n) { return (int)((n + kPTile - 1) / kPTile); }
+
+// Integer sums wrap like the reference's dax::Id arithmetic: accumulate in
+// the unsigned type of the same width.
+template <typename T> struct Acc { typedef T type; };
+template <> struct Acc<int32_t> { typedef uint32_t type; };
+template <> struct Acc<int64_t> { typedef unsigned long long type; };
+
+template <typename A>
+__device__ __forceinline__ A block_exclusive(A v, A* s_warp, A* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  A x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const A y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  A base = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < kPT / 32; ++w) {
+    if (w < warp) base += s_warp[w];
+    tot += s_warp[w];
+  }
+  __syncthreads();
+  *total = tot;
+  return base + x - v;
+}
+
+// ---- scan -----------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(kPT) k_tile_sum(const T* __restrict__ in, long long n,
+                                                  typename Acc<T>::type* __restrict__ sums,
+                                                  int tiles) {
+  typedef typename Acc<T>::type A;
+  __shared__ A s_warp[kPT / 32];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    A v = 0;
+    const long long b = (long long)tile * kPTile;
+#pragma unroll 4
+    for (int e = 0; e < kPI; ++e) {
+      const long long i = b + e * kPT + threadIdx.x;
+      if (i < n) v += (A)in[i];
+    }
+    A tot;
+    block_exclusive(v, s_warp, &tot);
+    if (threadIdx.x == 0) sums[tile] = tot;
+  }
+}
+
+// One block: exclusive scan of the tile sums in place; the grand total goes
+// to sums[tiles].
+template <typename A>
+__global__ void __launch_bounds__(1024) k_scan_sums(A* __restrict__ sums, int tiles) {
+  __shared__ A s_warp[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  A carry = 0;
+  for (int c0 = 0; c0 < tiles; c0 += 1024) {
+    const int i = c0 + threadIdx.x;
+    const A v = i < tiles ? sums[i] : (A)0;
+    A x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const A y = __shfl_up_sync(kFull, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    A base = 0, tot = 0;
+    for (int w = 0; w < 32; ++w) {
+      if (w < warp) base += s_warp[w];
+      tot += s_warp[w];
+    }
+    if (i < tiles) sums[i] = carry + base + x - v;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[tiles] = carry;
+}
+
+// A tile is loaded with coalesced (striped) loads into shared memory, each
+// thread then scans 16 consecutive elements, and the results leave the same
+// way.  The tile's prefix comes from the scanned sums.  Every element of a
+// tile is read before any is written: in place is fine.
+__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
+
+template <typename T>
+__global__ void __launch_bounds__(kPT) k_tile_scan(const T* __restrict__ in, T* out, long long n,
+                                                   const typename Acc<T>::type* __restrict__ pre,
+                                                   int tiles, int exclusive) {
+  typedef typename Acc<T>::type A;
+  __shared__ A s_warp[kPT / 32];
+  __shared__ A s_t[kPTile + kPTile / 32];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long b = (long long)tile * kPTile;
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const int li = e * kPT + threadIdx.x;
+      s_t[pad(li)] = b + li < n ? (A)in[b + li] : (A)0;
+    }
+    __syncthreads();
+    A v[kPI];
+    A sum = 0;
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      v[e] = s_t[pad(threadIdx.x * kPI + e)];
+      sum += v[e];
+    }
+    A tot;
+    A run = pre[tile] + block_exclusive(sum, s_warp, &tot);
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const A next = run + v[e];
+      s_t[pad(threadIdx.x * kPI + e)] = exclusive ? run : next;
+      run = next;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const int li = e * kPT + threadIdx.x;
+      if (b + li < n) out[b + li] = (T)s_t[pad(li)];
+    }
+    __syncthreads();
+  }
+}
+
+// Two-level scan of many sums: chunks of 1024 scanned in parallel (each
+// chunk's total to aux), the totals scanned by one block, then added back.
+template <typename A>
+__global__ void __launch_bounds__(1024) k_chunk_scan(A* __restrict__ v, int count,
+                                                     A* __restrict__ aux) {
+  __shared__ A s_warp[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const A x0 = i < count ? v[i] : (A)0;
+  A x = x0;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const A y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  A base = 0, tot = 0;
+  for (int w = 0; w < 32; ++w) {
+    if (w < warp) base += s_warp[w];
+    tot += s_warp[w];
+  }
+  if (i < count) v[i] = base + x - x0;
+  if (threadIdx.x == 0) aux[blockIdx.x] = tot;
+}
+
+template <typename A>
+__global__ void __launch_bounds__(1024) k_chunk_add(A* __restrict__ v, int count,
+                                                    const A* __restrict__ aux, int chunks) {
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < count) v[i] += aux[blockIdx.x];
+  if (blockIdx.x == 0 && threadIdx.x == 0) v[count] = aux[chunks];
+}
+
+// Exclusive scan of v[0..count) in place, total to v[count]; aux holds
+// count / 1024 + 2 entries.
+template <typename A>
+void scan_sums(A* v, int count, A* aux, cudaStream_t s) {
+  if (count <= 8192) {
+    k_scan_sums<A><<<1, 1024, 0, s>>>(v, count);
+    return;
+  }
+  const int chunks = (count + 1023) / 1024;
+  k_chunk_scan<A><<<chunks, 1024, 0, s>>>(v, count, aux);
+  k_scan_sums<A><<<1, 1024, 0, s>>>(aux, chunks);
+  k_chunk_add<A><<<chunks, 1024, 0, s>>>(v, count, aux, chunks);
+}
+
+int sum_slots(long long n) { return ptiles(n) + 1 + ptiles(n) / 1024 + 2; }
+
+int resident(const void* kernel, int threads, int num_sms, long long want) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0) != cudaSuccess ||
+      per < 1)
+    per = 1;
+  const long long cap = (long long)num_sms * per;
+  return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+template <typename T>
+void scan_t(const T* in, T* out, long long n, bool exclusive, void* scratch, void* d_total,
+            int num_sms, cudaStream_t s) {
+  typedef typename Acc<T>::type A;
+  const int tiles = ptiles(n);
+  A* sums = static_cast<A*>(scratch);
+  const int b = resident((const void*)k_tile_sum<T>, kPT, num_sms, tiles);
+  k_tile_sum<T><<<b, kPT, 0, s>>>(in, n, sums, tiles);
+  scan_sums<A>(sums, tiles, sums + tiles + 1, s);
+  k_tile_scan<T><<<b, kPT, 0, s>>>(in, out, n, sums, tiles, exclusive ? 1 : 0);
+  if (d_total) cudaMemcpyAsync(d_total, sums + tiles, sizeof(T), cudaMemcpyDeviceToDevice, s);
+}
+
+// ---- radix sort -------------------------------------------------------------
+
+// Keys as unsigned integers whose order is the key type's order (ascending);
+// descending order is the complement.  Floats: negative values have all bits
+// flipped, the others only the sign bit (IEEE total order for non-NaN keys).
+template <typename U> struct Bits;
+template <> struct Bits<uint32_t> {
+  static constexpr uint32_t sign = 0x80000000u;
+};
+template <> struct Bits<unsigned long long> {
+  static constexpr unsigned long long sign = 0x8000000000000000ull;
+};
+
+template <typename U>
+__device__ __forceinline__ U to_ordered(U x, int kind, bool desc) {
+  // kind: 0 unsigned, 1 signed, 2 float
+  U t = x;
+  if (kind == 1) t = x ^ Bits<U>::sign;
+  if (kind == 2) t = (x & Bits<U>::sign) ? (U)~x : (U)(x ^ Bits<U>::sign);
+  return desc ? (U)~t : t;
+}
+
+template <typename U>
+__device__ __forceinline__ U from_ordered(U t, int kind, bool desc) {
+  if (desc) t = (U)~t;
+  if (kind == 1) return t ^ Bits<U>::sign;
+  if (kind == 2) return (t & Bits<U>::sign) ? (U)(t ^ Bits<U>::sign) : (U)~t;
+  return t;
+}
+
+template <typename U>
+__global__ void k_order_keys(U* keys, long long n, int kind, int desc, int inverse) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    keys[i] = inverse ? from_ordered(keys[i], kind, desc != 0) : to_ordered(keys[i], kind, desc != 0);
+}
+
+// Digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
+template <typename U>
+__global__ void __launch_bounds__(kPT) k_digit_hist(const U* __restrict__ keys, long long n,
+                                                    int shift, uint32_t* __restrict__ hist,
+                                                    int tiles) {
+  __shared__ uint32_t s_h[256];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    s_h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long b = (long long)tile * kPTile;
+#pragma unroll 4
+    for (int e = 0; e < kPI; ++e) {
+      const long long i = b + e * kPT + threadIdx.x;
+      if (i < n) atomicAdd(&s_h[(unsigned)(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(long long)threadIdx.x * tiles + tile] = s_h[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+// Stable scatter of one pass.  Warp w of a tile owns its 512 consecutive
+// elements (tile-local w*512 + e*32 + lane, e = 0..15, loads coalesced) and
+// ranks them in element order against warp-private digit counters (warp
+// match: equal digits of earlier lanes, plus the warp's earlier rounds).  A
+// block-wide prefix over (digit, warp) and over the tile's digits then gives
+// every element its place in the tile sorted by digit; keys and source
+// indices are staged there in shared memory, and written out in that order:
+// consecutive threads write consecutive places of one digit's run (the
+// tile's offset for the digit, from the scanned histograms), values gathered
+// from the tile's own range.
+template <typename U>
+__global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin,
+                                                       U* __restrict__ kout,
+                                                       const uint32_t* __restrict__ vin,
+                                                       uint32_t* __restrict__ vout, int vwords,
+                                                       long long n, int shift,
+                                                       const uint32_t* __restrict__ off,
+                                                       int tiles) {
+  extern __shared__ unsigned long long s_dyn[];
+  U* s_key = reinterpret_cast<U*>(s_dyn);                        // [kPTile]
+  uint32_t* s_src = reinterpret_cast<uint32_t*>(s_key + kPTile);  // [kPTile]
+  uint32_t* s_cnt = s_src + kPTile;                               // [kPT/32][256]
+  uint32_t* s_dst = s_cnt + (kPT / 32) * 256;                     // [256] global run start - local start
+  uint32_t* s_warp = s_dst + 256;                                 // [kPT/32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t* cnt = s_cnt + warp * 256;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+#pragma unroll
+    for (int w = 0; w < kPT / 32; ++w) s_cnt[w * 256 + threadIdx.x] = 0;
+    __syncthreads();
+    const long long tb = (long long)tile * kPTile;
+    const int lb = warp * (kPI * 32);
+    U key[kPI];
+    uint32_t rank[kPI];
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const long long i = tb + lb + e * 32 + lane;
+      const bool ok = i < n;
+      key[e] = ok ? kin[i] : (U)0;
+      const unsigned d = ok ? ((unsigned)(key[e] >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(kFull, d);
+      const uint32_t before = d < 256u ? cnt[d] : 0u;
+      rank[e] = before + __popc(peers & lt);
+      __syncwarp();
+      if (d < 256u && lane == __ffs(peers) - 1) cnt[d] = before + __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // thread t = digit: its tile count, prefix over warps, and the tile-local
+    // start of its run (exclusive scan over the digits)
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kPT / 32; ++w) {
+      const uint32_t c = s_cnt[w * 256 + threadIdx.x];
+      s_cnt[w * 256 + threadIdx.x] = tot;
+      tot += c;
+    }
+    uint32_t x = tot;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t lstart = x - tot;
+    for (int w = 0; w < warp; ++w) lstart += s_warp[w];
+#pragma unroll
+    for (int w = 0; w < kPT / 32; ++w) s_cnt[w * 256 + threadIdx.x] += lstart;
+    s_dst[threadIdx.x] = off[(long long)threadIdx.x * tiles + tile] - lstart;
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const int li = lb + e * 32 + lane;
+      if (tb + li < n) {
+        const unsigned d = (unsigned)(key[e] >> shift) & 255u;
+        const uint32_t lp = cnt[d] + rank[e];
+        s_key[lp] = key[e];
+        s_src[lp] = (uint32_t)li;
+      }
+    }
+    __syncthreads();
+    const int valid = (int)min((long long)kPTile, n - tb);
+    for (int j = threadIdx.x; j < valid; j += kPT) {
+      const U k = s_key[j];
+      const uint32_t pos = s_dst[(unsigned)(k >> shift) & 255u] + j;
+      kout[pos] = k;
+      const long long src = tb + s_src[j];
+      for (int q = 0; q < vwords; ++q) vout[(long long)pos * vwords + q] = vin[src * vwords + q];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename U>
+size_t scatter_smem() {
+  return (size_t)kPTile * sizeof(U) + (size_t)kPTile * 4 + (kPT / 32) * 256 * 4 + 256 * 4 +
+         (kPT / 32) * 4;
+}
+
+// ---- compaction (Unique, StreamCompact) ----------------------------------
+
+// Whether element i is kept.  mode 0: stencil int32 != 0; 1: stencil float
+// != 0; 2: key differs from the previous key (word-sized keys compared as
+// values of the key type, so +0.0 and -0.0 are equal and NaNs all differ).
+struct KeepTest {
+  int mode;
+  int key_kind;   // for mode 2: 0 unsigned, 1 signed, 2 float
+  int key_bytes;  // 4 or 8
+  const void* data;
+  __device__ __forceinline__ bool operator()(long long i) const {
+    if (mode == 0) return static_cast<const int32_t*>(data)[i] != 0;
+    if (mode == 1) return static_cast<const float*>(data)[i] != 0.0f;
+    if (i == 0) return true;
+    if (key_bytes == 4) {
+      if (key_kind == 2) {
+        const float* k = static_cast<const float*>(data);
+        return k[i] != k[i - 1];
+      }
+      const uint32_t* k = static_cast<const uint32_t*>(data);
+      return k[i] != k[i - 1];
+    }
+    const unsigned long long* k = static_cast<const unsigned long long*>(data);
+    return k[i] != k[i - 1];
+  }
+};
+
+__global__ void __launch_bounds__(kPT) k_keep_count(KeepTest keep, long long n,
+                                                    unsigned long long* __restrict__ cnt,
+                                                    int tiles) {
+  __shared__ unsigned long long s_warp[kPT / 32];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    unsigned long long c = 0;
+    const long long b = (long long)tile * kPTile;
+#pragma unroll 4
+    for (int e = 0; e < kPI; ++e) {
+      const long long i = b + e * kPT + threadIdx.x;
+      if (i < n && keep(i)) ++c;
+    }
+    unsigned long long tot;
+    block_exclusive(c, s_warp, &tot);
+    if (threadIdx.x == 0) cnt[tile] = tot;
+  }
+}
+
+// Order-preserving scatter of the kept elements: element bytes (a multiple of
+// 4) from `in`, or the element's index as int32 when `in` is NULL.
+__global__ void __launch_bounds__(kPT) k_keep_scatter(KeepTest keep, const uint32_t* __restrict__ in,
+                                                      int words, long long n, uint32_t* __restrict__ out,
+                                                      const unsigned long long* __restrict__ pre,
+                                                      int tiles) {
+  __shared__ unsigned long long s_warp[kPT / 32];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long b = (long long)tile * kPTile + (long long)threadIdx.x * kPI;
+    uint32_t flags = 0;
+    unsigned long long c = 0;
+#pragma unroll
+    for (int e = 0; e < kPI; ++e)
+      if (b + e < n && keep(b + e)) {
+        flags |= 1u << e;
+        ++c;
+      }
+    unsigned long long tot;
+    unsigned long long pos = pre[tile] + block_exclusive(c, s_warp, &tot);
+    for (uint32_t f = flags; f; f &= f - 1, ++pos) {
+      const long long i = b + __ffs(f) - 1;
+      if (in) {
+        for (int q = 0; q < words; ++q) out[pos * words + q] = in[i * words + q];
+      } else {
+        out[pos] = (uint32_t)i;
+      }
+    }
+  }
+}
+
+// Kept elements of `in` (or their indices) into `out`; the count goes to
+// cnt_pre[tiles] on the device.  cnt_pre holds sum_slots(n) entries.
+void keep_pass(const KeepTest& keep, const void* in, int words, long long n, void* out,
+               unsigned long long* cnt_pre, int num_sms, cudaStream_t s) {
+  const int tiles = ptiles(n);
+  const int b = resident((const void*)k_keep_count, kPT, num_sms, tiles);
+  k_keep_count<<<b, kPT, 0, s>>>(keep, n, cnt_pre, tiles);
+  scan_sums<unsigned long long>(cnt_pre, tiles, cnt_pre + tiles + 1, s);
+  k_keep_scatter<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), words, n,
+                                   static_cast<uint32_t*>(out), cnt_pre, tiles);
+}
+
+// ---- sort driver -----------------------------------------------------------
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct SortLayout {
+  size_t ktmp, vtmp, hist, sums, total;
+};
+
+SortLayout sort_layout(long long n, int key_bytes, int value_bytes) {
+  const long long tiles = ptiles(n);
+  const long long hn = 256 * tiles;
+  SortLayout L;
+  L.ktmp = 0;
+  L.vtmp = align256(L.ktmp + (size_t)n * key_bytes);
+  L.hist = align256(L.vtmp + (size_t)n * value_bytes);
+  L.sums = align256(L.hist + (size_t)hn * 4);
+  L.total = align256(L.sums + (size_t)sum_slots(hn) * 4);
+  return L;
+}
+
+template <typename U>
+void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool desc,
+                char* scratch, int num_sms, cudaStream_t s) {
+  const SortLayout L = sort_layout(n, (int)sizeof(U), 4 * vwords);
+  U* ktmp = reinterpret_cast<U*>(scratch + L.ktmp);
+  uint32_t* vtmp = reinterpret_cast<uint32_t*>(scratch + L.vtmp);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.hist);
+  void* sums = scratch + L.sums;
+  const int tiles = ptiles(n);
+  const int ob = resident((const void*)k_order_keys<U>, 256, num_sms, (n + 255) / 256);
+  k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 0);
+  const int bh = resident((const void*)k_digit_hist<U>, kPT, num_sms, tiles);
+  const size_t sm = scatter_smem<U>();
+  cudaFuncSetAttribute(k_digit_scatter<U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_digit_scatter<U>, kPT, sm) !=
+          cudaSuccess || per < 1)
+    per = 1;
+  const int bs = (int)(tiles < (long long)num_sms * per ? tiles : (long long)num_sms * per);
+  const int passes = (int)sizeof(U);  // one 8-bit digit per byte: an even count
+  for (int p = 0; p < passes; ++p) {
+    const U* ksrc = (p & 1) ? ktmp : keys;
+    U* kdst = (p & 1) ? keys : ktmp;
+    const uint32_t* vsrc = (p & 1) ? vtmp : vals;
+    uint32_t* vdst = (p & 1) ? vals : vtmp;
+    k_digit_hist<U><<<bh, kPT, 0, s>>>(ksrc, n, 8 * p, hist, tiles);
+    scan_t<uint32_t>(hist, hist, 256ll * tiles, true, sums, nullptr, num_sms, s);
+    k_digit_scatter<U><<<bs, kPT, sm, s>>>(ksrc, kdst, vsrc, vdst, vwords, n, 8 * p, hist, tiles);
+  }
+  k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 1);
+}
+
+// ---- bounds -------------------------------------------------------------------
+
+template <typename T, bool UPPER>
+__global__ void k_bounds(const T* __restrict__ sorted, long long n, const T* values, long long m,
+                         int32_t* out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T v = values[i];
+    long long lo = 0, hi = n;  // first index whose element is >= v (> v for UPPER)
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      const T x = sorted[mid];
+      const bool before = UPPER ? !(v < x) : (x < v);
+      if (before) lo = mid + 1;
+      else hi = mid;
+    }
+    out[i] = (int32_t)lo;
+  }
+}
+
+}  // namespace
+
+namespace {
+
+int prim_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  return sms;
+}
+
+int bad(const char* msg) {
+  set_last_error(msg);
+  return DAX_GB300_ERROR_BAD_VALUE;
+}
+
+int launched(const char* where) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return DAX_GB300_SUCCESS;
+  set_last_error(std::string(where) + ": " + cudaGetErrorString(e));
+  return DAX_GB300_ERROR_CUDA;
+}
+
+int type_bytes(int t) {
+  switch (t) {
+    case DAX_GB300_TYPE_I32: case DAX_GB300_TYPE_U32: case DAX_GB300_TYPE_F32: return 4;
+    case DAX_GB300_TYPE_I64: case DAX_GB300_TYPE_U64: return 8;
+    default: return 0;
+  }
+}
+
+int type_kind(int t) {
+  return (t == DAX_GB300_TYPE_F32) ? 2 : ((t == DAX_GB300_TYPE_I32 || t == DAX_GB300_TYPE_I64) ? 1 : 0);
+}
+
+bool size_ok(long long n) { return n >= 0 && n <= 2147483647ll; }
+
+int read_back(void* host, const void* dev, size_t bytes, cudaStream_t s, const char* what) {
+  cudaError_t e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) return DAX_GB300_SUCCESS;
+  set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return DAX_GB300_ERROR_CUDA;
+}
+
+size_t scan_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
+
+size_t keep_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
+
+}  // namespace
+}  // namespace daxgb
+
+using daxgb::align256;
+
+extern "C" {
+
+size_t dax_gb300_scan_scratch_bytes(int64_t n) { return daxgb::scan_bytes(n < 1 ? 1 : n); }
+
+int dax_gb300_scan(const void* d_in, void* d_out, int64_t n, int type, int exclusive,
+                   void* d_scratch, size_t scratch_bytes, void* h_total, void* stream) {
+  using namespace daxgb;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!size_ok(n)) return bad("scan length must be in [0, 2^31 - 1]");
+  const int tb = type_bytes(type);
+  if (!tb) return bad("unknown element type");
+  if (n == 0) {
+    if (h_total) memset(h_total, 0, (size_t)tb);
+    return DAX_GB300_SUCCESS;
+  }
+  if (!d_in || !d_out || !d_scratch) return bad("NULL input, output or scratch");
+  if (scratch_bytes < scan_bytes(n)) return bad("scratch smaller than dax_gb300_scan_scratch_bytes()");
+  const int sms = prim_sms();
+  char* sc = static_cast<char*>(d_scratch);
+  switch (type) {
+    case DAX_GB300_TYPE_I32: scan_t<int32_t>((const int32_t*)d_in, (int32_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+    case DAX_GB300_TYPE_U32: scan_t<uint32_t>((const uint32_t*)d_in, (uint32_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+    case DAX_GB300_TYPE_F32: scan_t<float>((const float*)d_in, (float*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+    case DAX_GB300_TYPE_I64: scan_t<int64_t>((const int64_t*)d_in, (int64_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+    default: scan_t<unsigned long long>((const unsigned long long*)d_in, (unsigned long long*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+  }
+  int st = launched("scan kernels");
+  if (st || !h_total) return st;
+  // the scanned tile sums end with the grand total, in a type as wide as the element
+  return read_back(h_total, sc + (size_t)ptiles(n) * tb, (size_t)tb, s, "reading the scan total");
+}
+
+size_t dax_gb300_sort_scratch_bytes(int64_t n, int key_type, int value_bytes) {
+  using namespace daxgb;
+  const int kb = type_bytes(key_type);
+  if (!kb || n < 0 || value_bytes < 0 || value_bytes > 16 || (value_bytes & 3)) return 0;
+  const long long nn = n < 1 ? 1 : n;
+  const SortLayout L = sort_layout(nn, kb, value_bytes);
+  return L.total + scan_bytes(256ll * ptiles(nn));
+}
+
+int dax_gb300_sort_by_key(void* d_keys, void* d_values, int64_t n, int key_type, int value_bytes,
+                          int descending, void* d_scratch, size_t scratch_bytes, void* stream) {
+  using namespace daxgb;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!size_ok(n)) return bad("sort length must be in [0, 2^31 - 1]");
+  const int kb = type_bytes(key_type);
+  if (!kb) return bad("unknown key type");
+  if (value_bytes < 0 || value_bytes > 16 || (value_bytes & 3))
+    return bad("value size must be 0, 4, 8, 12 or 16 bytes");
+  if (n < 2) return DAX_GB300_SUCCESS;
+  if (!d_keys || (value_bytes && !d_values) || !d_scratch) return bad("NULL keys, values or scratch");
+  if (scratch_bytes < dax_gb300_sort_scratch_bytes(n, key_type, value_bytes))
+    return bad("scratch smaller than dax_gb300_sort_scratch_bytes()");
+  const int kind = type_kind(key_type);
+  char* sc = static_cast<char*>(d_scratch);
+  if (kb == 4)
+    radix_sort<uint32_t>(static_cast<uint32_t*>(d_keys), static_cast<uint32_t*>(d_values),
+                         value_bytes / 4, n, kind, descending != 0, sc, prim_sms(), s);
+  else
+    radix_sort<unsigned long long>(static_cast<unsigned long long*>(d_keys),
+                                   static_cast<uint32_t*>(d_values), value_bytes / 4, n, kind,
+                                   descending != 0, sc, prim_sms(), s);
+  return launched("sort kernels");
+}
+
+size_t dax_gb300_compact_scratch_bytes(int64_t n, int element_bytes) {
+  using namespace daxgb;
+  if (n < 0 || element_bytes < 0) return 0;
+  const long long nn = n < 1 ? 1 : n;
+  return keep_bytes(nn) + align256((size_t)nn * element_bytes);
+}
+
+int dax_gb300_unique(void* d_keys, int64_t n, int key_type, void* d_scratch, size_t scratch_bytes,
+                     int64_t* h_count, void* stream) {
+  using namespace daxgb;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!size_ok(n)) return bad("unique length must be in [0, 2^31 - 1]");
+  const int kb = type_bytes(key_type);
+  if (!kb) return bad("unknown key type");
+  if (n == 0) {
+    if (h_count) *h_count = 0;
+    return DAX_GB300_SUCCESS;
+  }
+  if (!d_keys || !d_scratch) return bad("NULL keys or scratch");
+  if (scratch_bytes < dax_gb300_compact_scratch_bytes(n, kb))
+    return bad("scratch smaller than dax_gb300_compact_scratch_bytes(n, key bytes)");
+  char* sc = static_cast<char*>(d_scratch);
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(sc);
+  void* tmp = sc + keep_bytes(n);
+  KeepTest keep{2, type_kind(key_type), kb, d_keys};
+  keep_pass(keep, d_keys, kb / 4, n, tmp, cnt, prim_sms(), s);
+  cudaMemcpyAsync(d_keys, tmp, (size_t)n * kb, cudaMemcpyDeviceToDevice, s);
+  int st = launched("unique kernels");
+  if (st || !h_count) return st;
+  unsigned long long c = 0;
+  st = read_back(&c, cnt + ptiles(n), sizeof(c), s, "reading the unique count");
+  *h_count = (int64_t)c;
+  return st;
+}
+
+int dax_gb300_stream_compact(const void* d_input, int value_bytes, const void* d_stencil,
+                             int stencil_type, int64_t n, void* d_output, void* d_scratch,
+                             size_t scratch_bytes, int64_t* h_count, void* stream) {
+  using namespace daxgb;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!size_ok(n)) return bad("compaction length must be in [0, 2^31 - 1]");
+  if (stencil_type != DAX_GB300_TYPE_I32 && stencil_type != DAX_GB300_TYPE_F32)
+    return bad("stencil must be int32 or float");
+  if (d_input && (value_bytes <= 0 || value_bytes > 16 || (value_bytes & 3)))
+    return bad("value size must be 4, 8, 12 or 16 bytes");
+  if (n == 0) {
+    if (h_count) *h_count = 0;
+    return DAX_GB300_SUCCESS;
+  }
+  if (!d_stencil || !d_output || !d_scratch) return bad("NULL stencil, output or scratch");
+  if (scratch_bytes < dax_gb300_compact_scratch_bytes(n, 0))
+    return bad("scratch smaller than dax_gb300_compact_scratch_bytes(n, 0)");
+  unsigned long long* cnt = static_cast<unsigned long long*>(d_scratch);
+  KeepTest keep{stencil_type == DAX_GB300_TYPE_I32 ? 0 : 1, 0, 4, d_stencil};
+  keep_pass(keep, d_input, d_input ? value_bytes / 4 : 1, n, d_output, cnt, prim_sms(), s);
+  int st = launched("compaction kernels");
+  if (st || !h_count) return st;
+  unsigned long long c = 0;
+  st = read_back(&c, cnt + ptiles(n), sizeof(c), s, "reading the compacted count");
+  *h_count = (int64_t)c;
+  return st;
+}
+
+int dax_gb300_bounds(const void* d_sorted, int64_t n, const void* d_values, int64_t m,
+                     int key_type, int upper, int32_t* d_out, void* stream) {
+  using namespace daxgb;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!size_ok(n) || !size_ok(m)) return bad("lengths must be in [0, 2^31 - 1]");
+  if (!type_bytes(key_type)) return bad("unknown key type");
+  if (m == 0) return DAX_GB300_SUCCESS;
+  if ((n && !d_sorted) || !d_values || !d_out) return bad("NULL input, values or output");
+  const int b = (int)((m + 255) / 256 < prim_sms() * 8 ? (m + 255) / 256 : prim_sms() * 8);
+#define DAXGB_BOUNDS(T)                                                                         \
+  (upper ? k_bounds<T, true><<<b, 256, 0, s>>>((const T*)d_sorted, n, (const T*)d_values, m, d_out) \
+         : k_bounds<T, false><<<b, 256, 0, s>>>((const T*)d_sorted, n, (const T*)d_values, m, d_out))
+  switch (key_type) {
+    case DAX_GB300_TYPE_I32: DAXGB_BOUNDS(int32_t); break;
+    case DAX_GB300_TYPE_U32: DAXGB_BOUNDS(uint32_t); break;
+    case DAX_GB300_TYPE_F32: DAXGB_BOUNDS(float); break;
+    case DAX_GB300_TYPE_I64: DAXGB_BOUNDS(int64_t); break;
+    default: DAXGB_BOUNDS(unsigned long long); break;
+  }
+#undef DAXGB_BOUNDS
+  return launched("bounds kernel");
+}
+
+}  // extern "C"

@@ -273,6 +273,72 @@ int dax_gb300_field_adjoint(const dax_gb300_uniform_grid* grid, const float* d_f
                             const float* d_grad_vertices, const float* d_grad_cell_gradient,
                             float* d_grad_field, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Generic primitives of the device adapter                                  */
+/* (dax::cont::internal::DeviceAdapterAlgorithm<Tag>,                         */
+/*  dax/cont/internal/DeviceAdapterAlgorithm.h:44-331; generic versions in    */
+/*  dax/cont/internal/DeviceAdapterAlgorithmGeneral.h)                        */
+/* ------------------------------------------------------------------------ */
+
+/* Element types.  dax::Id is DAX_GB300_TYPE_I32, dax::Scalar F32. */
+#define DAX_GB300_TYPE_I32 0
+#define DAX_GB300_TYPE_U32 1
+#define DAX_GB300_TYPE_F32 2
+#define DAX_GB300_TYPE_I64 3
+#define DAX_GB300_TYPE_U64 4
+
+/* Scratch bytes for dax_gb300_scan on n elements (any type). */
+size_t dax_gb300_scan_scratch_bytes(int64_t n);
+
+/* ScanInclusive / ScanExclusive (DeviceAdapterAlgorithm.h ScanInclusive,
+ * ScanExclusive; DeviceAdapterAlgorithmGeneral.h:337-448): d_out[i] = sum of
+ * d_in[0..i] (inclusive) or d_in[0..i-1] (exclusive), any type above; d_out
+ * may equal d_in.  Integer sums wrap in the element width.  If h_total is
+ * not NULL it receives the sum of all elements (one element of the type; the
+ * stream is synchronised for it), which is what the reference returns. */
+int dax_gb300_scan(const void* d_in, void* d_out, int64_t n, int type, int exclusive,
+                   void* d_scratch, size_t scratch_bytes, void* h_total, void* stream);
+
+/* Scratch bytes for dax_gb300_sort_by_key (0 for an unsupported shape). */
+size_t dax_gb300_sort_scratch_bytes(int64_t n, int key_type, int value_bytes);
+
+/* Sort / SortByKey (DeviceAdapterAlgorithm.h Sort, SortByKey;
+ * DeviceAdapterAlgorithmGeneral.h:658-695): sorts d_keys in place, ascending
+ * (descending = 0, the reference's default and SortLess) or descending
+ * (SortGreater), carrying d_values (value_bytes = 0 for Sort, else 4, 8, 12
+ * or 16 bytes per element: a dax::Vector3 is 12).  Stable: equal keys keep
+ * their order (the reference leaves it unspecified).  Float keys sort by
+ * IEEE order with -0 before +0; NaN keys are not supported. */
+int dax_gb300_sort_by_key(void* d_keys, void* d_values, int64_t n, int key_type, int value_bytes,
+                          int descending, void* d_scratch, size_t scratch_bytes, void* stream);
+
+/* Scratch bytes for dax_gb300_unique (element_bytes = key bytes) and
+ * dax_gb300_stream_compact (element_bytes = 0). */
+size_t dax_gb300_compact_scratch_bytes(int64_t n, int element_bytes);
+
+/* Unique (DeviceAdapterAlgorithmGeneral.h:905-927): keeps the first of every
+ * run of equal adjacent keys, in place, in order.  h_count (if not NULL, the
+ * stream is synchronised) receives the new length -- the reference shrinks
+ * the array to it. */
+int dax_gb300_unique(void* d_keys, int64_t n, int key_type, void* d_scratch, size_t scratch_bytes,
+                     int64_t* h_count, void* stream);
+
+/* StreamCompact (DeviceAdapterAlgorithmGeneral.h:770-830): the elements of
+ * d_input (value_bytes each: 4, 8, 12 or 16) whose stencil entry differs from
+ * zero, in order; with d_input NULL, the int32 indices of those entries (the
+ * reference's one-argument form).  Stencil: int32 or float.  h_count as for
+ * dax_gb300_unique.  d_output holds n elements at most. */
+int dax_gb300_stream_compact(const void* d_input, int value_bytes, const void* d_stencil,
+                             int stencil_type, int64_t n, void* d_output, void* d_scratch,
+                             size_t scratch_bytes, int64_t* h_count, void* stream);
+
+/* LowerBounds / UpperBounds (DeviceAdapterAlgorithmGeneral.h:175-308,
+ * :961-1091): for each of the m values, the first index of the sorted array
+ * (n elements) whose element is not less than (upper = 0) or greater than
+ * (upper = 1) the value, as int32.  d_out may equal d_values for 4-byte keys. */
+int dax_gb300_bounds(const void* d_sorted, int64_t n, const void* d_values, int64_t m,
+                     int key_type, int upper, int32_t* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
