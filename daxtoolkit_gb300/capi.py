@@ -89,6 +89,10 @@ SIGNATURES = {
     "dax_gb300_graph_launch": ([vp, vp], i32),
     "dax_gb300_graph_destroy": ([vp], i32),
     "dax_gb300_mc_noalloc": ([gp, vp, f32, i32, vp, i64, vp, i64, vp, vp], i32),
+    "dax_gb300_slice_field": ([gp, vp, vp, vp, ctypes.POINTER(f32), vp], i32),
+    "dax_gb300_slice_count": ([gp, vp, vp, vp, sz, vp], i32),
+    "dax_gb300_slice_generate": ([gp, vp, vp, ctypes.c_int, vp, sz, vp, i64, vp, i64, vp, vp, vp,
+                                  vp], i32),
     "dax_gb300_scan_scratch_bytes": ([i64], sz),
     "dax_gb300_scan": ([vp, vp, i64, i32, i32, vp, sz, vp, vp], i32),
     "dax_gb300_sort_scratch_bytes": ([i64, i32, i32], sz),

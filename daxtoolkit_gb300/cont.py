@@ -20,7 +20,7 @@ __all__ = [
     "UniformGrid", "UnstructuredGrid", "MarchingCubesCount", "MarchingCubesGenerate",
     "ThresholdCount", "ThresholdTopology", "CellGradient", "DispatcherMapCell",
     "DispatcherGenerateInterpolatedCells", "DispatcherGenerateTopology", "marching_cubes",
-    "threshold", "cell_gradient", "Scratch",
+    "threshold", "cell_gradient", "Scratch", "SliceCount", "SliceGenerate", "slice", "slice_field",
 ]
 
 
@@ -161,6 +161,19 @@ class MarchingCubesGenerate:
         self.IsoValue = float(isovalue)
 
 
+class SliceCount:
+    """dax/worklet/Slice.h:28-77: triangles per cell of the plane through
+    `origin` with `normal` (the point field is the grid's coordinates)."""
+
+    def __init__(self, origin, normal):
+        self.Origin = tuple(float(v) for v in origin)
+        self.Normal = tuple(float(v) for v in normal)
+
+
+class SliceGenerate(SliceCount):
+    """dax/worklet/Slice.h:82-168."""
+
+
 class ThresholdCount:
     """dax/worklet/Threshold.h:69-96."""
 
@@ -204,6 +217,52 @@ def marching_cubes(grid, field, isovalue, merge=True, records=False, scratch=Non
     capi.call("dax_gb300_mc_generate", ctypes.byref(g), _ptr(field), float(isovalue),
               int(bool(merge)), _ptr(buf), buf.numel(), _ptr(verts), V, _ptr(conn), T, _ptr(ra),
               _ptr(rb), _ptr(rw), s)
+    out = dict(verts=verts, conn=conn)
+    if records:
+        out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
+    return out
+
+
+def slice_field(grid, origin, normal, out=None, stream=None):
+    """The point field of a slice, dot(normal, coord(p) - origin), and its
+    isovalue dot(normal, origin): marching cubes of it is the reference's
+    Slice (dax/worklet/Slice.h)."""
+    g = grid.desc()
+    if out is None:
+        out = torch.empty(grid.GetNumberOfPoints(), dtype=torch.float32, device="cuda")
+    o = (ctypes.c_float * 3)(*[float(v) for v in origin])
+    nrm = (ctypes.c_float * 3)(*[float(v) for v in normal])
+    iso = ctypes.c_float(0.0)
+    capi.call("dax_gb300_slice_field", ctypes.byref(g), o, nrm, _ptr(out), ctypes.byref(iso),
+              _stream(stream))
+    return out, iso.value
+
+
+def slice(grid, origin, normal, merge=True, records=False, scratch=None, stream=None):
+    """Triangles of the reference's Slice (SliceCount + SliceGenerate) for the
+    plane given by `origin` and `normal`: the same dict as marching_cubes.
+    The slice field is evaluated from the grid coordinates; none is stored."""
+    g = grid.desc()
+    s = _stream(stream)
+    o = (ctypes.c_float * 3)(*[float(v) for v in origin])
+    nrm = (ctypes.c_float * 3)(*[float(v) for v in normal])
+    nbytes = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    buf = (scratch or _scratch_for("mc")).get(nbytes)
+    capi.call("dax_gb300_slice_count", ctypes.byref(g), o, nrm, _ptr(buf), buf.numel(), s)
+    T, Vm = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", _ptr(buf), ctypes.byref(T), ctypes.byref(Vm), s)
+    T = T.value
+    V = Vm.value if merge else 3 * T
+    dev = buf.device
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+    ra = rb = rw = None
+    if records:
+        ra = torch.empty(V, dtype=torch.int32, device=dev)
+        rb = torch.empty(V, dtype=torch.int32, device=dev)
+        rw = torch.empty(V, dtype=torch.float32, device=dev)
+    capi.call("dax_gb300_slice_generate", ctypes.byref(g), o, nrm, int(bool(merge)), _ptr(buf),
+              buf.numel(), _ptr(verts), V, _ptr(conn), T, _ptr(ra), _ptr(rb), _ptr(rw), s)
     out = dict(verts=verts, conn=conn)
     if records:
         out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
@@ -255,15 +314,22 @@ class DispatcherMapCell:
     def __init__(self, worklet):
         self.worklet = worklet
 
-    def Invoke(self, grid, field, stream=None):
-        _require_field(field, grid)
+    def Invoke(self, grid, field=None, stream=None):
         w = self.worklet
+        if not isinstance(w, SliceCount):  # a slice's point field is the implicit coordinates
+            _require_field(field, grid)
         g = grid.desc()
         C = grid.GetNumberOfCells()
         if isinstance(w, MarchingCubesCount):
             count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
             capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field), w.IsoValue,
                       _ptr(count), None, _stream(stream))
+            return count
+        if isinstance(w, SliceCount):
+            sf, iso = slice_field(grid, w.Origin, w.Normal, stream=stream)
+            count = torch.empty(C, dtype=torch.int32, device=sf.device)
+            capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(sf), iso, _ptr(count),
+                      None, _stream(stream))
             return count
         if isinstance(w, ThresholdCount):
             count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
@@ -311,9 +377,14 @@ class DispatcherGenerateInterpolatedCells:
     def SetReleaseCount(self, b):
         self.ReleaseCount = bool(b)
 
-    def Invoke(self, grid, field, stream=None):
-        out = marching_cubes(grid, field, self.worklet.IsoValue, merge=self.RemoveDuplicatePoints,
-                             records=True, stream=stream)
+    def Invoke(self, grid, field=None, stream=None):
+        w = self.worklet
+        if isinstance(w, SliceGenerate):
+            out = slice(grid, w.Origin, w.Normal, merge=self.RemoveDuplicatePoints, records=True,
+                        stream=stream)
+        else:
+            out = marching_cubes(grid, field, w.IsoValue, merge=self.RemoveDuplicatePoints,
+                                 records=True, stream=stream)
         self._records = (out["rec_first"], out["rec_second"], out["rec_weight"])
         if self.ReleaseCount:
             self.count = None

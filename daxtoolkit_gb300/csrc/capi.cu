@@ -344,6 +344,79 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
   return check_launch("mc generate kernel");
 }
 
+int dax_gb300_slice_field(const dax_gb300_uniform_grid* grid, const float* origin,
+                          const float* normal, float* d_field, float* h_isovalue, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!origin || !normal || !d_field)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL origin, normal or field");
+  if (h_isovalue) *h_isovalue = daxgb::slice_isovalue(origin, normal);
+  daxgb::launch_slice_field(g, make_float3(origin[0], origin[1], origin[2]),
+                            make_float3(normal[0], normal[1], normal[2]), d_field, num_sms(),
+                            static_cast<cudaStream_t>(stream));
+  return check_launch("slice field kernel");
+}
+
+int dax_gb300_slice_count(const dax_gb300_uniform_grid* grid, const float* origin,
+                          const float* normal, void* d_scratch, size_t scratch_bytes,
+                          void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!origin || !normal || !d_scratch)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL origin, normal or scratch");
+  const McLayout L = mc_layout(g);
+  if (scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!has_cells(g)) {
+    cudaError_t e = cudaMemsetAsync(d_scratch, 0, sizeof(Info), s);
+    return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing scratch");
+  }
+  const int sms = num_sms();
+  const float iso = daxgb::slice_isovalue(origin, normal);
+  daxgb::GridSet S = daxgb::single_set(g, nullptr, iso, 0.0f);
+  S.one.plane_o = make_float3(origin[0], origin[1], origin[2]);
+  S.one.plane_n = make_float3(normal[0], normal[1], normal[2]);
+  uint32_t* bits = at<uint32_t>(d_scratch, L.bits);
+  const daxgb::WordOffsets wo = L.offsets(d_scratch);
+  // the row splits live in the active-word list (R <= R * wr entries), which
+  // the scan rewrites afterwards
+  daxgb::launch_slice_bits(g, S.one.plane_o, S.one.plane_n, iso, bits, daxgb::bit_words(g.P),
+                           wo.act, sms, s);
+  if ((st = check_launch("slice classify kernels"))) return st;
+  daxgb::launch_mc_scan(S, bits, wo, at<Info>(d_scratch, L.info), sms, s);
+  return check_launch("count/scan kernels");
+}
+
+int dax_gb300_slice_generate(const dax_gb300_uniform_grid* grid, const float* origin,
+                             const float* normal, int merge, void* d_scratch,
+                             size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                             int32_t* d_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                             int32_t* d_rec_second, float* d_rec_weight, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!has_cells(g)) return DAX_GB300_SUCCESS;
+  if (!origin || !normal || !d_scratch)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL origin, normal or scratch");
+  if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
+      tri_capacity < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
+  const McLayout L = mc_layout(g);
+  if (scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
+  daxgb::GridSet S = daxgb::single_set(g, nullptr, daxgb::slice_isovalue(origin, normal), 0.0f);
+  S.one.plane_o = make_float3(origin[0], origin[1], origin[2]);
+  S.one.plane_n = make_float3(normal[0], normal[1], normal[2]);
+  daxgb::launch_mc_emit(S, merge != 0, at<uint32_t>(d_scratch, L.bits), L.offsets(d_scratch),
+                        at<Info>(d_scratch, L.info), d_verts, vert_capacity, d_conn, tri_capacity,
+                        d_rec_first, d_rec_second, d_rec_weight, num_sms(),
+                        static_cast<cudaStream_t>(stream));
+  return check_launch("slice generate kernel");
+}
+
 int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t* d_rec_second,
                                       const float* d_rec_weight, int64_t n, const float* d_in,
                                       float* d_out, void* stream) {

@@ -67,6 +67,8 @@ struct GridSlot {
   long long word0;        // first bit word of the grid's bits (= 4 * chunk0)
   long long row0;         // first global point row
   long long rw0;          // first global row word (row-padded word arrays)
+  float3 plane_o;         // field == NULL: the implicit slice field
+  float3 plane_n;         //   dot(plane_n, coord - plane_o)
 };
 
 // A set of grids processed by one launch per pass.  count == 1: the grid is
@@ -137,6 +139,23 @@ __device__ __forceinline__ float coord(float o, float s, int i, int m) {
 // dax::math::Lerp(a, b, w) = a + w * (b - a), dax/math/VectorAnalysis.h:35-50.
 __device__ __forceinline__ float lerp_rn(float a, float b, float w) {
   return __fadd_rn(a, __fmul_rn(w, __fsub_rn(b, a)));
+}
+
+// The slice field at point (i, j, k): dot(N, coord - O) with dax::dot's
+// component order, a0*b0 + a1*b1 + a2*b2, every step rounded on its own
+// (dax/worklet/Slice.h:64-73, :131-138; dax/Types.h:611-621).
+__device__ __forceinline__ float plane_value(const Grid& g, const float3& o, const float3& n, int i,
+                                             int j, int k) {
+  const float dx = __fsub_rn(coord(g.ox, g.sx, i, g.mx), o.x);
+  const float dy = __fsub_rn(coord(g.oy, g.sy, j, g.my), o.y);
+  const float dz = __fsub_rn(coord(g.oz, g.sz, k, g.mz), o.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(n.x, dx), __fmul_rn(n.y, dy)), __fmul_rn(n.z, dz));
+}
+
+// Point value of slot sl at flat point p = (i, j, k): the stored field, or
+// the implicit slice field when the slot has none.
+__device__ __forceinline__ float slot_value(const GridSlot& sl, long long p, int i, int j, int k) {
+  return sl.field ? __ldg(sl.field + p) : plane_value(sl.g, sl.plane_o, sl.plane_n, i, j, k);
 }
 
 // 32 consecutive bits of the flat bit stream starting at bit `pos` (any

@@ -120,4 +120,15 @@ void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32
 
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s);
 
+// Slice: the isovalue dot(normal, origin); the classification bits of the
+// implicit field dot(normal, coord - origin) > iso (bit_words(P) words, the
+// layout launch_classify_bits writes; row_scratch: uint32[R] for the
+// per-row splits, or NULL to test every point); the field itself (float[P]).
+float slice_isovalue(const float origin[3], const float normal[3]);
+bool slice_rows_exact(const Grid& g, float3 o, float3 n);
+void launch_slice_bits(const Grid& g, float3 o, float3 n, float iso, uint32_t* bits,
+                       long long nwords, uint32_t* row_scratch, int num_sms, cudaStream_t s);
+void launch_slice_field(const Grid& g, float3 o, float3 n, float* out, int num_sms,
+                        cudaStream_t s);
+
 }  // namespace daxgb

@@ -391,15 +391,19 @@ void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o
 // Vertex on the edge owned by point (i, j, k) along `axis`:
 // weight = (iso - f[A]) / (f[B] - f[A]) (dax/worklet/MarchingCubes.h:160-161),
 // position = Lerp(coord A, coord B, weight) per component
-// (dax/exec/internal/kernel/GenerateWorklets.h:79-92).
-__device__ __forceinline__ void emit_vertex(const Grid& g, const float* __restrict__ f, float iso,
-                                            int i, int j, int k, int axis, long long vid,
-                                            float* __restrict__ verts, int32_t* __restrict__ ra,
-                                            int32_t* __restrict__ rb, float* __restrict__ rw) {
+// (dax/exec/internal/kernel/GenerateWorklets.h:79-92).  A slot without a
+// field is a slice: the end values are dot(N, coord - O), the same values
+// Slice.h:137 computes per cell vertex.
+__device__ __forceinline__ void emit_vertex(const GridSlot& sl, int i, int j, int k, int axis,
+                                            long long vid, float* __restrict__ verts,
+                                            int32_t* __restrict__ ra, int32_t* __restrict__ rb,
+                                            float* __restrict__ rw) {
+  const Grid& g = sl.g;
   const long long pa = ((long long)k * g.ny + j) * g.nx + i;
   const long long pb = pa + (axis == 0 ? 1ll : (axis == 1 ? (long long)g.nx : (long long)g.nx * g.ny));
-  const float fa = __ldg(f + pa), fb = __ldg(f + pb);
-  const float w = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
+  const float fa = slot_value(sl, pa, i, j, k);
+  const float fb = slot_value(sl, pb, i + (axis == 0), j + (axis == 1), k + (axis == 2));
+  const float w = __fdiv_rn(__fsub_rn(sl.iso, fa), __fsub_rn(fb, fa));
   const float xa = coord(g.ox, g.sx, i, g.mx), ya = coord(g.oy, g.sy, j, g.my),
               za = coord(g.oz, g.sz, k, g.mz);
   const float xb = axis == 0 ? coord(g.ox, g.sx, i + 1, g.mx) : xa;
@@ -674,7 +678,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
             ((ow.X >> b) & 1u) | (((ow.Y >> b) & 1u) << 1) | (((ow.Z >> b) & 1u) << 2);
         const int axis = nth_bit(own, left);
         const GridSlot& sl = S.count == 1 ? S.one : S.slots[window(st, kFSlot, s)];
-        emit_vertex(sl.g, sl.field, sl.iso, (int)window(st, kFI0, s) + b, (int)window(st, kFJ, s),
+        emit_vertex(sl, (int)window(st, kFI0, s) + b, (int)window(st, kFJ, s),
                     (int)window(st, kFK, s), axis, ow.base + rnk, verts, ra, rb, rw);
       }
     }
@@ -754,8 +758,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
           } else {
             const long long vid = 3 * tri + corner;
             conn[vid] = (int32_t)(vid - vbase0);
-            emit_vertex(sl.g, sl.field, sl.iso, i + di, j + dj, k + dk, axis, vid, verts, ra, rb,
-                        rw);
+            emit_vertex(sl, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
           }
         }
       }

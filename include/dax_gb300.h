@@ -168,6 +168,36 @@ int dax_gb300_mc_noalloc(const dax_gb300_uniform_grid* grid, const float* d_fiel
                          int64_t tri_capacity, int64_t* d_totals, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Slice (dax/worklet/Slice.h)                                               */
+/* ------------------------------------------------------------------------ */
+
+/* SliceCount + SliceGenerate (Slice.h:28-77, :82-168) as one count pass and
+ * one generate pass, with the scratch and totals of marching cubes:
+ * dax_gb300_mc_scratch_bytes(grid) bytes of scratch, dax_gb300_mc_totals()
+ * between the passes, outputs and merge exactly as dax_gb300_mc_generate.
+ * The cell values are s = dot(normal, coord - origin) against the isovalue
+ * dot(normal, origin), as Slice.h:64-73 computes them (the surface is the
+ * plane dot(normal, x) = 2 dot(normal, origin)); they are evaluated from the
+ * grid coordinates, so no field is read or stored.  origin and normal are
+ * host float[3].  Asynchronous. */
+int dax_gb300_slice_count(const dax_gb300_uniform_grid* grid, const float* origin,
+                          const float* normal, void* d_scratch, size_t scratch_bytes,
+                          void* stream);
+int dax_gb300_slice_generate(const dax_gb300_uniform_grid* grid, const float* origin,
+                             const float* normal, int merge, void* d_scratch,
+                             size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                             int32_t* d_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                             int32_t* d_rec_second, float* d_rec_weight, void* stream);
+
+/* The slice's point field itself: d_field[p] = dot(normal, coord(p) - origin)
+ * (float[P], device memory) and *h_isovalue = dot(normal, origin) if
+ * h_isovalue is not NULL.  Marching cubes of this field at this isovalue
+ * equals the slice; the per-cell SliceCount handle is
+ * dax_gb300_mc_classify_count of it.  Asynchronous. */
+int dax_gb300_slice_field(const dax_gb300_uniform_grid* grid, const float* origin,
+                          const float* normal, float* d_field, float* h_isovalue, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batched marching cubes: many grids, one launch per pass                   */
 /* ------------------------------------------------------------------------ */
 

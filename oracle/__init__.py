@@ -70,6 +70,12 @@ class Oracle:
         self._thr_gen.restype = i64
         self._grad = getattr(L, prefix + "cell_gradient")
         self._grad.argtypes = [gp, vp, vp]
+        self._slice_count = getattr(L, prefix + "slice_count")
+        self._slice_count.argtypes = [gp, vp, vp, vp]
+        self._slice_gen = getattr(L, prefix + "slice_generate")
+        self._slice_gen.argtypes = [gp, vp, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp,
+                                    ctypes.POINTER(i64)]
+        self._slice_gen.restype = i64
         if kind == "reference":
             L.ref_set_threads.argtypes = [ctypes.c_int]
             L.ref_max_threads.restype = ctypes.c_int
@@ -144,6 +150,33 @@ class Oracle:
         assert k == K
         U = pu.value
         return dict(conn=conn[:8 * K].reshape(K, 8), coords=coords[:U], field=fout[:U])
+
+    def slice_count(self, g, origin, normal):
+        o = np.asarray(origin, np.float32)
+        nrm = np.asarray(normal, np.float32)
+        count = np.zeros(self._cells(g), np.int32)
+        self._slice_count(ctypes.byref(g), _ptr(o), _ptr(nrm), _ptr(count))
+        return count
+
+    def slice_generate(self, g, origin, normal, count, merge=True):
+        """Returns dict(verts, conn, rec_a, rec_b, rec_w) as mc_generate."""
+        o = np.asarray(origin, np.float32)
+        nrm = np.asarray(normal, np.float32)
+        count = np.ascontiguousarray(count, dtype=np.int32)
+        T = int(count.astype(np.int64).sum())
+        cap = max(3 * T, 1)
+        verts = np.zeros((cap, 3), np.float32)
+        conn = np.zeros(cap, np.int32)
+        ra = np.zeros(cap, np.int32)
+        rb = np.zeros(cap, np.int32)
+        rw = np.zeros(cap, np.float32)
+        nv = ctypes.c_int64(0)
+        t = self._slice_gen(ctypes.byref(g), _ptr(o), _ptr(nrm), _ptr(count), int(bool(merge)),
+                            _ptr(verts), _ptr(conn), _ptr(ra), _ptr(rb), _ptr(rw), ctypes.byref(nv))
+        assert t == T
+        V = nv.value
+        return dict(verts=verts[:V], conn=conn[:3 * T].reshape(T, 3), rec_a=ra[:V], rec_b=rb[:V],
+                    rec_w=rw[:V])
 
     def cell_gradient(self, g, field):
         field = np.ascontiguousarray(field, dtype=np.float32).ravel()

@@ -356,3 +356,54 @@ void orc_cell_gradient(const orc_grid* g, const float* field, float* out) {
     for (int a = 0; a < 3; ++a) out[3 * c + a] = sum[a] / (c6[a] - c0[a]);
   }
 }
+
+/*
+ * Slice on a uniform grid (dax/worklet/Slice.h:28-168).  SliceCount and
+ * SliceGenerate classify and interpolate each cell with
+ * s = dot(normal, coords[v] - origin) per vertex against the isovalue
+ * dot(normal, origin), with the voxel edges listed lower point first
+ * (Slice.h:143-148) and the same TriTable, weight and merge as marching
+ * cubes.  s depends only on the point, so the slice is the marching-cubes
+ * dispatch on the point field s(p) with that isovalue.  dax::dot accumulates
+ * in component order, a0*b0 + a1*b1 + a2*b2 (dax/Types.h:611-620).
+ */
+static float dot3(const float a[3], const float b[3]) {
+  float r = a[0] * b[0];
+  r += a[1] * b[1];
+  r += a[2] * b[2];
+  return r;
+}
+
+static float* slice_field(const orc_grid* g, const float origin[3], const float normal[3],
+                          float* iso) {
+  int64_t d[3];
+  dims_of(g, d);
+  const int64_t P = d[0] * d[1] * d[2];
+  float* f = (float*)malloc(sizeof(float) * (P > 0 ? P : 1));
+  for (int64_t p = 0; p < P; ++p) {
+    float c[3], r[3];
+    point_coords(g, d, p, c);
+    for (int a = 0; a < 3; ++a) r[a] = c[a] - origin[a];
+    f[p] = dot3(normal, r);
+  }
+  *iso = dot3(normal, origin);
+  return f;
+}
+
+void orc_slice_count(const orc_grid* g, const float* origin, const float* normal, int32_t* count) {
+  float iso;
+  float* f = slice_field(g, origin, normal, &iso);
+  orc_mc_count(g, f, iso, count, NULL);
+  free(f);
+}
+
+int64_t orc_slice_generate(const orc_grid* g, const float* origin, const float* normal,
+                           const int32_t* count, int merge, float* verts, int32_t* conn,
+                           int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
+  float iso;
+  float* f = slice_field(g, origin, normal, &iso);
+  const int64_t T = orc_mc_generate(g, f, iso, count, merge, verts, conn, rec_a, rec_b, rec_w,
+                                    nverts);
+  free(f);
+  return T;
+}

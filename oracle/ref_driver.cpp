@@ -1,6 +1,6 @@
 // Reference-side CPU driver: runs the DaxToolkit's OWN worklet functors
-// (MarchingCubesCount, MarchingCubesGenerate, ThresholdCount,
-// ThresholdTopology, CellGradient), its TopologyUniform connectivity and
+// (MarchingCubesCount, MarchingCubesGenerate, SliceCount, SliceGenerate,
+// ThresholdCount, ThresholdTopology, CellGradient), its TopologyUniform connectivity and
 // point coordinates, its PointAsEdgeInterpolation ordering and dax::math::Lerp, compiled from the reference's headers.  Only the dispatcher
 // layer is restated here (the full dispatcher stack needs Boost.MPL and is not
 // buildable in this environment): it follows the Serial adapter's std::
@@ -18,6 +18,7 @@
 #include <dax/math/VectorAnalysis.h>
 #include <dax/worklet/CellGradient.h>
 #include <dax/worklet/MarchingCubes.h>
+#include <dax/worklet/Slice.h>
 #include <dax/worklet/Threshold.h>
 
 #include <algorithm>
@@ -62,6 +63,14 @@ struct Ctx {
   dax::exec::CellVertices<dax::CellTagVoxel> Verts(dax::Id cell) const {
     return topo.GetCellConnections(cell);
   }
+  // The cell's point coordinates, as BindCellPoints gathers them for a
+  // Vector3 point field.
+  dax::exec::CellField<dax::Vector3, dax::CellTagVoxel> Coords(
+      const dax::exec::CellVertices<dax::CellTagVoxel>& v) const {
+    dax::exec::CellField<dax::Vector3, dax::CellTagVoxel> c;
+    for (int n = 0; n < 8; ++n) c[n] = Coord(v[n]);
+    return c;
+  }
   template <typename T>
   dax::exec::CellField<T, dax::CellTagVoxel> Gather(
       const dax::exec::CellVertices<dax::CellTagVoxel>& v, const T* f) const {
@@ -97,6 +106,60 @@ dax::Id ScanAndUpperBounds(const int32_t* count, dax::Id C, std::vector<dax::Id>
 #pragma omp parallel for schedule(static) if (g_threads > 1)
   for (dax::Id t = 0; t < T; ++t)
     cellOf[t] = std::upper_bound(scan.begin(), scan.end(), t) - scan.begin();
+  return T;
+}
+
+// DispatcherGenerateInterpolatedCells with the Serial adapter
+// (dax/cont/DispatcherGenerateInterpolatedCells.h:158-301): ScanInclusive +
+// UpperBounds -> input cell of every output triangle, visit index, the
+// worklet's interpolated triangle, then (merge) Sort/Unique/LowerBounds of
+// the PointAsEdgeInterpolation records and the coordinates by Lerp.
+template <typename Build>
+int64_t GenerateInterpolated(const Ctx& ctx, const int32_t* count, int merge, float* verts,
+                             int32_t* conn, int32_t* rec_a, int32_t* rec_b, float* rec_w,
+                             int64_t* nverts, Build build) {
+  *nverts = 0;
+  std::vector<dax::Id> cellOf;
+  const dax::Id T = ScanAndUpperBounds(count, ctx.numCells, cellOf);
+  if (T == 0) return 0;
+  std::vector<dax::PointAsEdgeInterpolation> recs(3 * T);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id t = 0; t < T; ++t) {
+    // ComputeVisitIndex: workId - LowerBounds(cellIds, cellIds[t])
+    const dax::Id visit =
+        t - (std::lower_bound(cellOf.begin(), cellOf.end(), cellOf[t]) - cellOf.begin());
+    dax::exec::InterpolatedCellPoints<dax::CellTagTriangle> out;
+    build(cellOf[t], visit, out);
+    for (int m = 0; m < 3; ++m) recs[3 * t + m] = out[m];
+  }
+  std::vector<dax::PointAsEdgeInterpolation> weights(recs);
+  if (merge) {
+    sort_any(weights.begin(), weights.end());
+    weights.erase(std::unique(weights.begin(), weights.end()), weights.end());
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+    for (dax::Id i = 0; i < 3 * T; ++i)
+      conn[i] = (int32_t)(std::lower_bound(weights.begin(), weights.end(), recs[i]) -
+                          weights.begin());
+  } else {
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+    for (dax::Id i = 0; i < 3 * T; ++i) conn[i] = (int32_t)i;
+  }
+  const dax::Id V = (dax::Id)weights.size();
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id i = 0; i < V; ++i) {
+    const dax::PointAsEdgeInterpolation& r = weights[i];
+    dax::Vector3 p = dax::math::Lerp(ctx.Coord(r.EdgeIdFirst), ctx.Coord(r.EdgeIdSecond),
+                                     r.Weight);
+    verts[3 * i + 0] = p[0];
+    verts[3 * i + 1] = p[1];
+    verts[3 * i + 2] = p[2];
+    if (rec_a) {
+      rec_a[i] = r.EdgeIdFirst;
+      rec_b[i] = r.EdgeIdSecond;
+      rec_w[i] = r.Weight;
+    }
+  }
+  *nverts = V;
   return T;
 }
 
@@ -138,52 +201,39 @@ int64_t ref_mc_generate(const RefGrid* g, const float* field, float iso, const i
                         int merge, float* verts, int32_t* conn, int32_t* rec_a, int32_t* rec_b,
                         float* rec_w, int64_t* nverts) {
   Ctx ctx(g);
-  *nverts = 0;
-  std::vector<dax::Id> cellOf;
-  const dax::Id T = ScanAndUpperBounds(count, ctx.numCells, cellOf);
-  if (T == 0) return 0;
   dax::worklet::MarchingCubesGenerate worklet(iso);
-  std::vector<dax::PointAsEdgeInterpolation> recs(3 * T);
+  return GenerateInterpolated(
+      ctx, count, merge, verts, conn, rec_a, rec_b, rec_w, nverts,
+      [&](dax::Id cell, dax::Id visit, dax::exec::InterpolatedCellPoints<dax::CellTagTriangle>& out) {
+        dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cell);
+        dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> vals = ctx.Gather(v, field);
+        worklet(v, out, vals, visit);
+      });
+}
+
+// SliceCount over all cells: the cell's point coordinates against the plane
+// (dax/worklet/Slice.h:28-77).
+void ref_slice_count(const RefGrid* g, const float* origin, const float* normal, int32_t* count) {
+  Ctx ctx(g);
+  dax::worklet::SliceCount worklet(dax::make_Vector3(origin[0], origin[1], origin[2]),
+                                   dax::make_Vector3(normal[0], normal[1], normal[2]));
 #pragma omp parallel for schedule(static) if (g_threads > 1)
-  for (dax::Id t = 0; t < T; ++t) {
-    // ComputeVisitIndex: workId - LowerBounds(cellIds, cellIds[t])
-    const dax::Id visit =
-        t - (std::lower_bound(cellOf.begin(), cellOf.end(), cellOf[t]) - cellOf.begin());
-    dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cellOf[t]);
-    dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> vals = ctx.Gather(v, field);
-    dax::exec::InterpolatedCellPoints<dax::CellTagTriangle> out;
-    worklet(v, out, vals, visit);
-    for (int m = 0; m < 3; ++m) recs[3 * t + m] = out[m];
-  }
-  std::vector<dax::PointAsEdgeInterpolation> weights(recs);
-  if (merge) {
-    sort_any(weights.begin(), weights.end());
-    weights.erase(std::unique(weights.begin(), weights.end()), weights.end());
-#pragma omp parallel for schedule(static) if (g_threads > 1)
-    for (dax::Id i = 0; i < 3 * T; ++i)
-      conn[i] = (int32_t)(std::lower_bound(weights.begin(), weights.end(), recs[i]) -
-                          weights.begin());
-  } else {
-#pragma omp parallel for schedule(static) if (g_threads > 1)
-    for (dax::Id i = 0; i < 3 * T; ++i) conn[i] = (int32_t)i;
-  }
-  const dax::Id V = (dax::Id)weights.size();
-#pragma omp parallel for schedule(static) if (g_threads > 1)
-  for (dax::Id i = 0; i < V; ++i) {
-    const dax::PointAsEdgeInterpolation& r = weights[i];
-    dax::Vector3 p = dax::math::Lerp(ctx.Coord(r.EdgeIdFirst), ctx.Coord(r.EdgeIdSecond),
-                                     r.Weight);
-    verts[3 * i + 0] = p[0];
-    verts[3 * i + 1] = p[1];
-    verts[3 * i + 2] = p[2];
-    if (rec_a) {
-      rec_a[i] = r.EdgeIdFirst;
-      rec_b[i] = r.EdgeIdSecond;
-      rec_w[i] = r.Weight;
-    }
-  }
-  *nverts = V;
-  return T;
+  for (dax::Id c = 0; c < ctx.numCells; ++c) count[c] = (int32_t)worklet(ctx.Coords(ctx.Verts(c)));
+}
+
+// DispatcherGenerateInterpolatedCells<SliceGenerate> (Slice.h:82-168).
+int64_t ref_slice_generate(const RefGrid* g, const float* origin, const float* normal,
+                           const int32_t* count, int merge, float* verts, int32_t* conn,
+                           int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
+  Ctx ctx(g);
+  dax::worklet::SliceGenerate worklet(dax::make_Vector3(origin[0], origin[1], origin[2]),
+                                      dax::make_Vector3(normal[0], normal[1], normal[2]));
+  return GenerateInterpolated(
+      ctx, count, merge, verts, conn, rec_a, rec_b, rec_w, nverts,
+      [&](dax::Id cell, dax::Id visit, dax::exec::InterpolatedCellPoints<dax::CellTagTriangle>& out) {
+        dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cell);
+        worklet(v, out, ctx.Coords(v), visit);
+      });
 }
 
 void ref_interpolate_point_field(const int32_t* rec_a, const int32_t* rec_b, const float* rec_w,

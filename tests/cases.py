@@ -123,3 +123,43 @@ def gradient_cases():
     out.append(("single_cell", (2, 2, 2), (0.5, 0.5, 0.5), (2.0, 3.0, 4.0), (0, 0, 0),
                 np.arange(8, dtype=np.float32) ** 2))
     return out
+
+
+def slice_cases():
+    """(name, dims, origin, spacing, extent_min, plane_origin, plane_normal).
+
+    dax::worklet::Slice compares dot(N, x - O) against dot(N, O)
+    (Slice.h:60-70), so the surface cut is the plane dot(N, x) = 2 dot(N, O);
+    the cases are chosen against that plane."""
+    out = []
+    # UnitTestWorkletSlice.cxx:22-24 -- 8^3 unit grid, O=(3,2,1), N=(1,0,0):
+    # the cut x = 6 runs through grid points; 98 triangles, 64 merged points
+    out.append(("kat8_axis_x", (8, 8, 8), (0, 0, 0), (1, 1, 1), (0, 0, 0), (3, 2, 1), (1, 0, 0)))
+    out.append(("axis_z_between", (12, 10, 9), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                (0, 0, 1.7), (0, 0, 1)))
+    out.append(("oblique_offset", (30, 24, 18), (-1, 0.5, 2), (0.1, 0.13, 0.2), (2, -3, 1),
+                (0.7, 0.9, 3.1), (0.3, -0.5, 0.81)))
+    out.append(("nonunit_normal", (41, 33, 20), (0, 0, 0), (0.05, 0.05, 0.05), (0, 0, 0),
+                (0.4, 0.3, 0.2), (2.5, 1.25, -3.0)))
+    out.append(("misses_grid", (10, 10, 10), (0, 0, 0), (1, 1, 1), (0, 0, 0), (50, 0, 0), (1, 0, 0)))
+    out.append(("single_cell", (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                (0.2, 0.25, 0.3), (1, 1, 1)))
+    out.append(("diagonal_x130", (130, 9, 6), (-3, -1, -1), (0.05, 0.25, 0.4), (0, 0, 0),
+                (0.5, 0.2, 0.1), (1, 1, 1)))
+    out.append(("far_origin", (37, 21, 25), (1000.0, -4.1, 250.0), (0.013, 0.7, 0.05), (-5, 2, 100),
+                (500.1, -1.0, 127.6), (0.6, 0.0, -0.8)))
+    # a normal with zero x component: every row is all inside or all outside
+    out.append(("rows_constant", (45, 12, 11), (0, 0, 0), (0.1, 0.1, 0.1), (0, 0, 0),
+                (0.2, 0.31, 0.4), (0.0, 0.6, 0.8)))
+    # negative spacing along x and a negative normal: the inside part of each
+    # row is a prefix, then a suffix
+    out.append(("negative_spacing", (50, 13, 9), (5, 0, 0), (-0.2, 0.25, 0.5), (1, 0, 0),
+                (1.0, 1.1, 1.2), (0.7, -0.2, 0.3)))
+    out.append(("negative_normal", (50, 13, 9), (0, 0, 0), (0.2, 0.25, 0.5), (0, 0, 0),
+                (1.0, 1.1, 1.2), (-0.7, -0.2, 0.3)))
+    # values that overflow to infinity, and a NaN normal: the per-point path
+    out.append(("overflow_inf", (9, 7, 5), (0, 0, 0), (3e37, 1, 1), (0, 0, 0),
+                (1e38, 0.0, 0.0), (3.0, 0.5, 0.25)))
+    out.append(("nan_normal", (9, 7, 5), (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                (1.0, 2.0, 3.0), (float("nan"), 0.0, 1.0)))
+    return out

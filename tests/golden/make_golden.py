@@ -55,6 +55,14 @@ def main():
         put(meta, arrays, "thr/%s/count" % name, count)
         for k in ("conn", "coords", "field"):
             put(meta, arrays, "thr/%s/%s" % (name, k), out[k])
+    for name, dims, origin, spacing, emin, po, pn in cases.slice_cases():
+        g = oracle.make_grid(dims, origin, spacing, emin)
+        count = R.slice_count(g, po, pn)
+        put(meta, arrays, "slice/%s/count" % name, count)
+        for merge in (0, 1):
+            out = R.slice_generate(g, po, pn, count, bool(merge))
+            for k in ("verts", "conn", "rec_a", "rec_b", "rec_w"):
+                put(meta, arrays, "slice/%s/m%d/%s" % (name, merge, k), out[k])
     for name, dims, origin, spacing, emin, f in cases.gradient_cases():
         g = oracle.make_grid(dims, origin, spacing, emin)
         put(meta, arrays, "grad/%s" % name, R.cell_gradient(g, f))

@@ -63,7 +63,21 @@ def test_gradient_golden(port, case):
     check("grad/%s" % name, port.cell_gradient(oracle.make_grid(dims, origin, spacing, emin), f))
 
 
+@pytest.mark.parametrize("case", cases.slice_cases(), ids=lambda c: c[0])
+def test_slice_golden(port, case):
+    name, dims, origin, spacing, emin, po, pn = case
+    g = oracle.make_grid(dims, origin, spacing, emin)
+    count = port.slice_count(g, po, pn)
+    check("slice/%s/count" % name, count)
+    for merge in (0, 1):
+        out = port.slice_generate(g, po, pn, count, bool(merge))
+        for k in ("verts", "conn", "rec_a", "rec_b", "rec_w"):
+            check("slice/%s/m%d/%s" % (name, merge, k), out[k])
+
+
 def test_known_answers_in_golden():
     assert META["mc/kat26_linear/m1/verts"]["shape"] == [45, 3]
     assert META["mc/kat26_linear/m0/verts"]["shape"] == [183, 3]
     assert META["mc/kat26_linear/m1/conn"]["shape"] == [61, 3]
+    assert META["slice/kat8_axis_x/m0/verts"]["shape"] == [294, 3]
+    assert META["slice/kat8_axis_x/m1/verts"]["shape"] == [64, 3]

@@ -8,6 +8,8 @@ Known answers (DaxToolkit unit tests):
   * UnitTestWorkletThreshold.cxx:40-42, :86-239 -- 26^3, [70, 82]: every kept
     cell's points in range, coordinates of kept cells in input order.
   * UnitTestWorkletCellGradient.cxx:31, :83-117 -- 8^3, x+y+z, gradient (1,1,1).
+  * UnitTestWorkletSlice.cxx:22-24, :84-108 -- 8^3, origin (3,2,1), normal
+    (1,0,0): 2 * 7^2 triangles, 3 points each unmerged, 8^2 points merged.
 """
 import numpy as np
 import pytest
@@ -84,6 +86,36 @@ def test_gradient_known_answer(kind):
     grad = O.cell_gradient(g, cases.linear_field((8, 8, 8)))
     assert grad.shape == (343, 3)
     assert dax_test_equal(grad, np.ones_like(grad))
+
+
+@pytest.mark.parametrize("kind", _kinds())
+def test_slice_known_answer(kind):
+    O = oracle.Oracle(kind)
+    g = _grid((8, 8, 8))
+    count = O.slice_count(g, (3, 2, 1), (1, 0, 0))
+    assert int(count.sum()) == 7 * 7 * 2
+    a = O.slice_generate(g, (3, 2, 1), (1, 0, 0), count, merge=False)
+    b = O.slice_generate(g, (3, 2, 1), (1, 0, 0), count, merge=True)
+    assert a["conn"].shape == (98, 3) and a["verts"].shape == (98 * 3, 3)
+    assert b["conn"].shape == (98, 3) and b["verts"].shape == (64, 3)
+    assert np.all(b["verts"][:, 0] == 6.0)
+
+
+@pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
+@pytest.mark.parametrize("case", cases.slice_cases(), ids=lambda c: c[0])
+def test_slice_port_matches_reference_build(case):
+    name, dims, origin, spacing, emin, po, pn = case
+    P, R = oracle.Oracle("port"), oracle.Oracle("reference")
+    g = _grid(dims, origin, spacing, emin)
+    c1, c2 = P.slice_count(g, po, pn), R.slice_count(g, po, pn)
+    assert np.array_equal(c1, c2)
+    for merge in (False, True):
+        a = P.slice_generate(g, po, pn, c1, merge)
+        b = R.slice_generate(g, po, pn, c2, merge)
+        for key in ("conn", "rec_a", "rec_b"):
+            assert np.array_equal(a[key], b[key]), key
+        for key in ("verts", "rec_w"):
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), key
 
 
 @pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
