@@ -329,6 +329,7 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                     "field_kernel_ms": t_sf, "field_kernel_gbs": 4 * P / (t_sf / 1e3) / 1e9,
                     "field_kernel_frac": 4 * P / (t_sf / 1e3) / 1e9 / peak}
     del sfield, sscr, sverts, sconn
+    out["marching_tetrahedra"] = mt_measurements(peak, stream, dev, reps=max(3, reps // 5))
 
     # --- 64 uneven grids: batched graph replay vs per-grid loop -------------
     gdims = synthetic.batch_grid_dims(64, 32, 192, 777)
@@ -363,6 +364,45 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                       "graph_replay_matches_batch_run": ok}
     out["primitives"] = primitive_measurements(peak, stream, dev)
     return out
+
+
+def mt_measurements(peak, stream, dev, reps=10, n=256):
+    """Marching tetrahedra on an n^3 grid split 5 ways by Tetrahedralize
+    (83 M tetrahedra at n = 256), the 8-blob field, isovalue 0.5: the count
+    pass alone (4 B id x 4 + 1 B case per tetrahedron, field gathers from
+    L2), and count + generate unmerged and merged (sort / unique / bounds;
+    the merged call reads T and V back to the host, as a caller must)."""
+    import torch
+    from daxtoolkit_gb300 import capi, cont, synthetic
+    L = capi.lib()
+    s = ctypes.c_void_p(stream.cuda_stream)
+    ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    grid = cont.UniformGrid((n, n, n), spacing=(1.0 / (n - 1),) * 3)
+    tg = cont.tetrahedralize(grid)
+    conn, pts = tg.GetCellConnections(), tg.GetPointCoordinates()
+    f = synthetic.blob_field((n, n, n), 8, seed=0, device=dev)
+    C, P = conn.shape[0], pts.shape[0]
+    iso = 0.5
+    nb = L.dax_gb300_mt_scratch_bytes(C)
+    scr = torch.empty(nb, dtype=torch.uint8, device=dev)
+
+    def count():
+        capi.call("dax_gb300_mt_count", ptr(conn), C, ptr(f), P, iso, ptr(scr), nb, s)
+
+    t_count = _event_ms(count, reps, stream)
+    t_unmerged = _event_ms(lambda: cont.marching_tetrahedra(tg, f, iso, merge=False, stream=stream),
+                           reps, stream)
+    t_merged = _event_ms(lambda: cont.marching_tetrahedra(tg, f, iso, merge=True, stream=stream),
+                         reps, stream)
+    o = cont.marching_tetrahedra(tg, f, iso, merge=True, stream=stream)
+    cbytes = 17 * C
+    return {"grid": "%d^3 points, Tetrahedralize (5 per voxel)" % n, "tetrahedra": C,
+            "triangles": int(o["conn"].shape[0]), "merged_points": int(o["verts"].shape[0]),
+            "count_ms": t_count, "count_gbs": cbytes / (t_count / 1e3) / 1e9,
+            "count_frac": cbytes / (t_count / 1e3) / 1e9 / peak,
+            "count_formula": "17 B per tetrahedron (ids + case byte)",
+            "unmerged_ms": t_unmerged, "merged_ms": t_merged,
+            "tetrahedra_per_s_merged": C / (t_merged / 1e3)}
 
 
 def primitive_measurements(peak, stream, dev, reps=10):

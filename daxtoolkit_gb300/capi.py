@@ -93,6 +93,15 @@ SIGNATURES = {
     "dax_gb300_slice_count": ([gp, vp, vp, vp, sz, vp], i32),
     "dax_gb300_slice_generate": ([gp, vp, vp, ctypes.c_int, vp, sz, vp, i64, vp, i64, vp, vp, vp,
                                   vp], i32),
+    "dax_gb300_tetrahedralize": ([gp, vp, vp], i32),
+    "dax_gb300_point_coordinates": ([gp, vp, vp], i32),
+    "dax_gb300_mt_classify_count": ([vp, i64, vp, i64, f32, vp, vp], i32),
+    "dax_gb300_mt_scratch_bytes": ([i64], sz),
+    "dax_gb300_mt_count": ([vp, i64, vp, i64, f32, vp, sz, vp], i32),
+    "dax_gb300_mt_merge_scratch_bytes": ([i64, i64], sz),
+    "dax_gb300_mt_merge": ([vp, i64, vp, i64, f32, vp, sz, vp, sz, ctypes.POINTER(i64), vp], i32),
+    "dax_gb300_mt_generate": ([vp, vp, i64, vp, i64, f32, ctypes.c_int, vp, sz, vp, sz, vp, i64,
+                               vp, i64, vp, vp, vp, vp], i32),
     "dax_gb300_scan_scratch_bytes": ([i64], sz),
     "dax_gb300_scan": ([vp, vp, i64, i32, i32, vp, sz, vp, vp], i32),
     "dax_gb300_sort_scratch_bytes": ([i64, i32, i32], sz),

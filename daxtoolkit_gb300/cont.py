@@ -21,6 +21,8 @@ __all__ = [
     "ThresholdCount", "ThresholdTopology", "CellGradient", "DispatcherMapCell",
     "DispatcherGenerateInterpolatedCells", "DispatcherGenerateTopology", "marching_cubes",
     "threshold", "cell_gradient", "Scratch", "SliceCount", "SliceGenerate", "slice", "slice_field",
+    "MarchingTetrahedraCount", "MarchingTetrahedraGenerate", "marching_tetrahedra",
+    "Tetrahedralize", "tetrahedralize",
 ]
 
 
@@ -98,7 +100,9 @@ class UniformGrid:
 
 
 class UnstructuredGrid:
-    """Output grid: explicit points [N,3] and connectivity [cells, verts]."""
+    """Explicit points [N,3] and connectivity [cells, verts]: the output of
+    the generate dispatchers, and (with int32 [C,4] tetrahedra) the input of
+    marching tetrahedra (dax::cont::UnstructuredGrid<CellTagTetrahedron>)."""
 
     def __init__(self, points, connectivity):
         self.points = points
@@ -172,6 +176,20 @@ class SliceCount:
 
 class SliceGenerate(SliceCount):
     """dax/worklet/Slice.h:82-168."""
+
+
+class MarchingTetrahedraCount:
+    """dax/worklet/MarchingTetrahedra.h:49-80."""
+
+    def __init__(self, isovalue):
+        self.IsoValue = float(isovalue)
+
+
+class MarchingTetrahedraGenerate:
+    """dax/worklet/MarchingTetrahedra.h:85-161."""
+
+    def __init__(self, isovalue):
+        self.IsoValue = float(isovalue)
 
 
 class ThresholdCount:
@@ -269,6 +287,81 @@ def slice(grid, origin, normal, merge=True, records=False, scratch=None, stream=
     return out
 
 
+class Tetrahedralize:
+    """dax/worklet/Tetrahedralize.h:55-82: 5 tetrahedra per voxel."""
+
+
+def tetrahedralize(grid, stream=None):
+    """DispatcherGenerateTopology<Tetrahedralize> (count 5 per cell, points
+    not merged) over a UniformGrid: an UnstructuredGrid of tetrahedra whose
+    points are the uniform grid's points, in id order."""
+    g = grid.desc()
+    s = _stream(stream)
+    conn = torch.empty((5 * grid.GetNumberOfCells(), 4), dtype=torch.int32, device="cuda")
+    capi.call("dax_gb300_tetrahedralize", ctypes.byref(g), _ptr(conn), s)
+    pts = torch.empty((grid.GetNumberOfPoints(), 3), dtype=torch.float32, device="cuda")
+    capi.call("dax_gb300_point_coordinates", ctypes.byref(g), _ptr(pts), s)
+    return UnstructuredGrid(pts, conn)
+
+
+def _tet_conn(grid):
+    conn = grid.GetCellConnections()
+    if (not isinstance(conn, torch.Tensor) or not conn.is_cuda or conn.dtype != torch.int32
+            or conn.dim() != 2 or conn.shape[1] != 4 or not conn.is_contiguous()):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "tetrahedra must be a contiguous int32 CUDA tensor [C, 4]")
+    return conn
+
+
+def marching_tetrahedra(grid, field, isovalue, merge=True, records=False, scratch=None,
+                        stream=None):
+    """MarchingTetrahedraCount + Generate on an UnstructuredGrid of
+    tetrahedra: the same dict as marching_cubes."""
+    _require_field(field, grid)
+    conn = _tet_conn(grid)
+    pts = grid.GetPointCoordinates()
+    if (not isinstance(pts, torch.Tensor) or not (pts.is_cuda or pts.is_pinned())
+            or pts.dtype != torch.float32 or tuple(pts.shape) != (grid.GetNumberOfPoints(), 3)
+            or not pts.is_contiguous()):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "points must be a contiguous float32 tensor [P, 3]")
+    L = capi.lib()
+    s = _stream(stream)
+    C, P = conn.shape[0], pts.shape[0]
+    iso = float(isovalue)
+    nbytes = L.dax_gb300_mt_scratch_bytes(C)
+    buf = (scratch or _scratch_for("mt")).get(nbytes)
+    capi.call("dax_gb300_mt_count", _ptr(conn), C, _ptr(field), P, iso, _ptr(buf), buf.numel(), s)
+    T = ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", _ptr(buf), ctypes.byref(T), None, s)
+    T = T.value
+    mbuf, mbytes = None, 0
+    if merge:
+        mbytes = L.dax_gb300_mt_merge_scratch_bytes(T, P)
+        mbuf = _scratch_for("mt_merge").get(mbytes)
+        V = ctypes.c_int64(0)
+        capi.call("dax_gb300_mt_merge", _ptr(conn), C, _ptr(field), P, iso, _ptr(buf), buf.numel(),
+                  _ptr(mbuf), mbuf.numel(), ctypes.byref(V), s)
+        V = V.value
+    else:
+        V = 3 * T
+    dev = conn.device
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    tconn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+    ra = rb = rw = None
+    if records:
+        ra = torch.empty(V, dtype=torch.int32, device=dev)
+        rb = torch.empty(V, dtype=torch.int32, device=dev)
+        rw = torch.empty(V, dtype=torch.float32, device=dev)
+    capi.call("dax_gb300_mt_generate", _ptr(pts), _ptr(conn), C, _ptr(field), P, iso,
+              int(bool(merge)), _ptr(buf), buf.numel(), _ptr(mbuf), mbuf.numel() if merge else 0,
+              _ptr(verts), V, _ptr(tconn), T, _ptr(ra), _ptr(rb), _ptr(rw), s)
+    out = dict(verts=verts, conn=tconn)
+    if records:
+        out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
+    return out
+
+
 def interpolate_point_field(rec_first, rec_second, rec_weight, field, stream=None):
     out = torch.empty(rec_first.numel(), dtype=torch.float32, device=_out_device(field))
     capi.call("dax_gb300_interpolate_point_field", _ptr(rec_first), _ptr(rec_second),
@@ -318,6 +411,12 @@ class DispatcherMapCell:
         w = self.worklet
         if not isinstance(w, SliceCount):  # a slice's point field is the implicit coordinates
             _require_field(field, grid)
+        if isinstance(w, MarchingTetrahedraCount):
+            conn = _tet_conn(grid)
+            count = torch.empty(conn.shape[0], dtype=torch.int32, device=_out_device(field))
+            capi.call("dax_gb300_mt_classify_count", _ptr(conn), conn.shape[0], _ptr(field),
+                      grid.GetNumberOfPoints(), w.IsoValue, _ptr(count), _stream(stream))
+            return count
         g = grid.desc()
         C = grid.GetNumberOfCells()
         if isinstance(w, MarchingCubesCount):
@@ -382,6 +481,9 @@ class DispatcherGenerateInterpolatedCells:
         if isinstance(w, SliceGenerate):
             out = slice(grid, w.Origin, w.Normal, merge=self.RemoveDuplicatePoints, records=True,
                         stream=stream)
+        elif isinstance(w, MarchingTetrahedraGenerate):
+            out = marching_tetrahedra(grid, field, w.IsoValue, merge=self.RemoveDuplicatePoints,
+                                      records=True, stream=stream)
         else:
             out = marching_cubes(grid, field, w.IsoValue, merge=self.RemoveDuplicatePoints,
                                  records=True, stream=stream)

@@ -185,6 +185,11 @@ int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
     return fail(DAX_GB300_ERROR_TIMEOUT, "scan look-back wait expired on the device");
   if (h.error & daxgb::kErrOverflow)
     return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31-1 triangles or vertices");
+  if (h.error & daxgb::kErrState)
+    return fail(DAX_GB300_ERROR_BAD_VALUE,
+                "the merge scratch does not hold dax_gb300_mt_merge's result for this count pass");
+  if (h.error & daxgb::kErrBadIndex)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "a cell lists a point id outside [0, num_points)");
   if (h.error & daxgb::kErrCapacity)
     return fail(DAX_GB300_ERROR_CAPACITY, "output capacity smaller than the result; nothing written");
   return DAX_GB300_SUCCESS;
@@ -415,6 +420,187 @@ int dax_gb300_slice_generate(const dax_gb300_uniform_grid* grid, const float* or
                         d_rec_first, d_rec_second, d_rec_weight, num_sms(),
                         static_cast<cudaStream_t>(stream));
   return check_launch("slice generate kernel");
+}
+
+int dax_gb300_tetrahedralize(const dax_gb300_uniform_grid* grid, int32_t* d_conn, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!has_cells(g)) return DAX_GB300_SUCCESS;
+  if (!d_conn) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL connectivity");
+  const long long C = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1);
+  if (5 * C > 2147483647ll)
+    return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31 - 1 tetrahedra (dax::Id is int32)");
+  daxgb::launch_tetrahedralize(g, d_conn, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("tetrahedralize kernel");
+}
+
+int dax_gb300_point_coordinates(const dax_gb300_uniform_grid* grid, float* d_points,
+                                void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!d_points) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL points");
+  daxgb::launch_point_coordinates(g, d_points, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("point coordinates kernel");
+}
+
+size_t dax_gb300_mt_scratch_bytes(int64_t num_cells) {
+  return num_cells < 0 ? 0 : daxgb::mt_layout(num_cells).total;
+}
+
+namespace {
+
+int mt_args(const int32_t* conn, int64_t C, const float*& f, int64_t P, const void* scratch,
+            size_t bytes) {
+  if (C < 0 || P < 0 || C > 2147483647ll || P > 2147483647ll)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "cell and point counts must be in [0, 2^31 - 1]");
+  if (C > 0 && (!conn || !f || !scratch))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL connectivity, field or scratch");
+  if (bytes < daxgb::mt_layout(C).total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mt_scratch_bytes()");
+  if (reinterpret_cast<uintptr_t>(scratch) & 15)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
+  return device_view(f, "field");
+}
+
+// Merge scratch: [header: V][keys: 3T][unique keys: 3T][primitive scratch].
+struct MtMerge {
+  size_t hdr, keys, uniq, prim, prim_bytes, total;
+  int type, kb;
+};
+MtMerge mt_merge_layout(int64_t T, int64_t P) {
+  MtMerge M;
+  const int bits = daxgb::mt_key_bits(P);
+  M.type = 2 * bits > 32 ? DAX_GB300_TYPE_U64 : DAX_GB300_TYPE_U32;
+  M.kb = 2 * bits > 32 ? 8 : 4;
+  const int64_t n = T > 0 ? 3 * T : 1;
+  const size_t sb = dax_gb300_sort_scratch_bytes(n, M.type, 0);
+  const size_t cb = dax_gb300_compact_scratch_bytes(n, M.kb);
+  M.prim_bytes = sb > cb ? sb : cb;
+  M.hdr = 0;
+  M.keys = 256;
+  M.uniq = align256(M.keys + (size_t)n * M.kb);
+  M.prim = align256(M.uniq + (size_t)n * M.kb);
+  M.total = align256(M.prim + M.prim_bytes);
+  return M;
+}
+
+}  // namespace
+
+int dax_gb300_mt_count(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                       int64_t num_points, float isovalue, void* d_scratch, size_t scratch_bytes,
+                       void* stream) {
+  int st = mt_args(d_conn, num_cells, d_field, num_points, d_scratch, scratch_bytes);
+  if (st) return st;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (num_cells == 0) {
+    if (!d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL scratch");
+    cudaError_t e = cudaMemsetAsync(d_scratch, 0, sizeof(Info), s);
+    return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing scratch");
+  }
+  daxgb::launch_mt_count(d_conn, num_cells, d_field, num_points, isovalue,
+                         static_cast<char*>(d_scratch), num_sms(), s);
+  return check_launch("marching tetrahedra count kernels");
+}
+
+int dax_gb300_mt_classify_count(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                                int64_t num_points, float isovalue, int32_t* d_count,
+                                void* stream) {
+  if (num_cells == 0) return DAX_GB300_SUCCESS;
+  if (num_cells < 0 || num_points < 0 || num_cells > 2147483647ll || num_points > 2147483647ll)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "cell and point counts must be in [0, 2^31 - 1]");
+  if (!d_conn || !d_field || !d_count)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL connectivity, field or count");
+  int st = device_view(d_field, "field");
+  if (st) return st;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* err = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&err), sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_fail(e, "allocating the error word");
+  daxgb::launch_mt_cell_count(d_conn, num_cells, d_field, num_points, isovalue, d_count, err,
+                              num_sms(), s);
+  int h = 0;
+  e = cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaFreeAsync(err, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "marching tetrahedra count kernel");
+  if (h & daxgb::kErrBadIndex)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "a cell lists a point id outside [0, num_points)");
+  return DAX_GB300_SUCCESS;
+}
+
+size_t dax_gb300_mt_merge_scratch_bytes(int64_t num_triangles, int64_t num_points) {
+  if (num_triangles < 0 || num_points < 0) return 0;
+  return mt_merge_layout(num_triangles, num_points).total;
+}
+
+int dax_gb300_mt_merge(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                       int64_t num_points, float isovalue, void* d_scratch, size_t scratch_bytes,
+                       void* d_merge, size_t merge_bytes, int64_t* h_num_merged, void* stream) {
+  int st = mt_args(d_conn, num_cells, d_field, num_points, d_scratch, scratch_bytes);
+  if (st) return st;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int64_t T = 0;
+  if (num_cells > 0 && (st = read_totals(d_scratch, &T, nullptr, s))) return st;
+  const MtMerge M = mt_merge_layout(T, num_points);
+  if (!d_merge || merge_bytes < M.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE,
+                "merge scratch smaller than dax_gb300_mt_merge_scratch_bytes()");
+  char* m = static_cast<char*>(d_merge);
+  int64_t V = 0;
+  if (T > 0) {
+    daxgb::launch_mt_emit_keys(d_conn, num_cells, d_field, num_points, isovalue,
+                               static_cast<char*>(d_scratch), m + M.keys, num_sms(), s);
+    if ((st = check_launch("marching tetrahedra key kernel"))) return st;
+    cudaError_t e = cudaMemcpyAsync(m + M.uniq, m + M.keys, (size_t)(3 * T) * M.kb,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "copying merge keys");
+    daxgb::sort_unsigned_bits(m + M.uniq, 3 * T, M.kb == 8, 2 * daxgb::mt_key_bits(num_points),
+                              m + M.prim, s);
+    if ((st = check_launch("merge key sort"))) return st;
+    if ((st = dax_gb300_unique(m + M.uniq, 3 * T, M.type, m + M.prim, M.prim_bytes, &V, stream)))
+      return st;
+  }
+  daxgb::launch_mt_set_merged(m + M.hdr, T, V, M.keys, M.uniq, s);
+  if (h_num_merged) *h_num_merged = V;
+  return check_launch("marching tetrahedra merge header");
+}
+
+int dax_gb300_mt_generate(const float* d_points, const int32_t* d_conn, int64_t num_cells,
+                          const float* d_field, int64_t num_points, float isovalue, int merge,
+                          void* d_scratch, size_t scratch_bytes, void* d_merge,
+                          size_t merge_bytes, float* d_verts, int64_t vert_capacity,
+                          int32_t* d_tri_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                          int32_t* d_rec_second, float* d_rec_weight, void* stream) {
+  int st = mt_args(d_conn, num_cells, d_field, num_points, d_scratch, scratch_bytes);
+  if (st) return st;
+  if (num_cells == 0) return DAX_GB300_SUCCESS;
+  if (!d_points) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL points");
+  if ((st = device_view(d_points, "points"))) return st;
+  if ((!d_verts && vert_capacity > 0) || (!d_tri_conn && tri_capacity > 0) || vert_capacity < 0 ||
+      tri_capacity < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
+  if ((d_rec_first || d_rec_second || d_rec_weight) &&
+      !(d_rec_first && d_rec_second && d_rec_weight))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "give all three record arrays or none");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* sc = static_cast<char*>(d_scratch);
+  if (!merge) {
+    daxgb::launch_mt_emit_direct(d_points, d_conn, num_cells, d_field, num_points, isovalue, sc,
+                                 d_verts, vert_capacity, d_tri_conn, tri_capacity, d_rec_first,
+                                 d_rec_second, d_rec_weight, num_sms(), s);
+    return check_launch("marching tetrahedra emit kernel");
+  }
+  // the keys, their count and their offsets come from dax_gb300_mt_merge on
+  // this scratch (its header); the kernels check the capacities on the device
+  if (!d_merge || merge_bytes < 256)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "merge needs the dax_gb300_mt_merge scratch");
+  daxgb::launch_mt_merged(d_points, num_cells, d_field, num_points, isovalue, sc, d_merge,
+                          merge_bytes, d_verts, vert_capacity, d_tri_conn, tri_capacity,
+                          d_rec_first, d_rec_second, d_rec_weight, num_sms(), s);
+  return check_launch("marching tetrahedra merged kernels");
 }
 
 int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t* d_rec_second,

@@ -128,6 +128,8 @@ struct Info {
 constexpr int kErrTimeout = 1;     // a look-back wait gave up
 constexpr int kErrCapacity = 2;    // output buffer too small
 constexpr int kErrOverflow = 4;    // more than 2^31 - 1 triangles or vertices
+constexpr int kErrBadIndex = 8;    // a cell lists a point id outside [0, P)
+constexpr int kErrState = 16;      // a merge scratch that no merge pass of this count wrote
 
 // Coordinate of grid index i along one axis: origin + spacing * (i + min),
 // computed in float with no fused multiply-add, as the reference's implicit

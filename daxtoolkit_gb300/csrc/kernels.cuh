@@ -131,4 +131,51 @@ void launch_slice_bits(const Grid& g, float3 o, float3 n, float iso, uint32_t* b
 void launch_slice_field(const Grid& g, float3 o, float3 n, float* out, int num_sms,
                         cudaStream_t s);
 
+// Ascending radix sort of unsigned keys (32- or 64-bit) whose set bits all lie
+// below `bits`: only those digits are sorted.  scratch as
+// dax_gb300_sort_scratch_bytes(n, U32 / U64, 0) (primitives.cu).
+void sort_unsigned_bits(void* keys, long long n, bool wide, int bits, void* scratch,
+                        cudaStream_t s);
+
+// Tetrahedralize: int32[5 * cells][4] (mt.cu); the uniform grid's point
+// coordinates as float[P][3].
+void launch_tetrahedralize(const Grid& g, int32_t* out, int num_sms, cudaStream_t s);
+void launch_point_coordinates(const Grid& g, float* out, int num_sms, cudaStream_t s);
+
+// Marching tetrahedra on an unstructured tetrahedral grid (mt.cu).
+// Count scratch: [Info][tile totals u32][tile offsets u64][chunk totals u32]
+// [case byte per cell].  A tile is kMtTile cells, a chunk kMtChunk cells (one
+// warp of the count and emit passes, 16 cells per lane in the emit).
+constexpr int kMtThreads = 256;
+constexpr int kMtPerLane = 16;
+constexpr int kMtChunk = 32 * kMtPerLane;                 // cells per chunk
+constexpr int kMtTile = (kMtThreads / 32) * kMtChunk;     // cells per tile
+struct MtLayout {
+  int tiles;
+  size_t info, tile_tot, tile_off, chunk_tot, cases, total;
+};
+MtLayout mt_layout(long long C);
+// Bits of the B half of a merge key (A << bits) | B: P <= 2^bits.  Keys are
+// 32-bit when 2 * bits <= 32, else 64-bit.
+int mt_key_bits(long long P);
+void launch_mt_count(const int32_t* conn, long long C, const float* f, long long P, float iso,
+                     char* scratch, int num_sms, cudaStream_t s);
+void launch_mt_cell_count(const int32_t* conn, long long C, const float* f, long long P,
+                          float iso, int32_t* count, int* err, int num_sms, cudaStream_t s);
+void launch_mt_emit_direct(const float* pts, const int32_t* conn, long long C, const float* f,
+                           long long P, float iso, char* scratch, float* verts, long long vcap,
+                           int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb, float* rw,
+                           int num_sms, cudaStream_t s);
+void launch_mt_emit_keys(const int32_t* conn, long long C, const float* f, long long P, float iso,
+                         char* scratch, void* keys, int num_sms, cudaStream_t s);
+// The merge scratch begins with a header (a marker, the unique-key count,
+// the byte offsets of the record keys and of the unique keys, the triangle
+// count it was built for) that the merged kernels check and read.
+void launch_mt_set_merged(void* merge, long long T, long long V, size_t keys_off,
+                          size_t uniq_off, cudaStream_t s);
+void launch_mt_merged(const float* pts, long long C, const float* f, long long P, float iso,
+                      char* scratch, const void* merge, size_t merge_bytes, float* verts,
+                      long long vcap, int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb,
+                      float* rw, int num_sms, cudaStream_t s);
+
 }  // namespace daxgb

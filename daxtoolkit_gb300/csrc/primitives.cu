@@ -498,9 +498,13 @@ SortLayout sort_layout(long long n, int key_bytes, int value_bytes) {
   return L;
 }
 
+// passes: 8-bit digits to sort, least significant first (an even count, so
+// the result ends in keys/vals); plain = the keys are unsigned, ascending and
+// need no order mapping.
 template <typename U>
 void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool desc,
-                char* scratch, int num_sms, cudaStream_t s) {
+                char* scratch, int num_sms, cudaStream_t s, int passes = (int)sizeof(U),
+                bool plain = false) {
   const SortLayout L = sort_layout(n, (int)sizeof(U), 4 * vwords);
   U* ktmp = reinterpret_cast<U*>(scratch + L.ktmp);
   uint32_t* vtmp = reinterpret_cast<uint32_t*>(scratch + L.vtmp);
@@ -508,7 +512,7 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
   void* sums = scratch + L.sums;
   const int tiles = ptiles(n);
   const int ob = resident((const void*)k_order_keys<U>, 256, num_sms, (n + 255) / 256);
-  k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 0);
+  if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 0);
   const int bh = resident((const void*)k_digit_hist<U>, kPT, num_sms, tiles);
   const size_t sm = scatter_smem<U>();
   cudaFuncSetAttribute(k_digit_scatter<U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -517,7 +521,6 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
           cudaSuccess || per < 1)
     per = 1;
   const int bs = (int)(tiles < (long long)num_sms * per ? tiles : (long long)num_sms * per);
-  const int passes = (int)sizeof(U);  // one 8-bit digit per byte: an even count
   for (int p = 0; p < passes; ++p) {
     const U* ksrc = (p & 1) ? ktmp : keys;
     U* kdst = (p & 1) ? keys : ktmp;
@@ -527,7 +530,7 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
     scan_t<uint32_t>(hist, hist, 256ll * tiles, true, sums, nullptr, num_sms, s);
     k_digit_scatter<U><<<bs, kPT, sm, s>>>(ksrc, kdst, vsrc, vdst, vwords, n, 8 * p, hist, tiles);
   }
-  k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 1);
+  if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 1);
 }
 
 // ---- bounds -------------------------------------------------------------------
@@ -604,6 +607,26 @@ size_t scan_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
 size_t keep_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
 
 }  // namespace
+}  // namespace daxgb
+
+namespace daxgb {
+
+void sort_unsigned_bits(void* keys, long long n, bool wide, int bits, void* scratch,
+                        cudaStream_t s) {
+  if (n < 2) return;
+  int passes = (bits + 7) / 8;
+  passes += passes & 1;
+  const int kind = type_kind(wide ? DAX_GB300_TYPE_U64 : DAX_GB300_TYPE_U32);
+  if (wide)
+    radix_sort<unsigned long long>(static_cast<unsigned long long*>(keys), nullptr, 0, n, kind,
+                                   false, static_cast<char*>(scratch), prim_sms(), s,
+                                   passes < 8 ? passes : 8, true);
+  else
+    radix_sort<uint32_t>(static_cast<uint32_t*>(keys), nullptr, 0, n, kind, false,
+                         static_cast<char*>(scratch), prim_sms(), s, passes < 4 ? passes : 4,
+                         true);
+}
+
 }  // namespace daxgb
 
 using daxgb::align256;

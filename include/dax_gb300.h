@@ -198,6 +198,65 @@ int dax_gb300_slice_field(const dax_gb300_uniform_grid* grid, const float* origi
                           const float* normal, float* d_field, float* h_isovalue, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Marching tetrahedra (dax/worklet/MarchingTetrahedra.h)                    */
+/* ------------------------------------------------------------------------ */
+
+/* DispatcherGenerateTopology<Tetrahedralize> over a uniform grid with a count
+ * of 5 per cell and no point merging (dax/worklet/Tetrahedralize.h:36-82):
+ * d_conn int32[5 * cells][4], output cell o from cell o / 5, split pattern by
+ * the parity of the cell id.  Point ids index the grid's points, whose
+ * coordinates dax_gb300_point_coordinates writes as float[P][3]
+ * (UniformGrid::ComputePointCoordinates).  Asynchronous. */
+int dax_gb300_tetrahedralize(const dax_gb300_uniform_grid* grid, int32_t* d_conn, void* stream);
+int dax_gb300_point_coordinates(const dax_gb300_uniform_grid* grid, float* d_points,
+                                void* stream);
+
+/* An unstructured tetrahedral grid, dax::cont::UnstructuredGrid<
+ * CellTagTetrahedron>: d_conn int32[num_cells][4] point ids, d_points
+ * float[num_points][3], d_field float[num_points] (device memory; the field
+ * and points may also be page-locked host memory).  Results are the
+ * reference's MarchingTetrahedraCount + DispatcherGenerateInterpolatedCells
+ * <MarchingTetrahedraGenerate> (MarchingTetrahedra.h:49-161,
+ * DispatcherGenerateInterpolatedCells.h:158-301) bit for bit: triangles in
+ * cell order then TriTable order, edges lower point id first, merged points
+ * in ascending (first, second) order.  A cell with a point id outside
+ * [0, num_points) yields DAX_GB300_ERROR_BAD_VALUE from the totals; no such
+ * id is dereferenced.
+ *
+ * DispatcherMapCell<MarchingTetrahedraCount>: int32 count per cell.
+ * Blocking (reads the error word back). */
+int dax_gb300_mt_classify_count(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                                int64_t num_points, float isovalue, int32_t* d_count,
+                                void* stream);
+
+/* Count pass (asynchronous); dax_gb300_mc_totals(d_scratch, &T, NULL, s)
+ * then returns the triangle count. */
+size_t dax_gb300_mt_scratch_bytes(int64_t num_cells);
+int dax_gb300_mt_count(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                       int64_t num_points, float isovalue, void* d_scratch, size_t scratch_bytes,
+                       void* stream);
+
+/* Merging (RemoveDuplicatePoints): after the count pass, Sort + Unique of the
+ * interpolation records in d_merge (dax_gb300_mt_merge_scratch_bytes(T, P)
+ * bytes).  Blocking; *h_num_merged = the number of merged points. */
+size_t dax_gb300_mt_merge_scratch_bytes(int64_t num_triangles, int64_t num_points);
+int dax_gb300_mt_merge(const int32_t* d_conn, int64_t num_cells, const float* d_field,
+                       int64_t num_points, float isovalue, void* d_scratch, size_t scratch_bytes,
+                       void* d_merge, size_t merge_bytes, int64_t* h_num_merged, void* stream);
+
+/* Generate pass (asynchronous).  merge = 0: 3T points, connectivity 0..3T-1,
+ * d_merge unused.  merge = 1: the points of dax_gb300_mt_merge on the same
+ * scratch and d_merge.  Records (first, second, weight) per output point are
+ * optional (all three or none).  If a capacity is too small nothing is
+ * written and dax_gb300_mc_totals then returns DAX_GB300_ERROR_CAPACITY. */
+int dax_gb300_mt_generate(const float* d_points, const int32_t* d_conn, int64_t num_cells,
+                          const float* d_field, int64_t num_points, float isovalue, int merge,
+                          void* d_scratch, size_t scratch_bytes, void* d_merge,
+                          size_t merge_bytes, float* d_verts, int64_t vert_capacity,
+                          int32_t* d_tri_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                          int32_t* d_rec_second, float* d_rec_weight, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batched marching cubes: many grids, one launch per pass                   */
 /* ------------------------------------------------------------------------ */
 

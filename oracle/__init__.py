@@ -76,6 +76,14 @@ class Oracle:
         self._slice_gen.argtypes = [gp, vp, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp,
                                     ctypes.POINTER(i64)]
         self._slice_gen.restype = i64
+        self._tetra = getattr(L, prefix + "tetrahedralize")
+        self._tetra.argtypes = [gp, vp]
+        self._mt_count = getattr(L, prefix + "mt_count")
+        self._mt_count.argtypes = [vp, i64, vp, ctypes.c_float, vp]
+        self._mt_gen = getattr(L, prefix + "mt_generate")
+        self._mt_gen.argtypes = [vp, vp, i64, vp, ctypes.c_float, vp, ctypes.c_int, vp, vp, vp, vp,
+                                 vp, ctypes.POINTER(i64)]
+        self._mt_gen.restype = i64
         if kind == "reference":
             L.ref_set_threads.argtypes = [ctypes.c_int]
             L.ref_max_threads.restype = ctypes.c_int
@@ -177,6 +185,42 @@ class Oracle:
         V = nv.value
         return dict(verts=verts[:V], conn=conn[:3 * T].reshape(T, 3), rec_a=ra[:V], rec_b=rb[:V],
                     rec_w=rw[:V])
+
+    def tetrahedralize(self, g):
+        """Tetrahedralize over the grid: int32 [5 * cells, 4]."""
+        conn = np.zeros((5 * self._cells(g), 4), np.int32)
+        self._tetra(ctypes.byref(g), _ptr(conn))
+        return conn
+
+    def mt_count(self, conn, field, iso):
+        """MarchingTetrahedraCount per tetrahedron; conn is int32 [C, 4]."""
+        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 4)
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        count = np.zeros(conn.shape[0], np.int32)
+        self._mt_count(_ptr(conn), conn.shape[0], _ptr(field), float(iso), _ptr(count))
+        return count
+
+    def mt_generate(self, points, conn, field, iso, count, merge=True):
+        """Returns dict(verts, conn, rec_a, rec_b, rec_w) as mc_generate."""
+        points = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 4)
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        count = np.ascontiguousarray(count, dtype=np.int32)
+        T = int(count.astype(np.int64).sum())
+        cap = max(3 * T, 1)
+        verts = np.zeros((cap, 3), np.float32)
+        tconn = np.zeros(cap, np.int32)
+        ra = np.zeros(cap, np.int32)
+        rb = np.zeros(cap, np.int32)
+        rw = np.zeros(cap, np.float32)
+        nv = ctypes.c_int64(0)
+        t = self._mt_gen(_ptr(points), _ptr(conn), conn.shape[0], _ptr(field), float(iso),
+                         _ptr(count), int(bool(merge)), _ptr(verts), _ptr(tconn), _ptr(ra),
+                         _ptr(rb), _ptr(rw), ctypes.byref(nv))
+        assert t == T
+        V = nv.value
+        return dict(verts=verts[:V], conn=tconn[:3 * T].reshape(T, 3), rec_a=ra[:V],
+                    rec_b=rb[:V], rec_w=rw[:V])
 
     def cell_gradient(self, g, field):
         field = np.ascontiguousarray(field, dtype=np.float32).ravel()

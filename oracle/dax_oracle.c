@@ -407,3 +407,140 @@ int64_t orc_slice_generate(const orc_grid* g, const float* origin, const float* 
   free(f);
   return T;
 }
+
+/* ---- Marching tetrahedra on an unstructured tetrahedral grid ------------- */
+
+#include "../daxtoolkit_gb300/csrc/mt_tables.h"
+
+static const uint32_t kMtCase[16] = DAX_GB300_MT_CASE_WORDS;
+/* NumFaces / TriTable: dax/worklet/internal/MarchingTetrahedraTable.h:28-53 */
+static int mt_num_faces(int c) { return (int)(kMtCase[c] >> 28); }
+static int mt_tri_edge(int c, int n) { return (int)((kMtCase[c] >> (4 * n)) & 0xF); }
+/* cellVertEdges: dax/worklet/MarchingTetrahedra.h:126-129 */
+static const unsigned char kTetVertEdges[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 1}, {3, 2}};
+
+/* GetTetrahedronClassification: dax/worklet/MarchingTetrahedra.h:36-46 */
+static int mt_classify(const float val[4], float iso) {
+  int c = 0;
+  for (int n = 0; n < 4; ++n) c |= (val[n] > iso) << n;
+  return c;
+}
+
+/* DispatcherMapCell<MarchingTetrahedraCount> (MarchingTetrahedra.h:49-80):
+ * conn holds 4 point ids per tetrahedron. */
+void orc_mt_count(const int32_t* conn, int64_t C, const float* field, float iso, int32_t* count) {
+  for (int64_t c = 0; c < C; ++c) {
+    float val[4];
+    for (int n = 0; n < 4; ++n) val[n] = field[conn[4 * c + n]];
+    count[c] = mt_num_faces(mt_classify(val, iso));
+  }
+}
+
+/* Lerp of two explicit point coordinates (points [P][3]). */
+static void lerp_points(const float* pts, const orc_edge_rec* r, float out[3]) {
+  const float* ca = pts + 3 * (int64_t)r->a;
+  const float* cb = pts + 3 * (int64_t)r->b;
+  for (int a = 0; a < 3; ++a) out[a] = ca[a] + r->w * (cb[a] - ca[a]);
+}
+
+/*
+ * DispatcherGenerateInterpolatedCells<MarchingTetrahedraGenerate> with the
+ * Serial adapter: the same scan / upper bounds / visit index / sort-unique-
+ * lower-bounds steps as orc_mc_generate, with MarchingTetrahedraGenerate::
+ * BuildTriangle (MarchingTetrahedra.h:117-161) per output triangle and the
+ * grid's explicit point coordinates.  Returns T; *nverts = V.
+ */
+int64_t orc_mt_generate(const float* pts, const int32_t* conn, int64_t C, const float* field,
+                        float iso, const int32_t* count, int merge, float* verts, int32_t* tconn,
+                        int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
+  *nverts = 0;
+  if (C == 0) return 0;
+  int64_t* scan = (int64_t*)malloc(sizeof(int64_t) * C);
+  int64_t acc = 0;
+  for (int64_t c = 0; c < C; ++c) { acc += count[c]; scan[c] = acc; }
+  const int64_t T = acc;
+  if (T == 0) { free(scan); return 0; }
+  int64_t* cell_of = (int64_t*)malloc(sizeof(int64_t) * T);
+  for (int64_t t = 0; t < T; ++t) cell_of[t] = upper_bound_i64(scan, C, t);
+  free(scan);
+  orc_edge_rec* recs = (orc_edge_rec*)malloc(sizeof(orc_edge_rec) * 3 * T);
+  for (int64_t t = 0; t < T; ++t) {
+    const int64_t visit = t - lower_bound_i64(cell_of, T, cell_of[t]);
+    const int32_t* v = conn + 4 * cell_of[t];
+    float val[4];
+    for (int n = 0; n < 4; ++n) val[n] = field[v[n]];
+    const int cs = mt_classify(val, iso);
+    for (int m = 0; m < 3; ++m) {
+      const int e = mt_tri_edge(cs, (int)(visit * 3 + m));
+      int va, vb;
+      if (v[kTetVertEdges[e][0]] < v[kTetVertEdges[e][1]]) {
+        va = kTetVertEdges[e][0];
+        vb = kTetVertEdges[e][1];
+      } else {
+        va = kTetVertEdges[e][1];
+        vb = kTetVertEdges[e][0];
+      }
+      recs[3 * t + m].a = v[va];
+      recs[3 * t + m].b = v[vb];
+      recs[3 * t + m].w = (iso - val[va]) / (val[vb] - val[va]);
+    }
+  }
+  int64_t V;
+  if (merge) {
+    orc_edge_rec* uniq = (orc_edge_rec*)malloc(sizeof(orc_edge_rec) * 3 * T);
+    memcpy(uniq, recs, sizeof(orc_edge_rec) * 3 * T);
+    qsort(uniq, (size_t)(3 * T), sizeof(orc_edge_rec), rec_cmp);
+    V = 0;
+    for (int64_t i = 0; i < 3 * T; ++i)
+      if (V == 0 || rec_cmp(&uniq[V - 1], &uniq[i]) != 0) uniq[V++] = uniq[i];
+    for (int64_t i = 0; i < 3 * T; ++i) {
+      int64_t lo = 0, hi = V;
+      while (lo < hi) {
+        int64_t mid = lo + (hi - lo) / 2;
+        if (rec_less(&uniq[mid], &recs[i])) lo = mid + 1; else hi = mid;
+      }
+      tconn[i] = (int32_t)lo;
+    }
+    for (int64_t i = 0; i < V; ++i) {
+      lerp_points(pts, &uniq[i], verts + 3 * i);
+      if (rec_a) { rec_a[i] = uniq[i].a; rec_b[i] = uniq[i].b; rec_w[i] = uniq[i].w; }
+    }
+    free(uniq);
+  } else {
+    V = 3 * T;
+    for (int64_t i = 0; i < V; ++i) {
+      lerp_points(pts, &recs[i], verts + 3 * i);
+      tconn[i] = (int32_t)i;
+      if (rec_a) { rec_a[i] = recs[i].a; rec_b[i] = recs[i].b; rec_w[i] = recs[i].w; }
+    }
+  }
+  free(recs);
+  free(cell_of);
+  *nverts = V;
+  return T;
+}
+
+/* ---- Tetrahedralize: 5 tetrahedra per voxel -------------------------------- */
+
+/* PossibleTetraSplitCases (dax/worklet/Tetrahedralize.h:36-48): rows 0-4 for
+ * even cell ids, 5-9 for odd, voxel corners in TopologyUniform order. */
+static const unsigned char kTetSplit[10][4] = {
+    {2, 1, 5, 0}, {0, 2, 3, 7}, {2, 5, 6, 7}, {0, 7, 4, 5}, {0, 2, 7, 5},
+    {1, 3, 6, 2}, {0, 1, 3, 4}, {1, 4, 5, 6}, {3, 6, 7, 4}, {1, 4, 6, 3}};
+
+/* DispatcherGenerateTopology<Tetrahedralize> with a constant count of 5 and
+ * no point merging (UnitTestWorkletTetrahedralize.cxx:73-90): output cell o
+ * comes from input cell o / 5 with visit index o % 5 (Tetrahedralize.h:71-80).
+ * conn gets [5C][4] point ids. */
+void orc_tetrahedralize(const orc_grid* g, int32_t* conn) {
+  int64_t d[3];
+  dims_of(g, d);
+  const int64_t C = num_cells(d);
+  for (int64_t o = 0; o < 5 * C; ++o) {
+    const int64_t cell = o / 5, visit = o % 5;
+    int64_t v[8];
+    cell_vertices(d, cell, v);
+    const unsigned char* row = kTetSplit[visit + 5 * (cell % 2)];
+    for (int n = 0; n < 4; ++n) conn[4 * o + n] = (int32_t)v[row[n]];
+  }
+}

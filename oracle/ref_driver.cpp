@@ -1,6 +1,7 @@
 // Reference-side CPU driver: runs the DaxToolkit's OWN worklet functors
 // (MarchingCubesCount, MarchingCubesGenerate, SliceCount, SliceGenerate,
-// ThresholdCount, ThresholdTopology, CellGradient), its TopologyUniform connectivity and
+// MarchingTetrahedraCount, MarchingTetrahedraGenerate, Tetrahedralize, ThresholdCount,
+// ThresholdTopology, CellGradient), its TopologyUniform connectivity and
 // point coordinates, its PointAsEdgeInterpolation ordering and dax::math::Lerp, compiled from the reference's headers.  Only the dispatcher
 // layer is restated here (the full dispatcher stack needs Boost.MPL and is not
 // buildable in this environment): it follows the Serial adapter's std::
@@ -18,7 +19,9 @@
 #include <dax/math/VectorAnalysis.h>
 #include <dax/worklet/CellGradient.h>
 #include <dax/worklet/MarchingCubes.h>
+#include <dax/worklet/MarchingTetrahedra.h>
 #include <dax/worklet/Slice.h>
+#include <dax/worklet/Tetrahedralize.h>
 #include <dax/worklet/Threshold.h>
 
 #include <algorithm>
@@ -114,8 +117,30 @@ dax::Id ScanAndUpperBounds(const int32_t* count, dax::Id C, std::vector<dax::Id>
 // UpperBounds -> input cell of every output triangle, visit index, the
 // worklet's interpolated triangle, then (merge) Sort/Unique/LowerBounds of
 // the PointAsEdgeInterpolation records and the coordinates by Lerp.
-template <typename Build>
-int64_t GenerateInterpolated(const Ctx& ctx, const int32_t* count, int merge, float* verts,
+// An unstructured tetrahedral grid: explicit point coordinates [P][3] and
+// four point ids per cell (dax::cont::UnstructuredGrid<CellTagTetrahedron>).
+struct TetCtx {
+  const float* pts;
+  const int32_t* conn;
+  dax::Id numCells;
+  dax::Vector3 Coord(dax::Id p) const {
+    return dax::make_Vector3(pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]);
+  }
+  dax::exec::CellVertices<dax::CellTagTetrahedron> Verts(dax::Id cell) const {
+    dax::exec::CellVertices<dax::CellTagTetrahedron> v;
+    for (int n = 0; n < 4; ++n) v[n] = conn[4 * cell + n];
+    return v;
+  }
+  dax::exec::CellField<dax::Scalar, dax::CellTagTetrahedron> Gather(
+      const dax::exec::CellVertices<dax::CellTagTetrahedron>& v, const float* f) const {
+    dax::exec::CellField<dax::Scalar, dax::CellTagTetrahedron> vals;
+    for (int n = 0; n < 4; ++n) vals[n] = f[v[n]];
+    return vals;
+  }
+};
+
+template <typename Grid, typename Build>
+int64_t GenerateInterpolated(const Grid& ctx, const int32_t* count, int merge, float* verts,
                              int32_t* conn, int32_t* rec_a, int32_t* rec_b, float* rec_w,
                              int64_t* nverts, Build build) {
   *nverts = 0;
@@ -233,6 +258,45 @@ int64_t ref_slice_generate(const RefGrid* g, const float* origin, const float* n
       [&](dax::Id cell, dax::Id visit, dax::exec::InterpolatedCellPoints<dax::CellTagTriangle>& out) {
         dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cell);
         worklet(v, out, ctx.Coords(v), visit);
+      });
+}
+
+// DispatcherGenerateTopology<Tetrahedralize> with a constant count of 5 and
+// no point merging (UnitTestWorkletTetrahedralize.cxx:73-90): output cell o
+// is the worklet's visit o % 5 of input cell o / 5.
+void ref_tetrahedralize(const RefGrid* g, int32_t* conn) {
+  Ctx ctx(g);
+  dax::worklet::Tetrahedralize worklet;
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id o = 0; o < 5 * ctx.numCells; ++o) {
+    dax::exec::CellVertices<dax::CellTagTetrahedron> out;
+    worklet(ctx.Verts(o / 5), out, o, o % 5);
+    for (int n = 0; n < 4; ++n) conn[4 * o + n] = (int32_t)out[n];
+  }
+}
+
+// DispatcherMapCell<MarchingTetrahedraCount> over a tetrahedral grid
+// (dax/worklet/MarchingTetrahedra.h:49-80).
+void ref_mt_count(const int32_t* conn, int64_t C, const float* field, float iso, int32_t* count) {
+  TetCtx ctx{nullptr, conn, (dax::Id)C};
+  dax::worklet::MarchingTetrahedraCount worklet(iso);
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id c = 0; c < ctx.numCells; ++c)
+    count[c] = (int32_t)worklet(ctx.Gather(ctx.Verts(c), field));
+}
+
+// DispatcherGenerateInterpolatedCells<MarchingTetrahedraGenerate>
+// (MarchingTetrahedra.h:85-161) with the grid's explicit coordinates.
+int64_t ref_mt_generate(const float* pts, const int32_t* conn, int64_t C, const float* field,
+                        float iso, const int32_t* count, int merge, float* verts, int32_t* tconn,
+                        int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
+  TetCtx ctx{pts, conn, (dax::Id)C};
+  dax::worklet::MarchingTetrahedraGenerate worklet(iso);
+  return GenerateInterpolated(
+      ctx, count, merge, verts, tconn, rec_a, rec_b, rec_w, nverts,
+      [&](dax::Id cell, dax::Id visit, dax::exec::InterpolatedCellPoints<dax::CellTagTriangle>& out) {
+        dax::exec::CellVertices<dax::CellTagTetrahedron> v = ctx.Verts(cell);
+        worklet(v, out, ctx.Gather(v, field), visit);
       });
 }
 

@@ -163,3 +163,95 @@ def slice_cases():
     out.append(("nan_normal", (9, 7, 5), (0, 0, 0), (1, 1, 1), (0, 0, 0),
                 (1.0, 2.0, 3.0), (float("nan"), 0.0, 1.0)))
     return out
+
+
+# Freudenthal subdivision of each hexahedron into 6 tetrahedra, in the
+# reference test grid's order (dax/cont/testing/TestingGridGenerator.h:
+# 301-330): voxel corner lists, corners in TopologyUniform order.
+_FREUDENTHAL = ((0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 5, 6, 4), (1, 5, 6, 0), (1, 6, 2, 0))
+_CORNER = ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1))
+
+
+def tetrahedralize(dims):
+    """int32 [6*C, 4] connectivity of the uniform grid `dims` (points x
+    fastest), cells in id order, 6 tetrahedra per cell."""
+    nx, ny, nz = dims
+    k, j, i = np.meshgrid(np.arange(nz - 1), np.arange(ny - 1), np.arange(nx - 1), indexing="ij")
+    first = (i + nx * (j + ny * k)).ravel().astype(np.int64)
+    off = np.array([dx + nx * (dy + ny * dz) for dx, dy, dz in _CORNER], np.int64)
+    tets = np.array(_FREUDENTHAL, np.int64)  # [6, 4] corner ids
+    conn = first[:, None, None] + off[tets][None, :, :]
+    return conn.reshape(-1, 4).astype(np.int32)
+
+
+def grid_points(dims, origin=(0, 0, 0), spacing=(1, 1, 1)):
+    """float32 [P, 3] coordinates origin + spacing * ijk, x fastest."""
+    f32 = np.float32
+    ax = [f32(origin[a]) + f32(spacing[a]) * np.arange(dims[a]).astype(f32) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1).astype(f32)
+
+
+def shuffle_mesh(points, conn, field, seed):
+    """The same mesh with point ids permuted, cells reordered and each
+    cell's vertex list rotated (an even permutation)."""
+    rng = np.random.default_rng(seed)
+    P = points.shape[0]
+    perm = rng.permutation(P)           # new id of old point p is inv[p]
+    inv = np.empty(P, np.int64)
+    inv[perm] = np.arange(P)
+    pts = points[perm]
+    fld = field[perm]
+    c = inv[conn.astype(np.int64)]
+    c = c[rng.permutation(c.shape[0])]
+    rot = rng.integers(0, 3, size=c.shape[0])
+    out = c.copy()
+    for r in (1, 2):  # cycle vertices 1..3, which keeps the orientation
+        m = rot == r
+        out[m, 1:] = np.roll(c[m, 1:], r, axis=1)
+    return pts, out.astype(np.int32), fld
+
+
+def all_tet_cases():
+    """16 separate tetrahedra, tetrahedron c in marching case c."""
+    pts, conn, f = [], [], []
+    base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    for c in range(16):
+        pts.append(base + np.float32(2 * c))
+        conn.append(np.arange(4) + 4 * c)
+        f.extend(1.0 if (c >> n) & 1 else -1.0 for n in range(4))
+    return (np.concatenate(pts).astype(np.float32), np.array(conn, np.int32),
+            np.array(f, np.float32))
+
+
+def mt_cases():
+    """(name, points [P,3] f32, conn [C,4] i32, field [P] f32, isovalue)."""
+    out = []
+    # UnitTestWorkletMarchingTetrahedra.cxx:33-34, :50-60 -- 26^3 grid split
+    # 6 ways, field x+y+z, isovalue 70: 151 merged points
+    d = (26, 26, 26)
+    out.append(("kat26_linear", grid_points(d), tetrahedralize(d), linear_field(d), 70.0))
+    d = (20, 17, 13)
+    sp = tuple(1 / (n - 1) for n in d)
+    bl = random_blobs(d, 3, 21, noise=0.05)
+    out.append(("blobs_20x17x13", grid_points(d, spacing=sp), tetrahedralize(d), bl, 0.5))
+    pts, conn, fld = shuffle_mesh(grid_points(d, spacing=sp), tetrahedralize(d), bl, 22)
+    out.append(("blobs_shuffled", pts, conn, fld, 0.5))
+    pts, conn, fld = all_tet_cases()
+    out.append(("all16_cases", pts, conn, fld, 0.0))
+    d = (12, 11, 10)
+    f = random_blobs(d, 2, 23)
+    f[::5] = np.nan
+    out.append(("nan_sprinkled", grid_points(d), tetrahedralize(d), f, 0.4))
+    out.append(("all_inside", grid_points((5, 4, 3)), tetrahedralize((5, 4, 3)),
+                np.ones(60, np.float32), 0.0))
+    # tetrahedra with a repeated point id: zero-length edges, 0/0 weights
+    pts = grid_points((3, 3, 2))
+    f = np.linspace(-1, 1, 18).astype(np.float32)
+    conn = np.array([[0, 0, 4, 13], [1, 5, 5, 9], [2, 3, 14, 14], [4, 10, 11, 12]], np.int32)
+    out.append(("degenerate_ids", pts, conn, f, 0.05))
+    d = (48, 40, 36)
+    sp = tuple(1 / (n - 1) for n in d)
+    out.append(("blobs_48x40x36", grid_points(d, spacing=sp), tetrahedralize(d),
+                random_blobs(d, 4, 11, noise=0.05), 0.5))
+    return out

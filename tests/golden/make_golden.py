@@ -63,6 +63,13 @@ def main():
             out = R.slice_generate(g, po, pn, count, bool(merge))
             for k in ("verts", "conn", "rec_a", "rec_b", "rec_w"):
                 put(meta, arrays, "slice/%s/m%d/%s" % (name, merge, k), out[k])
+    for name, pts, conn, f, iso in cases.mt_cases():
+        count = R.mt_count(conn, f, iso)
+        put(meta, arrays, "mt/%s/count" % name, count)
+        for merge in (0, 1):
+            out = R.mt_generate(pts, conn, f, iso, count, bool(merge))
+            for k in ("verts", "conn", "rec_a", "rec_b", "rec_w"):
+                put(meta, arrays, "mt/%s/m%d/%s" % (name, merge, k), out[k])
     for name, dims, origin, spacing, emin, f in cases.gradient_cases():
         g = oracle.make_grid(dims, origin, spacing, emin)
         put(meta, arrays, "grad/%s" % name, R.cell_gradient(g, f))

@@ -75,9 +75,21 @@ def test_slice_golden(port, case):
             check("slice/%s/m%d/%s" % (name, merge, k), out[k])
 
 
+@pytest.mark.parametrize("case", cases.mt_cases(), ids=lambda c: c[0])
+def test_mt_golden(port, case):
+    name, pts, conn, f, iso = case
+    count = port.mt_count(conn, f, iso)
+    check("mt/%s/count" % name, count)
+    for merge in (0, 1):
+        out = port.mt_generate(pts, conn, f, iso, count, bool(merge))
+        for k in ("verts", "conn", "rec_a", "rec_b", "rec_w"):
+            check("mt/%s/m%d/%s" % (name, merge, k), out[k])
+
+
 def test_known_answers_in_golden():
     assert META["mc/kat26_linear/m1/verts"]["shape"] == [45, 3]
     assert META["mc/kat26_linear/m0/verts"]["shape"] == [183, 3]
     assert META["mc/kat26_linear/m1/conn"]["shape"] == [61, 3]
     assert META["slice/kat8_axis_x/m0/verts"]["shape"] == [294, 3]
     assert META["slice/kat8_axis_x/m1/verts"]["shape"] == [64, 3]
+    assert META["mt/kat26_linear/m1/verts"]["shape"] == [151, 3]

@@ -10,6 +10,9 @@ Known answers (DaxToolkit unit tests):
   * UnitTestWorkletCellGradient.cxx:31, :83-117 -- 8^3, x+y+z, gradient (1,1,1).
   * UnitTestWorkletSlice.cxx:22-24, :84-108 -- 8^3, origin (3,2,1), normal
     (1,0,0): 2 * 7^2 triangles, 3 points each unmerged, 8^2 points merged.
+  * UnitTestWorkletMarchingTetrahedra.cxx:33-34, :86-113 -- 26^3 grid split
+    into 6 tetrahedra per cell, field x+y+z, isovalue 70: 3 points per
+    triangle unmerged, 151 points merged.
 """
 import numpy as np
 import pytest
@@ -99,6 +102,34 @@ def test_slice_known_answer(kind):
     assert a["conn"].shape == (98, 3) and a["verts"].shape == (98 * 3, 3)
     assert b["conn"].shape == (98, 3) and b["verts"].shape == (64, 3)
     assert np.all(b["verts"][:, 0] == 6.0)
+
+
+@pytest.mark.parametrize("kind", _kinds())
+def test_mt_known_answer(kind):
+    O = oracle.Oracle(kind)
+    d = (26, 26, 26)
+    pts, conn, f = cases.grid_points(d), cases.tetrahedralize(d), cases.linear_field(d)
+    count = O.mt_count(conn, f, 70.0)
+    a = O.mt_generate(pts, conn, f, 70.0, count, merge=False)
+    b = O.mt_generate(pts, conn, f, 70.0, count, merge=True)
+    assert a["verts"].shape[0] == 3 * a["conn"].shape[0]
+    assert b["verts"].shape[0] == 151
+
+
+@pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
+@pytest.mark.parametrize("case", cases.mt_cases(), ids=lambda c: c[0])
+def test_mt_port_matches_reference_build(case):
+    name, pts, conn, f, iso = case
+    P, R = oracle.Oracle("port"), oracle.Oracle("reference")
+    c1, c2 = P.mt_count(conn, f, iso), R.mt_count(conn, f, iso)
+    assert np.array_equal(c1, c2)
+    for merge in (False, True):
+        a = P.mt_generate(pts, conn, f, iso, c1, merge)
+        b = R.mt_generate(pts, conn, f, iso, c2, merge)
+        for key in ("conn", "rec_a", "rec_b"):
+            assert np.array_equal(a[key], b[key]), key
+        for key in ("verts", "rec_w"):
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), key
 
 
 @pytest.mark.skipif(not oracle.build.reference_available(), reason="reference tree absent")
