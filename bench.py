@@ -180,6 +180,71 @@ def cpu_baseline(field_host, dims, spacing, iso, target_s, kind_pref="reference"
             "seconds": t}
 
 
+def _ref_oracle(threads=None):
+    import oracle
+    try:
+        O = oracle.Oracle("reference")
+    except Exception:
+        O = oracle.Oracle("port")
+    cores = O.set_threads(threads or O.max_threads()) if O.kind == "reference" else 1
+    return O, cores
+
+
+def cpu_slice_baseline(dims, spacing, origin, normal, target_s):
+    """The CPU implementation's SliceCount + merged SliceGenerate on the first
+    kz z-planes of the grid, kz chosen so the run takes about target_s."""
+    import oracle
+    O, cores = _ref_oracle()
+    nx, ny, nz = dims
+
+    def run(kz):
+        g = oracle.make_grid((nx, ny, kz), spacing=spacing)
+        t0 = time.perf_counter()
+        c = O.slice_count(g, origin, normal)
+        O.slice_generate(g, origin, normal, c, True)
+        return time.perf_counter() - t0, (nx - 1) * (ny - 1) * (kz - 1)
+
+    t, c = run(min(nz, 9))
+    kz = int(min(nz, max(9, target_s / (t / c) / ((nx - 1) * (ny - 1)) + 1)))
+    t, c = run(kz)
+    return {"value": c / t, "unit": "cells/s", "cores": cores,
+            "kind": "reference" if O.kind == "reference" else "port",
+            "sample": "first %d of %d z-planes of the %dx%dx%d grid, count + merged generate"
+                      % (kz, nz, nx, ny, nz)}
+
+
+def cpu_mt_baseline(dims, spacing, field_host, iso, target_s):
+    """The CPU implementation's MarchingTetrahedraCount + merged Generate on the
+    tetrahedra of the first kz cell layers (Tetrahedralize order), kz chosen
+    so the run takes about target_s."""
+    import numpy as np
+    import oracle
+    O, cores = _ref_oracle()
+    nx, ny, nz = dims
+    f3 = field_host.reshape(nz, ny, nx)
+
+    def run(kz):
+        g = oracle.make_grid((nx, ny, kz + 1), spacing=spacing)
+        conn = O.tetrahedralize(g)
+        ax = [np.float32(spacing[a]) * np.arange(d, dtype=np.float32)
+              for a, d in enumerate((nx, ny, kz + 1))]
+        z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        pts = np.stack([x.ravel(), y.ravel(), z.ravel()], 1)
+        sub = np.ascontiguousarray(f3[:kz + 1]).ravel()
+        t0 = time.perf_counter()
+        c = O.mt_count(conn, sub, iso)
+        O.mt_generate(pts, conn, sub, iso, c, True)
+        return time.perf_counter() - t0, conn.shape[0]
+
+    t, c = run(4)
+    kz = int(min(nz - 1, max(4, target_s / (t / c) / (5 * (nx - 1) * (ny - 1)))))
+    t, c = run(kz)
+    return {"value": c / t, "unit": "tetrahedra/s", "cores": cores,
+            "kind": "reference" if O.kind == "reference" else "port",
+            "sample": "tetrahedra of the first %d of %d cell layers (%d), count + merged generate"
+                      % (kz, nz - 1, c)}
+
+
 def run_reference(args, rank, world):
     """The reference's CPU implementation on the host cores; rank 0 only."""
     if rank != 0:
@@ -396,7 +461,7 @@ def mt_measurements(peak, stream, dev, reps=10, n=256):
                          reps, stream)
     o = cont.marching_tetrahedra(tg, f, iso, merge=True, stream=stream)
     cbytes = 17 * C
-    return {"grid": "%d^3 points, Tetrahedralize (5 per voxel)" % n, "tetrahedra": C,
+    return {"grid": "%d^3 points, Tetrahedralize (5 per voxel)" % n, "n": n, "tetrahedra": C,
             "triangles": int(o["conn"].shape[0]), "merged_points": int(o["verts"].shape[0]),
             "count_ms": t_count, "count_gbs": cbytes / (t_count / 1e3) / 1e9,
             "count_frac": cbytes / (t_count / 1e3) / 1e9 / peak,
@@ -693,6 +758,19 @@ def main():
         fh = field.cpu().numpy()
         cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if "slice" in line:
+            sl = cpu_slice_baseline(dims, spacing, (0.45, 0.5, 0.55), (0.3, 0.9, -0.3), 4.0)
+            sl["gpu_over_cpu"] = line["slice"]["cells_per_s"] / sl["value"]
+            line["slice"]["cpu_baseline"] = sl
+        if "marching_tetrahedra" in line:
+            import torch
+            from daxtoolkit_gb300 import synthetic
+            mt = line["marching_tetrahedra"]
+            n = mt["n"]
+            fm = synthetic.blob_field((n, n, n), 8, seed=0).numpy().ravel()
+            cm = cpu_mt_baseline((n, n, n), (1.0 / (n - 1),) * 3, fm, 0.5, 4.0)
+            cm["gpu_over_cpu"] = mt["tetrahedra_per_s_merged"] / cm["value"]
+            mt["cpu_baseline"] = cm
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
