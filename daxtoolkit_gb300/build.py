@@ -22,8 +22,10 @@ OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libdax_gb300.so")
 
 SOURCES = ["classify.cu", "mc.cu", "threshold.cu", "gradient.cu", "adjoint.cu", "capi.cu",
-           "noalloc.cu", "primitives.cu", "slice.cu", "mt.cu"]
-HEADERS = ["common.cuh", "kernels.cuh", "mc_case.cuh", "mc_tables.h"]
+           "noalloc.cu", "primitives.cu", "slice.cu", "mt.cu",
+           "mandelbulb.cu"]
+HEADERS = ["common.cuh", "kernels.cuh", "mc_case.cuh", "mc_tables.h", "mt_tables.h",
+           "coolwarm_table.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]

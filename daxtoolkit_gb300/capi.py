@@ -102,6 +102,15 @@ SIGNATURES = {
     "dax_gb300_mt_merge": ([vp, i64, vp, i64, f32, vp, sz, vp, sz, ctypes.POINTER(i64), vp], i32),
     "dax_gb300_mt_generate": ([vp, vp, i64, vp, i64, f32, ctypes.c_int, vp, sz, vp, sz, vp, i64,
                                vp, i64, vp, vp, vp, vp], i32),
+    "dax_gb300_mc_counted_scratch_bytes": ([gp], sz),
+    "dax_gb300_mc_counted_scan": ([gp, vp, vp, sz, ctypes.POINTER(i64), vp], i32),
+    "dax_gb300_mc_counted_merge": ([gp, vp, f32, vp, vp, sz, vp, sz, ctypes.POINTER(i64), vp], i32),
+    "dax_gb300_mc_counted_generate": ([gp, vp, f32, vp, ctypes.c_int, vp, sz, vp, sz, vp, i64, vp,
+                                       i64, vp, vp, vp, vp], i32),
+    "dax_gb300_interpolate_point_field_n": ([vp, vp, vp, i64, vp, i64, ctypes.c_int, vp, vp], i32),
+    "dax_gb300_mandelbulb_field": ([gp, vp, vp], i32),
+    "dax_gb300_mandelbulb_clip_count": ([gp, vp, f32, vp, vp, vp, vp, vp], i32),
+    "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),
     "dax_gb300_scan_scratch_bytes": ([i64], sz),
     "dax_gb300_scan": ([vp, vp, i64, i32, i32, vp, sz, vp, vp], i32),
     "dax_gb300_sort_scratch_bytes": ([i64, i32, i32], sz),

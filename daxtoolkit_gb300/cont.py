@@ -12,6 +12,8 @@ all arithmetic runs in libdax_gb300.so.
 """
 import ctypes
 
+import numpy as np
+
 import torch
 
 from . import capi
@@ -22,7 +24,9 @@ __all__ = [
     "DispatcherGenerateInterpolatedCells", "DispatcherGenerateTopology", "marching_cubes",
     "threshold", "cell_gradient", "Scratch", "SliceCount", "SliceGenerate", "slice", "slice_field",
     "MarchingTetrahedraCount", "MarchingTetrahedraGenerate", "marching_tetrahedra",
-    "Tetrahedralize", "tetrahedralize",
+    "Tetrahedralize", "tetrahedralize", "marching_cubes_counted", "Mandlebulb",
+    "MandlebulbClipCount", "MandlebulbVolume", "MandlebulbSurface", "mandlebulb_field",
+    "compute_mandlebulb", "colors_and_norms", "extract_surface", "extract_cut",
 ]
 
 
@@ -363,10 +367,160 @@ def marching_tetrahedra(grid, field, isovalue, merge=True, records=False, scratc
 
 
 def interpolate_point_field(rec_first, rec_second, rec_weight, field, stream=None):
-    out = torch.empty(rec_first.numel(), dtype=torch.float32, device=_out_device(field))
-    capi.call("dax_gb300_interpolate_point_field", _ptr(rec_first), _ptr(rec_second),
-              _ptr(rec_weight), rec_first.numel(), _ptr(field), _ptr(out), _stream(stream))
+    """CompactPointField: a scalar field [P] gives [V]; a field of k floats per
+    point [P, k] (a dax::Vector3 field has k = 3) gives [V, k]."""
+    if field.dim() == 1:
+        out = torch.empty(rec_first.numel(), dtype=torch.float32, device=_out_device(field))
+        capi.call("dax_gb300_interpolate_point_field", _ptr(rec_first), _ptr(rec_second),
+                  _ptr(rec_weight), rec_first.numel(), _ptr(field), _ptr(out), _stream(stream))
+        return out
+    if field.dim() != 2 or field.dtype != torch.float32 or not field.is_contiguous():
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "point field must be contiguous float32 [P] or [P, k]")
+    k = int(field.shape[1])
+    out = torch.empty((rec_first.numel(), k), dtype=torch.float32, device=_out_device(field))
+    capi.call("dax_gb300_interpolate_point_field_n", _ptr(rec_first), _ptr(rec_second),
+              _ptr(rec_weight), rec_first.numel(), _ptr(field), field.shape[0], k, _ptr(out),
+              _stream(stream))
     return out
+
+
+def marching_cubes_counted(grid, field, isovalue, count, merge=True, records=False,
+                           stream=None):
+    """DispatcherGenerateInterpolatedCells<MarchingCubesGenerate> driven by an
+    arbitrary int32 count per cell: the same dict as marching_cubes."""
+    _require_field(field, grid)
+    if (not isinstance(count, torch.Tensor) or count.dtype != torch.int32 or not count.is_cuda
+            or count.numel() != grid.GetNumberOfCells() or not count.is_contiguous()):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "count must be a contiguous int32 CUDA tensor, one per cell")
+    L = capi.lib()
+    g = grid.desc()
+    s = _stream(stream)
+    iso = float(isovalue)
+    nbytes = L.dax_gb300_mc_counted_scratch_bytes(ctypes.byref(g))
+    buf = _scratch_for("counted").get(nbytes)
+    T = ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_counted_scan", ctypes.byref(g), _ptr(count), _ptr(buf), buf.numel(),
+              ctypes.byref(T), s)
+    T = T.value
+    mbuf = None
+    if merge:
+        mbytes = L.dax_gb300_mt_merge_scratch_bytes(T, grid.GetNumberOfPoints())
+        mbuf = _scratch_for("counted_merge").get(mbytes)
+        V = ctypes.c_int64(0)
+        capi.call("dax_gb300_mc_counted_merge", ctypes.byref(g), _ptr(field), iso, _ptr(count),
+                  _ptr(buf), buf.numel(), _ptr(mbuf), mbuf.numel(), ctypes.byref(V), s)
+        V = V.value
+    else:
+        V = 3 * T
+    dev = count.device
+    verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
+    conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
+    ra = rb = rw = None
+    if records:
+        ra = torch.empty(V, dtype=torch.int32, device=dev)
+        rb = torch.empty(V, dtype=torch.int32, device=dev)
+        rw = torch.empty(V, dtype=torch.float32, device=dev)
+    capi.call("dax_gb300_mc_counted_generate", ctypes.byref(g), _ptr(field), iso, _ptr(count),
+              int(bool(merge)), _ptr(buf), buf.numel(), _ptr(mbuf), mbuf.numel() if merge else 0,
+              _ptr(verts), V, _ptr(conn), T, _ptr(ra), _ptr(rb), _ptr(rw), s)
+    capi.call("dax_gb300_mc_totals", _ptr(buf), None, None, s)  # raises on a bad count array
+    out = dict(verts=verts, conn=conn)
+    if records:
+        out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
+    return out
+
+
+# ---- the Mandelbulb benchmark pipeline (Benchmarks/Mandlebulb) -------------
+class Mandlebulb:
+    """worklet::Mandlebulb (Benchmarks/Mandlebulb/Worklets.h:65-109): the
+    escape iteration of every grid point."""
+
+
+class MandlebulbClipCount:
+    """worklet::MandlebulbClipCount (Worklets.h:112-170)."""
+
+    def __init__(self, origin, location, normal, isovalue):
+        self.Origin = tuple(float(v) for v in origin)
+        self.Location = tuple(float(v) for v in location)
+        self.Normal = tuple(float(v) for v in normal)
+        self.IsoValue = float(isovalue)
+
+
+class MandlebulbVolume:
+    """mandle::MandlebulbVolume (Mandlebulb.h): the grid and its escape
+    iteration field."""
+
+    def __init__(self, grid, field):
+        self.Grid = grid
+        self.EscapeIteration = field
+
+
+class MandlebulbSurface:
+    """mandle::MandlebulbSurface (Mandlebulb.h): the unmerged triangle surface
+    with per-point normals [3T, 3] and colours [3T, 4] uint8 -- the device
+    buffers the reference hands to OpenGL."""
+
+    def __init__(self, data, norms, colors):
+        self.Data = data
+        self.Norms = norms
+        self.Colors = colors
+
+
+def mandlebulb_field(grid, stream=None):
+    g = grid.desc()
+    out = torch.empty(grid.GetNumberOfPoints(), dtype=torch.float32, device="cuda")
+    capi.call("dax_gb300_mandelbulb_field", ctypes.byref(g), _ptr(out), _stream(stream))
+    return out
+
+
+def compute_mandlebulb(origin, spacing, extent_max, stream=None):
+    """computeMandlebulb (Benchmarks/Mandlebulb/Mandlebulb.cxx:83-102) on the
+    grid of points 0 .. extent_max."""
+    grid = UniformGrid(tuple(int(e) + 1 for e in extent_max), origin, spacing)
+    return MandlebulbVolume(grid, mandlebulb_field(grid, stream=stream))
+
+
+def colors_and_norms(points, stream=None):
+    """worklet::ColorsAndNorms (Worklets.h:177-209) over an unmerged surface's
+    points [3T, 3]: (normals [3T, 3], colours [3T, 4] uint8)."""
+    n = int(points.shape[0])
+    norms = torch.empty((n, 3), dtype=torch.float32, device=points.device)
+    colors = torch.empty((n, 4), dtype=torch.uint8, device=points.device)
+    capi.call("dax_gb300_colors_and_norms", _ptr(points), n, _ptr(norms), _ptr(colors),
+              _stream(stream))
+    return norms, colors
+
+
+def _surface(out, stream):
+    norms, colors = colors_and_norms(out["verts"], stream=stream)
+    return MandlebulbSurface(UnstructuredGrid(out["verts"], out["conn"]), norms, colors)
+
+
+def extract_surface(vol, iteration, stream=None):
+    """extractSurface (Mandlebulb.cxx:105-123): marching cubes of the escape
+    iteration at `iteration`, points not merged, then ColorsAndNorms."""
+    out = marching_cubes(vol.Grid, vol.EscapeIteration, iteration, merge=False, stream=stream)
+    return _surface(out, stream)
+
+
+def extract_cut(vol, cut_percent, iteration, stream=None):
+    """extractCut (Mandlebulb.cxx:126-157): MandlebulbClipCount against the z
+    plane at cut_percent of the grid, the count-driven generate, points not
+    merged, then ColorsAndNorms."""
+    g = vol.Grid
+    o, sp = g.Origin, g.Spacing
+    cd = [n - 1 for n in g.dims]
+    f32 = np.float32
+    # the location as the reference computes it, in float
+    loc = (f32(o[0]) + f32(sp[0]) * f32(cd[0]), f32(o[1]) + f32(sp[1]) * f32(cd[1]),
+           f32(o[2]) + f32(sp[2]) * f32(f32(cd[2]) * f32(cut_percent)))
+    w = MandlebulbClipCount(o, [float(v) for v in loc], (0.0, 0.0, 1.0), iteration)
+    count = DispatcherMapCell(w).Invoke(g, vol.EscapeIteration, stream=stream)
+    out = marching_cubes_counted(g, vol.EscapeIteration, iteration, count, merge=False,
+                                 stream=stream)
+    return _surface(out, stream)
 
 
 def threshold(grid, field, lo, hi, compact_field=True, scratch=None, stream=None):
@@ -423,6 +577,13 @@ class DispatcherMapCell:
             count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
             capi.call("dax_gb300_mc_classify_count", ctypes.byref(g), _ptr(field), w.IsoValue,
                       _ptr(count), None, _stream(stream))
+            count._dax_mc_source = (field.data_ptr(), w.IsoValue)
+            return count
+        if isinstance(w, MandlebulbClipCount):
+            count = torch.empty(C, dtype=torch.int32, device=_out_device(field))
+            vec = lambda v: (ctypes.c_float * 3)(*v)
+            capi.call("dax_gb300_mandelbulb_clip_count", ctypes.byref(g), _ptr(field), w.IsoValue,
+                      vec(w.Origin), vec(w.Location), vec(w.Normal), _ptr(count), _stream(stream))
             return count
         if isinstance(w, SliceCount):
             sf, iso = slice_field(grid, w.Origin, w.Normal, stream=stream)
@@ -452,12 +613,14 @@ class DispatcherMapCell:
 
 
 class DispatcherGenerateInterpolatedCells:
-    """DispatcherGenerateInterpolatedCells<MarchingCubesGenerate>.
+    """DispatcherGenerateInterpolatedCells<MarchingCubesGenerate | SliceGenerate |
+    MarchingTetrahedraGenerate>.
 
-    The count array is accepted for interface parity; on this device adapter
-    the generate pass recounts from the field (identical by construction for
-    MarchingCubesCount with the same isovalue) so that no per-cell array is
-    written or scanned.
+    A count array from MarchingCubesCount on the same field and isovalue
+    (tagged when DispatcherMapCell made it) is not read: the generate pass recounts from the field (identical by
+    construction), so no per-cell array is scanned.  Any other count array
+    (a clip, a mask) drives the generate as the reference's dispatcher does:
+    scan, upper bounds, visit index (marching_cubes_counted).
     """
 
     def __init__(self, count, worklet):
@@ -484,6 +647,11 @@ class DispatcherGenerateInterpolatedCells:
         elif isinstance(w, MarchingTetrahedraGenerate):
             out = marching_tetrahedra(grid, field, w.IsoValue, merge=self.RemoveDuplicatePoints,
                                       records=True, stream=stream)
+        elif (self.count is not None and isinstance(w, MarchingCubesGenerate)
+              and getattr(self.count, "_dax_mc_source", None) != (field.data_ptr(), w.IsoValue)):
+            out = marching_cubes_counted(grid, field, w.IsoValue, self.count,
+                                         merge=self.RemoveDuplicatePoints, records=True,
+                                         stream=stream)
         else:
             out = marching_cubes(grid, field, w.IsoValue, merge=self.RemoveDuplicatePoints,
                                  records=True, stream=stream)

@@ -185,6 +185,9 @@ int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
     return fail(DAX_GB300_ERROR_TIMEOUT, "scan look-back wait expired on the device");
   if (h.error & daxgb::kErrOverflow)
     return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31-1 triangles or vertices");
+  if (h.error & daxgb::kErrBadCount)
+    return fail(DAX_GB300_ERROR_BAD_VALUE,
+                "the count array asks a cell for more triangles than its case has");
   if (h.error & daxgb::kErrState)
     return fail(DAX_GB300_ERROR_BAD_VALUE,
                 "the merge scratch does not hold dax_gb300_mt_merge's result for this count pass");
@@ -486,6 +489,47 @@ MtMerge mt_merge_layout(int64_t T, int64_t P) {
   return M;
 }
 
+// The keys of the 3T records, written at M.keys: sorted and made unique at
+// M.uniq (the reference's Sort + Unique), then the header the merged kernels
+// read.  Blocking (the unique count comes back to the host).
+int sort_unique_keys(const MtMerge& M, char* m, int64_t T, int64_t P, int64_t* h_num_merged,
+                     cudaStream_t s) {
+  int64_t V = 0;
+  if (T > 0) {
+    cudaError_t e = cudaMemcpyAsync(m + M.uniq, m + M.keys, (size_t)(3 * T) * M.kb,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "copying merge keys");
+    daxgb::sort_unsigned_bits(m + M.uniq, 3 * T, M.kb == 8, 2 * daxgb::mt_key_bits(P), m + M.prim,
+                              s);
+    int st = check_launch("merge key sort");
+    if (st) return st;
+    if ((st = dax_gb300_unique(m + M.uniq, 3 * T, M.type, m + M.prim, M.prim_bytes, &V, s)))
+      return st;
+  }
+  daxgb::launch_mt_set_merged(m + M.hdr, T, V, M.keys, M.uniq, s);
+  if (h_num_merged) *h_num_merged = V;
+  return check_launch("merge header");
+}
+
+// Count-array-driven marching cubes scratch: [Info][inclusive scan: C x i32]
+// [scan scratch].
+struct CountedLayout {
+  size_t info, scan, prim, prim_bytes, total;
+};
+CountedLayout counted_layout(long long C) {
+  CountedLayout L;
+  L.info = 0;
+  L.scan = align256(sizeof(Info));
+  L.prim = align256(L.scan + 4 * (size_t)(C > 0 ? C : 1));
+  L.prim_bytes = dax_gb300_scan_scratch_bytes(C > 0 ? C : 1);
+  L.total = align256(L.prim + L.prim_bytes);
+  return L;
+}
+
+long long num_cells_of(const Grid& g) {
+  return has_cells(g) ? (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1) : 0;
+}
+
 }  // namespace
 
 int dax_gb300_mt_count(const int32_t* d_conn, int64_t num_cells, const float* d_field,
@@ -549,23 +593,12 @@ int dax_gb300_mt_merge(const int32_t* d_conn, int64_t num_cells, const float* d_
     return fail(DAX_GB300_ERROR_BAD_VALUE,
                 "merge scratch smaller than dax_gb300_mt_merge_scratch_bytes()");
   char* m = static_cast<char*>(d_merge);
-  int64_t V = 0;
   if (T > 0) {
     daxgb::launch_mt_emit_keys(d_conn, num_cells, d_field, num_points, isovalue,
                                static_cast<char*>(d_scratch), m + M.keys, num_sms(), s);
     if ((st = check_launch("marching tetrahedra key kernel"))) return st;
-    cudaError_t e = cudaMemcpyAsync(m + M.uniq, m + M.keys, (size_t)(3 * T) * M.kb,
-                                    cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "copying merge keys");
-    daxgb::sort_unsigned_bits(m + M.uniq, 3 * T, M.kb == 8, 2 * daxgb::mt_key_bits(num_points),
-                              m + M.prim, s);
-    if ((st = check_launch("merge key sort"))) return st;
-    if ((st = dax_gb300_unique(m + M.uniq, 3 * T, M.type, m + M.prim, M.prim_bytes, &V, stream)))
-      return st;
   }
-  daxgb::launch_mt_set_merged(m + M.hdr, T, V, M.keys, M.uniq, s);
-  if (h_num_merged) *h_num_merged = V;
-  return check_launch("marching tetrahedra merge header");
+  return sort_unique_keys(M, m, T, num_points, h_num_merged, s);
 }
 
 int dax_gb300_mt_generate(const float* d_points, const int32_t* d_conn, int64_t num_cells,
@@ -597,10 +630,171 @@ int dax_gb300_mt_generate(const float* d_points, const int32_t* d_conn, int64_t 
   // this scratch (its header); the kernels check the capacities on the device
   if (!d_merge || merge_bytes < 256)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "merge needs the dax_gb300_mt_merge scratch");
-  daxgb::launch_mt_merged(d_points, num_cells, d_field, num_points, isovalue, sc, d_merge,
-                          merge_bytes, d_verts, vert_capacity, d_tri_conn, tri_capacity,
-                          d_rec_first, d_rec_second, d_rec_weight, num_sms(), s);
+  daxgb::launch_mt_merged(d_points, nullptr, at<Info>(sc, daxgb::mt_layout(num_cells).info),
+                          d_field, num_points, isovalue, d_merge, merge_bytes, d_verts,
+                          vert_capacity, d_tri_conn, tri_capacity, d_rec_first, d_rec_second,
+                          d_rec_weight, num_sms(), s);
   return check_launch("marching tetrahedra merged kernels");
+}
+
+size_t dax_gb300_mc_counted_scratch_bytes(const dax_gb300_uniform_grid* grid) {
+  Grid g;
+  if (make_grid(grid, g)) return 0;
+  return counted_layout(num_cells_of(g)).total;
+}
+
+int dax_gb300_mc_counted_scan(const dax_gb300_uniform_grid* grid, const int32_t* d_count,
+                              void* d_scratch, size_t scratch_bytes, int64_t* h_num_triangles,
+                              void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  const long long C = num_cells_of(g);
+  const CountedLayout L = counted_layout(C);
+  if (!d_scratch || scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (C > 0 && !d_count) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count array");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* sc = static_cast<char*>(d_scratch);
+  int32_t T32 = 0;
+  if (C > 0 && (st = dax_gb300_scan(d_count, sc + L.scan, C, DAX_GB300_TYPE_I32, 0, sc + L.prim,
+                                    L.prim_bytes, &T32, stream)))
+    return st;
+  // the scan wraps like dax::Id; a negative or oversized total cannot be honoured
+  const int error = (T32 < 0) ? daxgb::kErrBadCount
+                              : (3ll * T32 > 2147483647ll ? daxgb::kErrOverflow : 0);
+  daxgb::launch_set_total(at<Info>(sc, L.info), T32 < 0 ? 0 : T32, error, s);
+  if ((st = check_launch("counted totals"))) return st;
+  if (h_num_triangles) *h_num_triangles = T32 < 0 ? 0 : T32;
+  if (error & daxgb::kErrBadCount)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "the count array sums to a negative total");
+  if (error) return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31-1 vertex records");
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_mc_counted_merge(const dax_gb300_uniform_grid* grid, const float* d_field,
+                               float isovalue, const int32_t* d_count, void* d_scratch,
+                               size_t scratch_bytes, void* d_merge, size_t merge_bytes,
+                               int64_t* h_num_merged, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  const long long C = num_cells_of(g);
+  const CountedLayout L = counted_layout(C);
+  if (!d_scratch || scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (C > 0 && (!d_count || !d_field)) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count or field");
+  if ((st = device_view(d_field, "field"))) return st;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* sc = static_cast<char*>(d_scratch);
+  int64_t T = 0;
+  if ((st = read_totals(sc, &T, nullptr, s))) return st;
+  const MtMerge M = mt_merge_layout(T, g.P);
+  if (!d_merge || merge_bytes < M.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "merge scratch smaller than dax_gb300_mt_merge_scratch_bytes(T, P)");
+  char* m = static_cast<char*>(d_merge);
+  if (T > 0) {
+    daxgb::launch_mc_counted(g, d_field, isovalue, d_count, at<int32_t>(sc, L.scan),
+                             at<Info>(sc, L.info), m + M.keys, nullptr, 0, nullptr, 0, nullptr,
+                             nullptr, nullptr, T, num_sms(), s);
+    if ((st = check_launch("counted key kernel"))) return st;
+    // a count the worklet cannot honour shows here, before the keys are used
+    if ((st = read_totals(sc, nullptr, nullptr, s))) return st;
+  }
+  return sort_unique_keys(M, m, T, g.P, h_num_merged, s);
+}
+
+int dax_gb300_mc_counted_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                  float isovalue, const int32_t* d_count, int merge,
+                                  void* d_scratch, size_t scratch_bytes, void* d_merge,
+                                  size_t merge_bytes, float* d_verts, int64_t vert_capacity,
+                                  int32_t* d_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                                  int32_t* d_rec_second, float* d_rec_weight, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  const long long C = num_cells_of(g);
+  if (C == 0) return DAX_GB300_SUCCESS;
+  const CountedLayout L = counted_layout(C);
+  if (!d_scratch || scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (!d_count || !d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count or field");
+  if ((st = device_view(d_field, "field"))) return st;
+  if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
+      tri_capacity < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
+  if ((d_rec_first || d_rec_second || d_rec_weight) &&
+      !(d_rec_first && d_rec_second && d_rec_weight))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "give all three record arrays or none");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* sc = static_cast<char*>(d_scratch);
+  Info* info = at<Info>(sc, L.info);
+  if (!merge) {
+    daxgb::launch_mc_counted(g, d_field, isovalue, d_count, at<int32_t>(sc, L.scan), info,
+                             nullptr, d_verts, vert_capacity, d_conn, tri_capacity, d_rec_first,
+                             d_rec_second, d_rec_weight, tri_capacity, num_sms(), s);
+    return check_launch("counted generate kernel");
+  }
+  if (!d_merge || merge_bytes < 256)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "merge needs the dax_gb300_mc_counted_merge scratch");
+  daxgb::launch_mt_merged(nullptr, &g, info, d_field, g.P, isovalue, d_merge, merge_bytes,
+                          d_verts, vert_capacity, d_conn, tri_capacity, d_rec_first, d_rec_second,
+                          d_rec_weight, num_sms(), s);
+  return check_launch("counted merged kernels");
+}
+
+int dax_gb300_mandelbulb_field(const dax_gb300_uniform_grid* grid, float* d_field, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field");
+  daxgb::launch_mandelbulb_field(g, d_field, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("mandelbulb field kernel");
+}
+
+int dax_gb300_mandelbulb_clip_count(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                    float isovalue, const float* origin, const float* location,
+                                    const float* normal, int32_t* d_count, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!has_cells(g)) return DAX_GB300_SUCCESS;
+  if (!d_field || !d_count || !origin || !location || !normal)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL argument");
+  if ((st = device_view(d_field, "field"))) return st;
+  daxgb::launch_mandelbulb_clip_count(
+      g, d_field, isovalue, make_float3(origin[0], origin[1], origin[2]),
+      make_float3(normal[0], normal[1], normal[2]), daxgb::slice_isovalue(location, normal),
+      d_count, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("mandelbulb clip count kernel");
+}
+
+int dax_gb300_colors_and_norms(const float* d_verts, int64_t num_points, float* d_norms,
+                               uint8_t* d_colors, void* stream) {
+  if (num_points <= 0) return DAX_GB300_SUCCESS;
+  if (num_points % 3) return fail(DAX_GB300_ERROR_BAD_VALUE, "points must come 3 per triangle");
+  if (!d_verts || !d_norms || !d_colors) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL argument");
+  if (reinterpret_cast<uintptr_t>(d_colors) & 3)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "colors must be 4-byte aligned");
+  daxgb::launch_colors_and_norms(d_verts, num_points, d_norms, d_colors, num_sms(),
+                                 static_cast<cudaStream_t>(stream));
+  return check_launch("colors and norms kernel");
+}
+
+int dax_gb300_interpolate_point_field_n(const int32_t* d_rec_first, const int32_t* d_rec_second,
+                                        const float* d_rec_weight, int64_t n, const float* d_in,
+                                        int64_t num_points, int components, float* d_out,
+                                        void* stream) {
+  if (n <= 0) return DAX_GB300_SUCCESS;
+  if (components < 1 || components > 16)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "components must be in [1, 16]");
+  if (!d_rec_first || !d_rec_second || !d_rec_weight || !d_in || !d_out)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL argument");
+  int st = device_view(d_in, "point field");
+  if (st) return st;
+  daxgb::launch_interpolate_n(d_rec_first, d_rec_second, d_rec_weight, n, num_points, components,
+                              d_in, d_out, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("interpolate kernel");
 }
 
 int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t* d_rec_second,

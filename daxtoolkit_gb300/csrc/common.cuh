@@ -130,6 +130,7 @@ constexpr int kErrCapacity = 2;    // output buffer too small
 constexpr int kErrOverflow = 4;    // more than 2^31 - 1 triangles or vertices
 constexpr int kErrBadIndex = 8;    // a cell lists a point id outside [0, P)
 constexpr int kErrState = 16;      // a merge scratch that no merge pass of this count wrote
+constexpr int kErrBadCount = 32;   // a count array asks a cell for a triangle its case lacks
 
 // Coordinate of grid index i along one axis: origin + spacing * (i + min),
 // computed in float with no fused multiply-add, as the reference's implicit

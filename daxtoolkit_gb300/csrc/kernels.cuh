@@ -82,6 +82,9 @@ void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff
                          cudaStream_t s);
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s);
+void launch_interpolate_n(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
+                          long long P, int k, const float* in, float* out, int num_sms,
+                          cudaStream_t s);
 
 // Threshold over row words: per word the kept-cell and used-point masks, the
 // packed counts (kept << 16) | used and the tile totals for
@@ -173,9 +176,28 @@ void launch_mt_emit_keys(const int32_t* conn, long long C, const float* f, long 
 // count it was built for) that the merged kernels check and read.
 void launch_mt_set_merged(void* merge, long long T, long long V, size_t keys_off,
                           size_t uniq_off, cudaStream_t s);
-void launch_mt_merged(const float* pts, long long C, const float* f, long long P, float iso,
-                      char* scratch, const void* merge, size_t merge_bytes, float* verts,
+// Merged outputs from the merge scratch: points are pts[P][3], or the uniform
+// grid's when grid is not NULL.
+void launch_mt_merged(const float* pts, const Grid* grid, Info* info, const float* f,
+                      long long P, float iso, const void* merge, size_t merge_bytes, float* verts,
                       long long vcap, int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb,
                       float* rw, int num_sms, cudaStream_t s);
+
+// Marching cubes driven by an int32 count per cell (mt.cu): scan = its
+// inclusive scan, Info.total_a = T.  keys != NULL writes the merge keys of
+// the 3T records (mt_key_bits(P) format), else vertices / connectivity /
+// records directly.
+void launch_set_total(Info* info, long long T, int error, cudaStream_t s);
+void launch_mc_counted(const Grid& g, const float* f, float iso, const int32_t* count,
+                       const int32_t* scan, Info* info, void* keys, float* verts, long long vcap,
+                       int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb, float* rw,
+                       long long T_hint, int num_sms, cudaStream_t s);
+
+// Mandelbulb benchmark pipeline (mandelbulb.cu).
+void launch_mandelbulb_field(const Grid& g, float* out, int num_sms, cudaStream_t s);
+void launch_colors_and_norms(const float* verts, long long nv, float* norms, uint8_t* colors,
+                             int num_sms, cudaStream_t s);
+void launch_mandelbulb_clip_count(const Grid& g, const float* f, float iso, float3 o, float3 n,
+                                  float loc, int32_t* count, int num_sms, cudaStream_t s);
 
 }  // namespace daxgb

@@ -820,6 +820,35 @@ __global__ void k_interpolate(const int32_t* __restrict__ ra, const int32_t* __r
     out[v] = lerp_rn(__ldg(in + ra[v]), __ldg(in + rb[v]), rw[v]);
 }
 
+// k components per point: out[v][c] = Lerp(in[first[v]][c], in[second[v]][c],
+// weight[v]) for a Vector3 (or any float tuple) point field, the templated
+// CompactPointField (DispatcherGenerateInterpolatedCells.h:107-141,
+// GenerateWorklets.h:65-100).  Ids outside [0, P) give NaN, nothing is read.
+__global__ void k_interpolate_n(const int32_t* __restrict__ ra, const int32_t* __restrict__ rb,
+                                const float* __restrict__ rw, long long n, long long P, int k,
+                                const float* __restrict__ in, float* __restrict__ out) {
+  const long long total = n * k;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long v = e / k;
+    const int c = (int)(e - v * k);
+    const int a = __ldg(ra + v), b = __ldg(rb + v);
+    float r = __int_as_float(0x7fc00000);
+    if (a >= 0 && a < P && b >= 0 && b < P)
+      r = lerp_rn(__ldg(in + (long long)a * k + c), __ldg(in + (long long)b * k + c), __ldg(rw + v));
+    out[e] = r;
+  }
+}
+
+void launch_interpolate_n(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
+                          long long P, int k, const float* in, float* out, int num_sms,
+                          cudaStream_t s) {
+  const long long want = (n * k + 255) / 256;
+  const long long cap = (long long)num_sms * 16;
+  const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+  k_interpolate_n<<<blocks, 256, 0, s>>>(ra, rb, rw, n, P, k, in, out);
+}
+
 void launch_interpolate(const int32_t* ra, const int32_t* rb, const float* rw, long long n,
                         const float* in, float* out, int num_sms, cudaStream_t s) {
   const long long want = (n + 255) / 256;

@@ -28,6 +28,7 @@
 // and Info.error gets kErrBadIndex.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "mc_case.cuh"
 #include "mt_tables.h"
 
 namespace daxgb {
@@ -393,9 +394,18 @@ __global__ void __launch_bounds__(256) k_mt_merged_conn(const char* __restrict__
 
 // Vertex v of the merged output from unique key v: its two point ids, the
 // weight from their field values, Lerp of their coordinates.
-template <typename U>
+// (i, j, k) of point p of a uniform grid.
+__device__ __forceinline__ void grid_ijk(const Grid& g, int p, int& i, int& j, int& k) {
+  const unsigned row = (unsigned)p / (unsigned)g.nx;
+  i = p - (int)(row * (unsigned)g.nx);
+  split_row(g, row, j, k);
+}
+
+// GRID: the points are a uniform grid's (coordinates from the point id),
+// else the explicit pts array.
+template <typename U, bool GRID>
 __global__ void __launch_bounds__(256) k_mt_merged_verts(const char* __restrict__ m,
-                                                         unsigned long long mbytes,
+                                                         unsigned long long mbytes, Grid g,
                                                          const Info* info, long long tcap,
                                                          long long vcap, int kbits,
                                                          const float* __restrict__ pts,
@@ -417,10 +427,19 @@ __global__ void __launch_bounds__(256) k_mt_merged_verts(const char* __restrict_
     const int A = (int)(k >> kbits), B = (int)(k & mask);
     const float fa = __ldg(f + A), fb = __ldg(f + B);
     const float w = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
-    const float* pa = pts + 3 * (long long)A;
-    const float* pb = pts + 3 * (long long)B;
+    if (GRID) {
+      int ia, ja, ka, ib, jb, kb;
+      grid_ijk(g, A, ia, ja, ka);
+      grid_ijk(g, B, ib, jb, kb);
+      verts[3 * v + 0] = lerp_rn(coord(g.ox, g.sx, ia, g.mx), coord(g.ox, g.sx, ib, g.mx), w);
+      verts[3 * v + 1] = lerp_rn(coord(g.oy, g.sy, ja, g.my), coord(g.oy, g.sy, jb, g.my), w);
+      verts[3 * v + 2] = lerp_rn(coord(g.oz, g.sz, ka, g.mz), coord(g.oz, g.sz, kb, g.mz), w);
+    } else {
+      const float* pa = pts + 3 * (long long)A;
+      const float* pb = pts + 3 * (long long)B;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) verts[3 * v + a] = lerp_rn(__ldg(pa + a), __ldg(pb + a), w);
+      for (int a = 0; a < 3; ++a) verts[3 * v + a] = lerp_rn(__ldg(pa + a), __ldg(pb + a), w);
+    }
     if (ra) {
       ra[v] = A;
       rb[v] = B;
@@ -454,6 +473,148 @@ __global__ void __launch_bounds__(256) k_mt_cell_count(const int32_t* __restrict
 }
 
 __global__ void k_mt_set_header(MtMergeHeader* hdr, MtMergeHeader v) { *hdr = v; }
+
+// ---- Marching cubes driven by an arbitrary count array ----------------------
+// DispatcherGenerateInterpolatedCells<MarchingCubesGenerate> with any per-cell
+// count array (DispatcherGenerateInterpolatedCells.h:158-231): the inclusive
+// scan of the counts, UpperBounds(scan, t) for the input cell of output
+// triangle t, visit index t - (scan[cell] - count[cell]), then the worklet's
+// triangle (MarchingCubes.h:121-168).  A count of 0 drops a cell's
+// triangles; a visit index at or beyond the cell's NumFaces (a count the
+// worklet cannot honour) raises kErrBadCount and writes nothing for it.
+
+// cellVertEdges (MarchingCubes.h:131-135): byte e = corners of edge e (low
+// nibble, high nibble), bytes 0-7 in the first word, 8-11 in the second.
+constexpr unsigned long long kHexEdgesLo = 0x7467655430232110ull;
+constexpr unsigned int kHexEdgesHi = 0x73625140u;
+
+__device__ __forceinline__ int hex_edge(int e) {
+  return e < 8 ? (int)((kHexEdgesLo >> (8 * e)) & 0xFF) : (int)((kHexEdgesHi >> (8 * (e - 8))) & 0xFF);
+}
+
+template <bool KEYS>
+__global__ void __launch_bounds__(256) k_mc_counted(Grid g, const float* __restrict__ f, float iso,
+                                                    const int32_t* __restrict__ count,
+                                                    const int32_t* __restrict__ scan, long long C,
+                                                    unsigned long long mcx,
+                                                    unsigned long long mcy, Info* info, MtOut o) {
+  __shared__ uint64_t s_case[256];
+  s_case[threadIdx.x] = kMcCase[threadIdx.x];
+  __syncthreads();
+  const long long T = info->total_a;
+  if (info->error) return;
+  if (!KEYS && (T > o.tcap || 3 * T > o.vcap)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&info->error, kErrCapacity);
+    return;
+  }
+  const unsigned cx = (unsigned)(g.nx - 1), cy = (unsigned)(g.ny - 1);
+  const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+  bool bad = false;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < T;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long lo = 0, hi = C;  // UpperBounds: the first cell whose scan exceeds t
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if ((long long)__ldg(scan + mid) <= t) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= C) {
+      bad = true;
+      continue;
+    }
+    const long long c = lo;
+    const long long visit = t - ((long long)__ldg(scan + c) - __ldg(count + c));
+    const unsigned r = div_by((unsigned)c, mcx);
+    const int i = (int)((unsigned)c - r * cx);
+    const unsigned kk = div_by(r, mcy);
+    const int k = (int)kk, j = (int)(r - kk * cy);
+    const long long p0 = ((long long)k * g.ny + j) * g.nx + i;
+    int cs = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int dx = (0x66 >> q) & 1, dy = (0xCC >> q) & 1, dz = q >> 2;
+      cs |= (__ldg(f + p0 + dx + dy * sy + dz * sz) > iso ? 1 : 0) << q;
+    }
+    const uint64_t word = s_case[cs];
+    if (visit < 0 || visit >= (long long)(word >> 60)) {
+      bad = true;
+      continue;
+    }
+    for (int m = 0; m < 3; ++m) {
+      const int e = (int)((word >> (4 * (3 * visit + m))) & 0xF);
+      const int ed = hex_edge(e);
+      const int q0 = ed & 0xF, q1 = ed >> 4;
+      const long long id0 = p0 + ((0x66 >> q0) & 1) + ((0xCC >> q0) & 1) * sy + (q0 >> 2) * sz;
+      const long long id1 = p0 + ((0x66 >> q1) & 1) + ((0xCC >> q1) & 1) * sy + (q1 >> 2) * sz;
+      // the lower point id first (MarchingCubes.h:148-157)
+      const bool keep = id0 < id1;
+      const int qa = keep ? q0 : q1, qb = keep ? q1 : q0;
+      const int A = (int)(keep ? id0 : id1), B = (int)(keep ? id1 : id0);
+      const long long rec = 3 * t + m;
+      if (KEYS) {
+        if (o.wide)
+          static_cast<unsigned long long*>(o.keys)[rec] =
+              ((unsigned long long)A << o.kbits) | (unsigned long long)B;
+        else
+          static_cast<uint32_t*>(o.keys)[rec] = ((uint32_t)A << o.kbits) | (uint32_t)B;
+      } else {
+        const float fa = __ldg(f + A), fb = __ldg(f + B);
+        const float w = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
+        const int ia = i + ((0x66 >> qa) & 1), ja = j + ((0xCC >> qa) & 1), ka = k + (qa >> 2);
+        const int ib = i + ((0x66 >> qb) & 1), jb = j + ((0xCC >> qb) & 1), kb = k + (qb >> 2);
+        o.verts[3 * rec + 0] = lerp_rn(coord(g.ox, g.sx, ia, g.mx), coord(g.ox, g.sx, ib, g.mx), w);
+        o.verts[3 * rec + 1] = lerp_rn(coord(g.oy, g.sy, ja, g.my), coord(g.oy, g.sy, jb, g.my), w);
+        o.verts[3 * rec + 2] = lerp_rn(coord(g.oz, g.sz, ka, g.mz), coord(g.oz, g.sz, kb, g.mz), w);
+        o.tconn[rec] = (int32_t)rec;
+        if (o.ra) {
+          o.ra[rec] = A;
+          o.rb[rec] = B;
+          o.rw[rec] = w;
+        }
+      }
+    }
+  }
+  if (bad) atomicOr(&info->error, kErrBadCount);
+}
+
+__global__ void k_set_total(Info* info, long long T, int error) {
+  info->total_a = T;
+  info->total_b = 0;
+  info->total_c = 0;
+  info->error = error;
+}
+
+void launch_set_total(Info* info, long long T, int error, cudaStream_t s) {
+  k_set_total<<<1, 1, 0, s>>>(info, T, error);
+}
+
+void launch_mc_counted(const Grid& g, const float* f, float iso, const int32_t* count,
+                       const int32_t* scan, Info* info, void* keys, float* verts, long long vcap,
+                       int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb, float* rw,
+                       long long T_hint, int num_sms, cudaStream_t s) {
+  const long long C = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1);
+  MtOut o{};
+  o.verts = verts;
+  o.tconn = tconn;
+  o.ra = ra;
+  o.rb = rb;
+  o.rw = rw;
+  o.keys = keys;
+  o.kbits = mt_key_bits(g.P);
+  o.wide = 2 * o.kbits > 32;
+  o.vcap = vcap;
+  o.tcap = tcap;
+  const unsigned long long mcx = div_multiplier((unsigned)(g.nx - 1));
+  const unsigned long long mcy = div_multiplier((unsigned)(g.ny - 1));
+  const long long want = (T_hint + 255) / 256;
+  if (keys) {
+    const int b = resident_blocks(k_mc_counted<true>, 256, 0, num_sms, want);
+    k_mc_counted<true><<<b, 256, 0, s>>>(g, f, iso, count, scan, C, mcx, mcy, info, o);
+  } else {
+    const int b = resident_blocks(k_mc_counted<false>, 256, 0, num_sms, want);
+    k_mc_counted<false><<<b, 256, 0, s>>>(g, f, iso, count, scan, C, mcx, mcy, info, o);
+  }
+}
 
 // ---- Tetrahedralize (the upstream caller: uniform grid -> tetrahedra) -----
 // PossibleTetraSplitCases (dax/worklet/Tetrahedralize.h:36-48): rows 0-4
@@ -653,12 +814,11 @@ void launch_mt_set_merged(void* merge, long long T, long long V, size_t keys_off
   k_mt_set_header<<<1, 1, 0, s>>>(static_cast<MtMergeHeader*>(merge), h);
 }
 
-void launch_mt_merged(const float* pts, long long C, const float* f, long long P, float iso,
-                      char* scratch, const void* merge, size_t merge_bytes, float* verts,
+void launch_mt_merged(const float* pts, const Grid* grid, Info* info, const float* f,
+                      long long P, float iso, const void* merge, size_t merge_bytes, float* verts,
                       long long vcap, int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb,
                       float* rw, int num_sms, cudaStream_t s) {
-  const MtLayout L = mt_layout(C);
-  Info* info = reinterpret_cast<Info*>(scratch + L.info);
+  const Grid g = grid ? *grid : Grid{};
   const unsigned long long mb = (unsigned long long)merge_bytes;
   const char* m = static_cast<const char*>(merge);
   const int kbits = mt_key_bits(P);
@@ -667,16 +827,28 @@ void launch_mt_merged(const float* pts, long long C, const float* f, long long P
     typedef unsigned long long U;
     const int b1 = resident_blocks(k_mt_merged_conn<U>, 256, 0, num_sms, want);
     k_mt_merged_conn<U><<<b1, 256, 0, s>>>(m, mb, info, tcap, vcap, tconn);
-    const int b2 = resident_blocks(k_mt_merged_verts<U>, 256, 0, num_sms, want);
-    k_mt_merged_verts<U><<<b2, 256, 0, s>>>(m, mb, info, tcap, vcap, kbits, pts, f, iso, verts,
-                                            ra, rb, rw);
+    if (grid) {
+      const int b2 = resident_blocks(k_mt_merged_verts<U, true>, 256, 0, num_sms, want);
+      k_mt_merged_verts<U, true><<<b2, 256, 0, s>>>(m, mb, g, info, tcap, vcap, kbits, pts, f, iso,
+                                                    verts, ra, rb, rw);
+    } else {
+      const int b2 = resident_blocks(k_mt_merged_verts<U, false>, 256, 0, num_sms, want);
+      k_mt_merged_verts<U, false><<<b2, 256, 0, s>>>(m, mb, g, info, tcap, vcap, kbits, pts, f,
+                                                     iso, verts, ra, rb, rw);
+    }
   } else {
     typedef uint32_t U;
     const int b1 = resident_blocks(k_mt_merged_conn<U>, 256, 0, num_sms, want);
     k_mt_merged_conn<U><<<b1, 256, 0, s>>>(m, mb, info, tcap, vcap, tconn);
-    const int b2 = resident_blocks(k_mt_merged_verts<U>, 256, 0, num_sms, want);
-    k_mt_merged_verts<U><<<b2, 256, 0, s>>>(m, mb, info, tcap, vcap, kbits, pts, f, iso, verts,
-                                            ra, rb, rw);
+    if (grid) {
+      const int b2 = resident_blocks(k_mt_merged_verts<U, true>, 256, 0, num_sms, want);
+      k_mt_merged_verts<U, true><<<b2, 256, 0, s>>>(m, mb, g, info, tcap, vcap, kbits, pts, f, iso,
+                                                    verts, ra, rb, rw);
+    } else {
+      const int b2 = resident_blocks(k_mt_merged_verts<U, false>, 256, 0, num_sms, want);
+      k_mt_merged_verts<U, false><<<b2, 256, 0, s>>>(m, mb, g, info, tcap, vcap, kbits, pts, f,
+                                                     iso, verts, ra, rb, rw);
+    }
   }
 }
 

@@ -257,6 +257,72 @@ int dax_gb300_mt_generate(const float* d_points, const int32_t* d_conn, int64_t 
                           int32_t* d_rec_second, float* d_rec_weight, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Marching cubes driven by an arbitrary count array                          */
+/* ------------------------------------------------------------------------ */
+
+/* DispatcherGenerateInterpolatedCells<MarchingCubesGenerate> with any int32
+ * per-cell count array d_count (DispatcherGenerateInterpolatedCells.h:158-301):
+ * ScanInclusive of the counts, UpperBounds for each output triangle's cell, the
+ * visit index, the worklet's triangle; merging by Sort + Unique + LowerBounds
+ * of the interpolation records.  A count of 0 drops a cell (e.g. the
+ * Mandelbulb cut, below); a count above the cell's NumFaces yields
+ * DAX_GB300_ERROR_BAD_VALUE from the totals and writes nothing for it.
+ *   dax_gb300_mc_counted_scan     (blocking) -> *h_num_triangles = T
+ *   dax_gb300_mc_counted_merge    (blocking, merge only) -> *h_num_merged = V;
+ *                                 d_merge: dax_gb300_mt_merge_scratch_bytes(T, P)
+ *   dax_gb300_mc_counted_generate (asynchronous), outputs as dax_gb300_mc_generate;
+ *                                 dax_gb300_mc_totals(d_scratch, ...) reports errors. */
+size_t dax_gb300_mc_counted_scratch_bytes(const dax_gb300_uniform_grid* grid);
+int dax_gb300_mc_counted_scan(const dax_gb300_uniform_grid* grid, const int32_t* d_count,
+                              void* d_scratch, size_t scratch_bytes, int64_t* h_num_triangles,
+                              void* stream);
+int dax_gb300_mc_counted_merge(const dax_gb300_uniform_grid* grid, const float* d_field,
+                               float isovalue, const int32_t* d_count, void* d_scratch,
+                               size_t scratch_bytes, void* d_merge, size_t merge_bytes,
+                               int64_t* h_num_merged, void* stream);
+int dax_gb300_mc_counted_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                  float isovalue, const int32_t* d_count, int merge,
+                                  void* d_scratch, size_t scratch_bytes, void* d_merge,
+                                  size_t merge_bytes, float* d_verts, int64_t vert_capacity,
+                                  int32_t* d_conn, int64_t tri_capacity, int32_t* d_rec_first,
+                                  int32_t* d_rec_second, float* d_rec_weight, void* stream);
+
+/* CompactPointField for a point field of `components` floats per point (a
+ * dax::Vector3 field has 3): d_out[v][c] = Lerp(d_in[first[v]][c],
+ * d_in[second[v]][c], weight[v]); record ids outside [0, num_points) give
+ * NaN and are not read.  Asynchronous. */
+int dax_gb300_interpolate_point_field_n(const int32_t* d_rec_first, const int32_t* d_rec_second,
+                                        const float* d_rec_weight, int64_t n, const float* d_in,
+                                        int64_t num_points, int components, float* d_out,
+                                        void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* The Mandelbulb benchmark's compute pipeline (Benchmarks/Mandlebulb)        */
+/* ------------------------------------------------------------------------ */
+
+/* worklet::Mandlebulb (Worklets.h:65-109) over the grid's points: the escape
+ * iteration (0 .. 35) of pos -> pos^10 + c, as float[P].  The transcendental
+ * functions are CUDA's; a point on the fractal's boundary may escape one
+ * iteration apart from a host C library's evaluation.  Asynchronous. */
+int dax_gb300_mandelbulb_field(const dax_gb300_uniform_grid* grid, float* d_field, void* stream);
+
+/* worklet::MandlebulbClipCount (Worklets.h:112-170): per cell the
+ * marching-cubes triangle count at isovalue when a cell point lies beyond the
+ * plane (dot(normal, p - origin) > dot(normal, location)), else 0; int32 per
+ * cell, for dax_gb300_mc_counted_*.  Asynchronous. */
+int dax_gb300_mandelbulb_clip_count(const dax_gb300_uniform_grid* grid, const float* d_field,
+                                    float isovalue, const float* origin, const float* location,
+                                    const float* normal, int32_t* d_count, void* stream);
+
+/* worklet::ColorsAndNorms (Worklets.h:177-209) on an unmerged triangle surface
+ * (3 points per triangle, num_points = 3T): per point the unit normal of its
+ * triangle (float[3]) and its cool-warm colour, r g b 255 (uint8[4], 4-byte
+ * aligned), bit for bit as the reference computes them on the CPU.
+ * Asynchronous. */
+int dax_gb300_colors_and_norms(const float* d_verts, int64_t num_points, float* d_norms,
+                               uint8_t* d_colors, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batched marching cubes: many grids, one launch per pass                   */
 /* ------------------------------------------------------------------------ */
 

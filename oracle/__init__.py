@@ -78,6 +78,10 @@ class Oracle:
         self._slice_gen.restype = i64
         self._tetra = getattr(L, prefix + "tetrahedralize")
         self._tetra.argtypes = [gp, vp]
+        if kind == "port":
+            L.orc_mandelbulb_field.argtypes = [gp, vp]
+            L.orc_colors_and_norms.argtypes = [vp, i64, vp, vp]
+            L.orc_mandelbulb_clip_count.argtypes = [gp, vp, ctypes.c_float, vp, vp, vp, vp]
         self._mt_count = getattr(L, prefix + "mt_count")
         self._mt_count.argtypes = [vp, i64, vp, ctypes.c_float, vp]
         self._mt_gen = getattr(L, prefix + "mt_generate")
@@ -97,6 +101,11 @@ class Oracle:
 
     def max_threads(self):
         return int(self.lib.ref_max_threads()) if self.kind == "reference" else 1
+
+    @staticmethod
+    def _points(g):
+        d = grid_dims(g)
+        return d[0] * d[1] * d[2]
 
     @staticmethod
     def _cells(g):
@@ -191,6 +200,36 @@ class Oracle:
         conn = np.zeros((5 * self._cells(g), 4), np.int32)
         self._tetra(ctypes.byref(g), _ptr(conn))
         return conn
+
+    # -- Mandelbulb benchmark pipeline (C restatement only: the reference's
+    #    worklets there need Boost.Preprocessor, absent from this image) --
+    def mandelbulb_field(self, g):
+        out = np.zeros(self._points(g), np.float32)
+        self._port().orc_mandelbulb_field(ctypes.byref(g), _ptr(out))
+        return out
+
+    def colors_and_norms(self, verts):
+        verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        norms = np.zeros_like(verts)
+        colors = np.zeros((verts.shape[0], 4), np.uint8)
+        self._port().orc_colors_and_norms(_ptr(verts), verts.shape[0], _ptr(norms), _ptr(colors))
+        return norms, colors
+
+    def mandelbulb_clip_count(self, g, field, iso, origin, location, normal):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        vec = lambda v: np.asarray(v, np.float32)
+        o, l, n = vec(origin), vec(location), vec(normal)
+        count = np.zeros(self._cells(g), np.int32)
+        self._port().orc_mandelbulb_clip_count(ctypes.byref(g), _ptr(field), float(iso), _ptr(o),
+                                               _ptr(l), _ptr(n), _ptr(count))
+        return count
+
+    def _port(self):
+        if self.kind == "port":
+            return self.lib
+        if not hasattr(self, "_port_lib"):
+            self._port_lib = Oracle("port").lib
+        return self._port_lib
 
     def mt_count(self, conn, field, iso):
         """MarchingTetrahedraCount per tetrahedron; conn is int32 [C, 4]."""

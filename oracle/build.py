@@ -53,9 +53,10 @@ def _newer(target, sources):
 def build_oracle(force=False):
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "dax_oracle.c")
-    table = os.path.join(HERE, "..", "daxtoolkit_gb300", "csrc", "mc_tables.h")
-    if force or not _newer(ORACLE_SO, [src, table]):
-        subprocess.check_call(["gcc", "-std=c99"] + CFLAGS + [src, "-o", ORACLE_SO])
+    tables = [os.path.join(HERE, "..", "daxtoolkit_gb300", "csrc", t)
+              for t in ("mc_tables.h", "mt_tables.h", "coolwarm_table.h")]
+    if force or not _newer(ORACLE_SO, [src] + tables):
+        subprocess.check_call(["gcc", "-std=c99"] + CFLAGS + [src, "-o", ORACLE_SO, "-lm"])
     return ORACLE_SO
 
 

@@ -544,3 +544,119 @@ void orc_tetrahedralize(const orc_grid* g, int32_t* conn) {
     for (int n = 0; n < 4; ++n) conn[4 * o + n] = (int32_t)v[row[n]];
   }
 }
+
+/* ---- Mandelbulb benchmark pipeline (Benchmarks/Mandlebulb) ----------------- */
+
+#include <math.h>
+
+#include "../daxtoolkit_gb300/csrc/coolwarm_table.h"
+
+static const unsigned char kCoolWarm[3 * DAX_GB300_COOLWARM_ENTRIES] = DAX_GB300_COOLWARM_RGB;
+
+/* dax::math::MagnitudeSquared = dot(p, p), components in order. */
+static float magsq3(const float p[3]) {
+  float r = p[0] * p[0];
+  r += p[1] * p[1];
+  r += p[2] * p[2];
+  return r;
+}
+
+/* worklet::Mandlebulb::PowerN (Benchmarks/Mandlebulb/Worklets.h:92-108): the
+ * 10th power of White and Nylander's formula, in float with libm's float
+ * functions (dax::math maps Sqrt, ATan2, Pow, Sin, Tan, Cos to sqrtf ...). */
+static void mandelbulb_power(const float pos[3], float out[3]) {
+  const float squareR = magsq3(pos);
+  const float t = sqrtf(pos[0] * pos[0] + pos[1] * pos[1]);
+  const float thetaN = 10 * atan2f(t, pos[2]);
+  const float phiN = 10 * atan2f(pos[1], pos[2]);
+  const float powR = powf(squareR, 5.0f);
+  out[0] = powR * (sinf(thetaN) * tanf(phiN));
+  out[1] = powR * (sinf(thetaN) * sinf(phiN));
+  out[2] = powR * cosf(thetaN);
+}
+
+/* worklet::Mandlebulb::operator() (Worklets.h:70-90): the escape iteration of
+ * pos -> pos^10 + c, 0 when c itself lies outside radius sqrt(2), at most 35. */
+static float mandelbulb_value(const float c[3]) {
+  float pos[3] = {c[0], c[1], c[2]};
+  if (magsq3(pos) > 2) return 0;
+  for (int i = 1; i < 35; ++i) {
+    float q[3];
+    mandelbulb_power(pos, q);
+    for (int a = 0; a < 3; ++a) pos[a] = q[a] + c[a];
+    if (magsq3(pos) > 2) return (float)i;
+  }
+  return 35;
+}
+
+/* DispatcherMapField<Mandlebulb> over the grid's point coordinates
+ * (Benchmarks/Mandlebulb/Mandlebulb.cxx:83-102). */
+void orc_mandelbulb_field(const orc_grid* g, float* out) {
+  int64_t d[3];
+  dims_of(g, d);
+  const int64_t P = d[0] * d[1] * d[2];
+  for (int64_t p = 0; p < P; ++p) {
+    float c[3];
+    point_coords(g, d, p, c);
+    out[p] = mandelbulb_value(c);
+  }
+}
+
+/* worklet::ColorsAndNorms (Worklets.h:177-209) over the points of an unmerged
+ * triangle surface (point v belongs to triangle v / 3): the normal
+ * Normal(Cross(b - a, c - a)) = (1 / sqrt(dot)) * cross, and the cool-warm
+ * colour of |dot(point, (0.09, 0.09, 0.9))| (CoolWarmColorMap.h:38-45) with
+ * alpha 255.  norms [nv][3], colors [nv][4]. */
+void orc_colors_and_norms(const float* verts, int64_t nv, float* norms, uint8_t* colors) {
+  for (int64_t v = 0; v < nv; ++v) {
+    const float* c0 = verts + 3 * (3 * (v / 3));
+    const float* c1 = c0 + 3;
+    const float* c2 = c0 + 6;
+    float a[3], b[3], x[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = c1[k] - c0[k];
+      b[k] = c2[k] - c0[k];
+    }
+    x[0] = a[1] * b[2] - a[2] * b[1];
+    x[1] = a[2] * b[0] - a[0] * b[2];
+    x[2] = a[0] * b[1] - a[1] * b[0];
+    const float r = 1 / sqrtf(magsq3(x));
+    for (int k = 0; k < 3; ++k) norms[3 * v + k] = r * x[k];
+    const float* p = verts + 3 * v;
+    float s = p[0] * 0.09f;
+    s += p[1] * 0.09f;
+    s += p[2] * 0.9f;
+    s = fabsf(s);
+    s = fmaxf(0.0f, s);
+    s = fminf(0.9999f, s);
+    const int idx = (int)(257 * s);
+    for (int k = 0; k < 3; ++k) colors[4 * v + k] = kCoolWarm[3 * idx + k];
+    colors[4 * v + 3] = 255;
+  }
+}
+
+/* worklet::MandlebulbClipCount (Worklets.h:112-170): a cell counts its
+ * marching-cubes triangles only when one of its points lies beyond the plane,
+ * dot(N, p - O) > dot(N, L); otherwise 0. */
+void orc_mandelbulb_clip_count(const orc_grid* g, const float* field, float iso,
+                               const float* origin, const float* location, const float* normal,
+                               int32_t* count) {
+  int64_t d[3];
+  dims_of(g, d);
+  const int64_t C = num_cells(d);
+  const float loc = dot3(normal, location);
+  for (int64_t c = 0; c < C; ++c) {
+    int64_t v[8];
+    float val[8];
+    cell_vertices(d, c, v);
+    int in = 0;
+    for (int n = 0; n < 8; ++n) {
+      float p[3], r[3];
+      point_coords(g, d, v[n], p);
+      for (int a = 0; a < 3; ++a) r[a] = p[a] - origin[a];
+      in |= dot3(normal, r) > loc;
+      val[n] = field[v[n]];
+    }
+    count[c] = in ? num_faces(classify(val, iso)) : 0;
+  }
+}
