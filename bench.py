@@ -395,6 +395,7 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                     "field_kernel_frac": 4 * P / (t_sf / 1e3) / 1e9 / peak}
     del sfield, sscr, sverts, sconn
     out["marching_tetrahedra"] = mt_measurements(peak, stream, dev, reps=max(3, reps // 5))
+    out["mandelbulb"] = mandelbulb_measurements(stream, reps=max(3, reps // 5))
 
     # --- 64 uneven grids: batched graph replay vs per-grid loop -------------
     gdims = synthetic.batch_grid_dims(64, 32, 192, 777)
@@ -468,6 +469,52 @@ def mt_measurements(peak, stream, dev, reps=10, n=256):
             "count_formula": "17 B per tetrahedron (ids + case byte)",
             "unmerged_ms": t_unmerged, "merged_ms": t_merged,
             "tetrahedra_per_s_merged": C / (t_merged / 1e3)}
+
+
+def mandelbulb_measurements(stream, reps=10, sizes=(200, 512), iteration=3.5, cut=0.8):
+    """The Mandelbulb benchmark's compute pipeline (computeMandlebulb,
+    extractSurface, extractCut with ColorsAndNorms; Benchmarks/Mandlebulb) on
+    its own volume -- origin -1, spacing 2/n, points 0..n -- at the demo's
+    default n = 200 and at n = 512.  The escape-iteration field is bound by
+    the transcendental functions of up to 34 iterations per point, not by
+    memory; the surfaces are marching cubes of it."""
+    from daxtoolkit_gb300 import cont
+    out = {}
+    for n in sizes:
+        vol = cont.compute_mandlebulb((-1.0,) * 3, (2.0 / n,) * 3, (n, n, n), stream=stream)
+        t_field = _event_ms(lambda: cont.mandlebulb_field(vol.Grid, stream=stream), reps, stream)
+        surf = cont.extract_surface(vol, iteration, stream=stream)
+        t_surf = _event_ms(lambda: cont.extract_surface(vol, iteration, stream=stream), reps, stream)
+        cutsurf = cont.extract_cut(vol, cut, iteration, stream=stream)
+        t_cut = _event_ms(lambda: cont.extract_cut(vol, cut, iteration, stream=stream), reps, stream)
+        P = vol.Grid.GetNumberOfPoints()
+        out["n%d" % n] = {"points": P, "field_ms": t_field, "points_per_s": P / (t_field / 1e3),
+                          "iteration": iteration, "surface_triangles": surf.Data.GetNumberOfCells(),
+                          "surface_ms": t_surf, "cut": cut,
+                          "cut_triangles": cutsurf.Data.GetNumberOfCells(), "cut_ms": t_cut}
+    return out
+
+
+def cpu_mandelbulb_baseline(n, target_s):
+    """The C restatement of the Mandelbulb escape iteration (single thread; the
+    reference's worklet needs Boost.Preprocessor and is not built here) on the
+    first kz z-planes of the n^3 volume, kz chosen so it takes about target_s."""
+    import oracle
+    O = oracle.Oracle("port")
+    sp = 2.0 / n
+
+    def run(kz):
+        g = oracle.make_grid((n + 1, n + 1, kz), (-1.0, -1.0, -1.0 + sp * (n // 2)), (sp,) * 3)
+        t0 = time.perf_counter()
+        O.mandelbulb_field(g)
+        return time.perf_counter() - t0, (n + 1) * (n + 1) * kz
+
+    t, c = run(2)
+    kz = int(min(n + 1 - n // 2, max(2, target_s / (t / c) / ((n + 1) ** 2))))
+    t, c = run(kz)
+    return {"value": c / t, "unit": "points/s", "cores": 1, "kind": "port",
+            "sample": "escape iteration of %d z-planes through the middle of the %d^3-cell volume"
+                      % (kz, n)}
 
 
 def primitive_measurements(peak, stream, dev, reps=10):
@@ -762,6 +809,10 @@ def main():
             sl = cpu_slice_baseline(dims, spacing, (0.45, 0.5, 0.55), (0.3, 0.9, -0.3), 4.0)
             sl["gpu_over_cpu"] = line["slice"]["cells_per_s"] / sl["value"]
             line["slice"]["cpu_baseline"] = sl
+        if "mandelbulb" in line:
+            mb = cpu_mandelbulb_baseline(200, 3.0)
+            mb["gpu_over_cpu"] = line["mandelbulb"]["n200"]["points_per_s"] / mb["value"]
+            line["mandelbulb"]["cpu_baseline"] = mb
         if "marching_tetrahedra" in line:
             import torch
             from daxtoolkit_gb300 import synthetic
