@@ -396,6 +396,7 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
     del sfield, sscr, sverts, sconn
     out["marching_tetrahedra"] = mt_measurements(peak, stream, dev, reps=max(3, reps // 5))
     out["mandelbulb"] = mandelbulb_measurements(stream, reps=max(3, reps // 5))
+    out["reference_mc_benchmark"] = reference_benchmark_measurements(stream, reps=max(3, reps // 5))
 
     # --- 64 uneven grids: batched graph replay vs per-grid loop -------------
     gdims = synthetic.batch_grid_dims(64, 32, 192, 777)
@@ -469,6 +470,60 @@ def mt_measurements(peak, stream, dev, reps=10, n=256):
             "count_formula": "17 B per tetrahedron (ids + case byte)",
             "unmerged_ms": t_unmerged, "merged_ms": t_merged,
             "tetrahedra_per_s_merged": C / (t_merged / 1e3)}
+
+
+def reference_benchmark_measurements(stream, reps=10, sizes=(128, 256, 512)):
+    """The reference's own marching-cubes benchmark workload
+    (Benchmarks/MarchingCubes: main.cxx:21-44, Pipeline.h:100-150): a dim^3
+    grid of unit spacing, Magnitude of the point coordinates, marching cubes
+    at isovalue 100 with points merged (REMOVE_DUPLICATES) or not; the
+    benchmark's default size is 128.  The time is the benchmark's timed
+    region (count + generate, the field already computed), device-timed; the
+    VTK dump of the 128^3 merged surface is timed on the host."""
+    import tempfile
+    from daxtoolkit_gb300 import cont
+    out = {}
+    for dim in sizes:
+        grid = cont.UniformGrid((dim,) * 3)
+        f = cont.point_magnitude(grid, stream=stream)
+        C = grid.GetNumberOfCells()
+        row = {"cells": C}
+        for merge in (False, True):
+            o = cont.marching_cubes(grid, f, 100.0, merge=merge, stream=stream)
+            t = _event_ms(lambda: cont.marching_cubes(grid, f, 100.0, merge=merge, stream=stream),
+                          reps, stream)
+            key = "remove_duplicates" if merge else "plain"
+            row[key] = {"ms": t, "cells_per_s": C / (t / 1e3), "triangles": int(o["conn"].shape[0]),
+                        "points": int(o["verts"].shape[0])}
+        out["dim%d" % dim] = row
+        if dim == 128:
+            o = cont.marching_cubes(grid, f, 100.0, merge=True, stream=stream)
+            with tempfile.TemporaryDirectory() as d:
+                path = d + "/MCdaxResult.vtk"
+                t0 = time.perf_counter()
+                cont.write_vtk(path, cont.UnstructuredGrid(o["verts"], o["conn"]))
+                dt = time.perf_counter() - t0
+                size = os.path.getsize(path)
+            out["vtk_write_128"] = {"bytes": size, "seconds": dt, "mb_per_s": size / dt / 1e6}
+    return out
+
+
+def cpu_reference_benchmark(dim=128):
+    """The reference's CPU implementation (its worklets built from source,
+    OpenMP over all host threads) on the whole dim^3 benchmark workload."""
+    import oracle
+    O, cores = _ref_oracle()
+    g = oracle.make_grid((dim,) * 3)
+    f = O.point_magnitude(g)
+    out = {"cores": cores, "kind": "reference" if O.kind == "reference" else "port",
+           "sample": "the whole %d^3 benchmark grid" % dim, "unit": "cells/s"}
+    for merge in (False, True):
+        t0 = time.perf_counter()
+        c, _ = O.mc_count(g, f, 100.0)
+        O.mc_generate(g, f, 100.0, c, merge)
+        dt = time.perf_counter() - t0
+        out["remove_duplicates" if merge else "plain"] = (dim - 1) ** 3 / dt
+    return out
 
 
 def mandelbulb_measurements(stream, reps=10, sizes=(200, 512), iteration=3.5, cut=0.8):
@@ -809,6 +864,11 @@ def main():
             sl = cpu_slice_baseline(dims, spacing, (0.45, 0.5, 0.55), (0.3, 0.9, -0.3), 4.0)
             sl["gpu_over_cpu"] = line["slice"]["cells_per_s"] / sl["value"]
             line["slice"]["cpu_baseline"] = sl
+        if "reference_mc_benchmark" in line:
+            rb = cpu_reference_benchmark(128)
+            gb = line["reference_mc_benchmark"]["dim128"]
+            rb["gpu_over_cpu"] = {k: gb[k]["cells_per_s"] / rb[k] for k in ("plain", "remove_duplicates")}
+            line["reference_mc_benchmark"]["cpu_baseline"] = rb
         if "mandelbulb" in line:
             mb = cpu_mandelbulb_baseline(200, 3.0)
             mb["gpu_over_cpu"] = line["mandelbulb"]["n200"]["points_per_s"] / mb["value"]

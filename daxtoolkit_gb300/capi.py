@@ -108,6 +108,8 @@ SIGNATURES = {
     "dax_gb300_mc_counted_generate": ([gp, vp, f32, vp, ctypes.c_int, vp, sz, vp, sz, vp, i64, vp,
                                        i64, vp, vp, vp, vp], i32),
     "dax_gb300_interpolate_point_field_n": ([vp, vp, vp, i64, vp, i64, ctypes.c_int, vp, vp], i32),
+    "dax_gb300_point_magnitude": ([gp, vp, vp], i32),
+    "dax_gb300_write_vtk_polydata": ([ctypes.c_char_p, vp, i64, vp, i64, ctypes.c_int], i32),
     "dax_gb300_mandelbulb_field": ([gp, vp, vp], i32),
     "dax_gb300_mandelbulb_clip_count": ([gp, vp, f32, vp, vp, vp, vp, vp], i32),
     "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),

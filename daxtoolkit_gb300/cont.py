@@ -26,7 +26,8 @@ __all__ = [
     "MarchingTetrahedraCount", "MarchingTetrahedraGenerate", "marching_tetrahedra",
     "Tetrahedralize", "tetrahedralize", "marching_cubes_counted", "Mandlebulb",
     "MandlebulbClipCount", "MandlebulbVolume", "MandlebulbSurface", "mandlebulb_field",
-    "compute_mandlebulb", "colors_and_norms", "extract_surface", "extract_cut",
+    "compute_mandlebulb", "colors_and_norms", "extract_surface", "extract_cut", "point_magnitude",
+    "write_vtk",
 ]
 
 
@@ -430,6 +431,31 @@ def marching_cubes_counted(grid, field, isovalue, count, merge=True, records=Fal
     if records:
         out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
     return out
+
+
+def point_magnitude(grid, stream=None):
+    """DispatcherMapField<Magnitude> over the grid's point coordinates
+    (dax/worklet/Magnitude.h): |coord(p)| for every point, float32 [P]."""
+    g = grid.desc()
+    out = torch.empty(grid.GetNumberOfPoints(), dtype=torch.float32, device="cuda")
+    capi.call("dax_gb300_point_magnitude", ctypes.byref(g), _ptr(out), _stream(stream))
+    return out
+
+
+def write_vtk(path, grid):
+    """The legacy-VTK ASCII POLYDATA file of an UnstructuredGrid of triangles
+    (or other cells), as the reference benchmark's PrintContentsToStream
+    writes it (Benchmarks/MarchingCubes/Pipeline.h:51-98)."""
+    pts = grid.GetPointCoordinates().contiguous()
+    conn = grid.GetCellConnections().contiguous()
+    if pts.dtype != torch.float32 or conn.dtype != torch.int32:
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "points must be float32 and connectivity int32")
+    if pts.is_cuda or conn.is_cuda:
+        torch.cuda.synchronize()
+    V = int(conn.shape[1]) if conn.dim() == 2 else 3
+    capi.call("dax_gb300_write_vtk_polydata", str(path).encode(), _ptr(pts), int(pts.shape[0]),
+              _ptr(conn), int(conn.numel() // V), V)
 
 
 # ---- the Mandelbulb benchmark pipeline (Benchmarks/Mandlebulb) -------------

@@ -743,6 +743,15 @@ int dax_gb300_mc_counted_generate(const dax_gb300_uniform_grid* grid, const floa
   return check_launch("counted merged kernels");
 }
 
+int dax_gb300_point_magnitude(const dax_gb300_uniform_grid* grid, float* d_field, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field");
+  daxgb::launch_point_magnitude(g, d_field, num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("point magnitude kernel");
+}
+
 int dax_gb300_mandelbulb_field(const dax_gb300_uniform_grid* grid, float* d_field, void* stream) {
   Grid g;
   int st = make_grid(grid, g);

@@ -193,6 +193,9 @@ void launch_mc_counted(const Grid& g, const float* f, float iso, const int32_t* 
                        int32_t* tconn, long long tcap, int32_t* ra, int32_t* rb, float* rw,
                        long long T_hint, int num_sms, cudaStream_t s);
 
+// Magnitude of the grid's point coordinates (fields.cu).
+void launch_point_magnitude(const Grid& g, float* out, int num_sms, cudaStream_t s);
+
 // Mandelbulb benchmark pipeline (mandelbulb.cu).
 void launch_mandelbulb_field(const Grid& g, float* out, int num_sms, cudaStream_t s);
 void launch_colors_and_norms(const float* verts, long long nv, float* norms, uint8_t* colors,

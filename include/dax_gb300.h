@@ -297,6 +297,24 @@ int dax_gb300_interpolate_point_field_n(const int32_t* d_rec_first, const int32_
                                         void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Point fields and output                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* DispatcherMapField<Magnitude> over the grid's point coordinates
+ * (dax/worklet/Magnitude.h:27-38): float[P] = |coord(p)|, bit for bit; the
+ * field of the reference's marching-cubes benchmark
+ * (Benchmarks/MarchingCubes/Pipeline.h:100-106).  Asynchronous. */
+int dax_gb300_point_magnitude(const dax_gb300_uniform_grid* grid, float* d_field, void* stream);
+
+/* Legacy-VTK ASCII POLYDATA file of a cell set, byte for byte as the
+ * reference's PrintContentsToStream writes it
+ * (Benchmarks/MarchingCubes/Pipeline.h:51-98): points float[num_points][3],
+ * conn int32[num_cells][verts_per_cell] (3 for triangles), each in device or
+ * host memory.  Blocking; formats on the host cores. */
+int dax_gb300_write_vtk_polydata(const char* path, const float* points, int64_t num_points,
+                                 const int32_t* conn, int64_t num_cells, int verts_per_cell);
+
+/* ------------------------------------------------------------------------ */
 /* The Mandelbulb benchmark's compute pipeline (Benchmarks/Mandlebulb)        */
 /* ------------------------------------------------------------------------ */
 

@@ -76,6 +76,8 @@ class Oracle:
         self._slice_gen.argtypes = [gp, vp, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp,
                                     ctypes.POINTER(i64)]
         self._slice_gen.restype = i64
+        self._magnitude = getattr(L, prefix + "point_magnitude")
+        self._magnitude.argtypes = [gp, vp]
         self._tetra = getattr(L, prefix + "tetrahedralize")
         self._tetra.argtypes = [gp, vp]
         if kind == "port":
@@ -194,6 +196,12 @@ class Oracle:
         V = nv.value
         return dict(verts=verts[:V], conn=conn[:3 * T].reshape(T, 3), rec_a=ra[:V], rec_b=rb[:V],
                     rec_w=rw[:V])
+
+    def point_magnitude(self, g):
+        """Magnitude of every grid point's coordinates."""
+        out = np.zeros(self._points(g), np.float32)
+        self._magnitude(ctypes.byref(g), _ptr(out))
+        return out
 
     def tetrahedralize(self, g):
         """Tetrahedralize over the grid: int32 [5 * cells, 4]."""

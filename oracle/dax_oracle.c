@@ -660,3 +660,17 @@ void orc_mandelbulb_clip_count(const orc_grid* g, const float* field, float iso,
     count[c] = in ? num_faces(classify(val, iso)) : 0;
   }
 }
+
+/* DispatcherMapField<Magnitude> over the grid's point coordinates
+ * (dax/worklet/Magnitude.h:27-38): Sqrt(dot(p, p)). */
+void orc_point_magnitude(const orc_grid* g, float* out) {
+  int64_t d[3];
+  dims_of(g, d);
+  const int64_t P = d[0] * d[1] * d[2];
+  for (int64_t p = 0; p < P; ++p) {
+    float c[3];
+    point_coords(g, d, p, c);
+    out[p] = sqrtf(magsq3(c));
+  }
+}
+

@@ -1,6 +1,6 @@
 // Reference-side CPU driver: runs the DaxToolkit's OWN worklet functors
 // (MarchingCubesCount, MarchingCubesGenerate, SliceCount, SliceGenerate,
-// MarchingTetrahedraCount, MarchingTetrahedraGenerate, Tetrahedralize, ThresholdCount,
+// MarchingTetrahedraCount, MarchingTetrahedraGenerate, Tetrahedralize, Magnitude, ThresholdCount,
 // ThresholdTopology, CellGradient), its TopologyUniform connectivity and
 // point coordinates, its PointAsEdgeInterpolation ordering and dax::math::Lerp, compiled from the reference's headers.  Only the dispatcher
 // layer is restated here (the full dispatcher stack needs Boost.MPL and is not
@@ -18,6 +18,7 @@
 #include <dax/exec/internal/TopologyUniform.h>
 #include <dax/math/VectorAnalysis.h>
 #include <dax/worklet/CellGradient.h>
+#include <dax/worklet/Magnitude.h>
 #include <dax/worklet/MarchingCubes.h>
 #include <dax/worklet/MarchingTetrahedra.h>
 #include <dax/worklet/Slice.h>
@@ -259,6 +260,19 @@ int64_t ref_slice_generate(const RefGrid* g, const float* origin, const float* n
         dax::exec::CellVertices<dax::CellTagVoxel> v = ctx.Verts(cell);
         worklet(v, out, ctx.Coords(v), visit);
       });
+}
+
+// DispatcherMapField<Magnitude> over the grid's point coordinates
+// (dax/worklet/Magnitude.h:27-38).
+void ref_point_magnitude(const RefGrid* g, float* out) {
+  Ctx ctx(g);
+  dax::worklet::Magnitude worklet;
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+  for (dax::Id p = 0; p < ctx.numPoints; ++p) {
+    dax::Scalar v;
+    worklet(ctx.Coord(p), v);
+    out[p] = v;
+  }
 }
 
 // DispatcherGenerateTopology<Tetrahedralize> with a constant count of 5 and
