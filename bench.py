@@ -52,8 +52,11 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=512)
-    p.add_argument("--frames", type=int, default=3,
+    p.add_argument("--frames", type=int, default=4,
                    help="frames in flight (one stream, scratch and output set each)")
+    p.add_argument("--classify-blocks-per-sm", type=int, default=3,
+                   help="per-SM block limit of the classification pass while frames are in "
+                        "flight, leaving room for the other frames' passes (0 = no limit)")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -730,6 +733,9 @@ def main():
         b.record(cur)
         return a, b
 
+    # in flight, the classification leaves room on every SM for the other
+    # frames' count and emit passes (one frame at a time it runs unlimited)
+    capi.call("dax_gb300_set_blocks_per_sm", 0, max(0, args.classify_blocks_per_sm))
     for k in range(max(3, args.warmup) * F):
         frame(k)
     torch.cuda.synchronize()
@@ -757,6 +763,7 @@ def main():
         assert (T2.value, V2.value) == (T, V)
         assert torch.equal(sl["verts"], verts) and torch.equal(sl["conn"], conn)
     # one frame at a time: the single-frame latency
+    capi.call("dax_gb300_set_blocks_per_sm", 0, 0)
     reps1 = max(5, min(args.steps, 300))
     a1, b1 = run_frames(reps1, 1)
     torch.cuda.synchronize()
@@ -833,6 +840,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": dict(config_dict(n), frames_in_flight=F,
+                       classify_blocks_per_sm_in_flight=args.classify_blocks_per_sm,
                        frames_note="each in-flight frame has its own field copy, scratch, "
                                    "outputs and stream; every frame is a complete pass"),
         "ms_per_frame_one_in_flight": ms_one,

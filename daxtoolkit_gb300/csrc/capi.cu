@@ -238,6 +238,13 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
 
 namespace daxgb {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+int g_blocks_per_sm[kTunedPasses] = {0, 0, 0};
+}
+int tuned_blocks_per_sm(int pass) {
+  return pass >= 0 && pass < kTunedPasses ? g_blocks_per_sm[pass] : 0;
+}
 }  // namespace daxgb
 
 // Batched marching cubes plan (host side of dax_gb300_mc_batch).
@@ -266,6 +273,13 @@ struct dax_gb300_mc_batch {
 extern "C" {
 
 int dax_gb300_abi_version(void) { return DAX_GB300_ABI_VERSION; }
+
+int dax_gb300_set_blocks_per_sm(int pass, int blocks) {
+  if (pass < 0 || pass >= daxgb::kTunedPasses || blocks < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "unknown pass or negative block count");
+  daxgb::g_blocks_per_sm[pass] = blocks;
+  return DAX_GB300_SUCCESS;
+}
 
 const char* dax_gb300_last_error(void) { return g_last_error.c_str(); }
 

@@ -121,7 +121,7 @@ void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t
   const long long want = (S.chunks + 4 * 8 - 1) / (4 * 8);  // blocks of 8 warps x 4 chunks
 #define DAXGB_K1(M, V)                                                         \
   {                                                                            \
-    const int blocks = resident_blocks(k_classify_bits<M, V>, 256, 0, num_sms, want); \
+    const int blocks = resident_blocks(k_classify_bits<M, V>, 256, 0, num_sms, want, kPassClassify); \
     k_classify_bits<M, V><<<blocks, 256, 0, s>>>(S, bits, nwords);             \
   }
   if (mode == 0) {

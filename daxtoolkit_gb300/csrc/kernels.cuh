@@ -40,14 +40,26 @@ void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t
 void launch_cell_count(int mode, const Grid& g, const float* f, float a, float b, int32_t* count,
                        uint8_t* cases, int num_sms, cudaStream_t s);
 
+// Per-SM block limits of the marching-cubes passes (dax_gb300_set_blocks_per_sm):
+// 0 = as many as fit.  Below that, a pass leaves room on every SM for the
+// kernels of other frames in flight on other streams.
+enum TunedPass { kPassClassify = 0, kPassCount = 1, kPassEmit = 2, kTunedPasses = 3 };
+int tuned_blocks_per_sm(int pass);
+
 // Blocks of a grid-stride kernel that are resident at once on `num_sms` SMs
-// (never more than `want`): one wave, no tail.
+// (never more than `want`): one wave, no tail.  `pass` >= 0 applies that
+// pass's per-SM limit.
 template <typename K>
-inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long long want) {
+inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long long want,
+                           int pass = -1) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
+  if (pass >= 0) {
+    const int lim = tuned_blocks_per_sm(pass);
+    if (lim > 0 && lim < per_sm) per_sm = lim;
+  }
   const long long cap = (long long)num_sms * per_sm;
   return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }

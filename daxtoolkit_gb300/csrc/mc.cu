@@ -380,7 +380,7 @@ void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* ti
 void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
                     int num_sms, cudaStream_t s) {
   const int tiles = word_scan_tiles(S.rowwords);
-  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles);
+  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles, kPassCount);
   k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
   launch_word_scan(S.rowwords, o.wc, o.tile, o.wt, o.wv, o.act, info, s);
 }
@@ -786,11 +786,11 @@ void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const Wo
   // the active count lives on the device: one resident wave, warp-stride
   const long long want = (S.rowwords + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
   if (merge) {
-    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want);
+    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want, kPassEmit);
     k_mc_emit<true><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
                                                   rb, rw);
   } else {
-    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want);
+    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want, kPassEmit);
     k_mc_emit<false><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
                                                    rb, rw);
   }

@@ -60,6 +60,12 @@ typedef struct dax_gb300_uniform_grid {
 } dax_gb300_uniform_grid;
 
 int dax_gb300_abi_version(void);
+
+/* Per-SM block limit of one marching-cubes pass for later launches in this
+ * process: pass 0 = classification (K1), 1 = count (K2a), 2 = generate (K3);
+ * blocks = 0 restores "as many as fit".  A limit leaves room on every SM for
+ * the passes of other frames running on other streams. */
+int dax_gb300_set_blocks_per_sm(int pass, int blocks);
 const char* dax_gb300_last_error(void);
 
 /* Blocks until all work on `stream` is done and reports any sticky CUDA
