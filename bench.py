@@ -14,9 +14,10 @@ Reported:
                outputs, so one frame's bandwidth-bound classification overlaps
                the latency-bound count/scan/emit of the previous ones; the
                one-frame-at-a-time time is reported beside it
-  e2e          the same metric through the public API from pinned host memory:
-               H2D field copy + marching_cubes() (count, host sizing, generate)
-               + D2H of vertices and connectivity, every step
+  e2e          the same metric through the C ABI from page-locked host memory: every
+               step copies its whole field to the device, sizes, generates and
+               copies the surface back to host memory; two steps in flight on
+               their own streams and buffers
   roofline     dominant kernel (K1 point classification): algorithmic bytes
                4P read + P/8 written per launch over its CUDA-event time
   cpu_baseline the CPU implementation on a bounded z-slab sample of the same
@@ -812,26 +813,70 @@ def main():
     # copy would move, in one pass instead of copy-then-read), the emit kernel
     # reads crossing-edge values from it, and the surface comes back to
     # page-locked host buffers.
-    host_field = torch.empty(P, dtype=torch.float32, pin_memory=True)
-    host_field.copy_(field.cpu())
-    host_v = torch.empty((V, 3), dtype=torch.float32, pin_memory=True)
-    host_c = torch.empty((T, 3), dtype=torch.int32, pin_memory=True)
+    # End to end through the C ABI from page-locked host memory: every step
+    # copies its whole 512^3 field from page-locked host memory to the device,
+    # sizes its outputs from the totals, generates and copies the surface back
+    # to page-locked host memory.  Two steps are in flight on their own
+    # streams, each with its own host field, device copy, scratch and outputs:
+    # step k+1's field crosses the host link while step k sizes, generates and
+    # copies its surface out the other way.
+    E = 2
+    hf0 = field.cpu()
+    eslots = []
+    for q in range(E):
+        hf = torch.empty(P, dtype=torch.float32, pin_memory=True)
+        hf.copy_(hf0)
+        eslots.append(dict(
+            host=hf, dfield=torch.empty(P, dtype=torch.float32, device=dev),
+            scratch=torch.empty(nbytes, dtype=torch.uint8, device=dev),
+            verts=torch.empty((V, 3), dtype=torch.float32, device=dev),
+            conn=torch.empty((T, 3), dtype=torch.int32, device=dev),
+            hv=torch.empty((V, 3), dtype=torch.float32, pin_memory=True),
+            hc=torch.empty((T, 3), dtype=torch.int32, pin_memory=True),
+            stream=torch.cuda.Stream(device=dev)))
+    for q in eslots:
+        q["s"] = ctypes.c_void_p(q["stream"].cuda_stream)
+    del hf0
 
-    def e2e_step():
-        out = cont.marching_cubes(grid, host_field, iso, merge=True)
-        host_v.copy_(out["verts"], non_blocking=True)
-        host_c.copy_(out["conn"], non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+    def e2e_count(q):
+        with torch.cuda.stream(q["stream"]):
+            q["dfield"].copy_(q["host"], non_blocking=True)
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(q["dfield"]), iso, ptr(q["scratch"]),
+                  nbytes, q["s"])
+
+    def e2e_finish(q):
+        Tq, Vq = ctypes.c_int64(0), ctypes.c_int64(0)
+        capi.call("dax_gb300_mc_totals", ptr(q["scratch"]), ctypes.byref(Tq), ctypes.byref(Vq),
+                  q["s"])
+        assert (Tq.value, Vq.value) == (T, V)
+        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(q["dfield"]), iso, 1,
+                  ptr(q["scratch"]), nbytes, ptr(q["verts"]), Vq.value, ptr(q["conn"]), Tq.value,
+                  None, None, None, q["s"])
+        with torch.cuda.stream(q["stream"]):
+            q["hv"].copy_(q["verts"], non_blocking=True)
+            q["hc"].copy_(q["conn"], non_blocking=True)
+
+    def e2e_run(steps):
+        pending = None
+        for k in range(steps):
+            q = eslots[k % E]
+            e2e_count(q)               # enqueued before the host waits on the previous step
+            if pending is not None:
+                e2e_finish(pending)
+            pending = q
+        e2e_finish(pending)
+        for q in eslots:
+            q["stream"].synchronize()
 
     e2e_steps = max(3, min(args.steps, 50))
-    for _ in range(2):
-        e2e_step()
+    e2e_run(2 * E)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
+    e2e_run(e2e_steps)
     barrier()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    for q in eslots:
+        assert torch.equal(q["hv"], verts.cpu()) and torch.equal(q["hc"], conn.cpu())
     e2e_value = world * C / t_e2e
 
     line = {
@@ -857,7 +902,9 @@ def main():
                       "generate": t_gen},
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 4 * P,
                 "d2h_bytes_per_step": 12 * V + 12 * T, "ms_per_step": 1e3 * t_e2e,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "steps_in_flight": E,
+                "path": "C ABI; per step the field is copied from page-locked host memory to the "
+                        "device and the surface back to page-locked host memory"},
         # K1, K2a, K2b and K3 per step
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,

@@ -23,7 +23,7 @@ LIB = os.path.join(LIBDIR, "libdax_gb300.so")
 
 SOURCES = ["classify.cu", "mc.cu", "threshold.cu", "gradient.cu", "adjoint.cu", "capi.cu",
            "noalloc.cu", "primitives.cu", "slice.cu", "mt.cu",
-           "mandelbulb.cu", "fields.cu", "vtk.cu"]
+           "mandelbulb.cu", "fields.cu", "vtk.cu", "selftest.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "mc_case.cuh", "mc_tables.h", "mt_tables.h",
            "coolwarm_table.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

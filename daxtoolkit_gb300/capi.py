@@ -114,6 +114,8 @@ SIGNATURES = {
     "dax_gb300_mandelbulb_clip_count": ([gp, vp, f32, vp, vp, vp, vp, vp], i32),
     "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),
     "dax_gb300_set_blocks_per_sm": ([ctypes.c_int, ctypes.c_int], i32),
+    "dax_gb300_selfcheck_division": ([vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
+                                      ctypes.c_uint32, vp, vp], i32),
     "dax_gb300_scan_scratch_bytes": ([i64], sz),
     "dax_gb300_scan": ([vp, vp, i64, i32, i32, vp, sz, vp, vp], i32),
     "dax_gb300_sort_scratch_bytes": ([i64, i32, i32], sz),

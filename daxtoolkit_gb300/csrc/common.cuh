@@ -139,6 +139,29 @@ __device__ __forceinline__ float coord(float o, float s, int i, int m) {
   return __fadd_rn(o, __fmul_rn(s, (float)(i + m)));
 }
 
+// Division by a divisor d used many times, from its correctly rounded
+// reciprocal r = recip_or_zero(d): q = RN(x r), e = x - q d (exact with one
+// fused multiply-add), result RN(q + e r).  With r within half an ulp of 1/d
+// and q within one ulp of x/d this is the correctly rounded x / d (P.
+// Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Develop. 34(1), 1990; J.-M. Muller et al.,
+// Handbook of Floating-Point Arithmetic, 2010, Markstein's theorem), provided
+// no intermediate leaves the normal range: outside 2^-90 < |x|, |q| < 2^90
+// (and for r = 0, a divisor outside that band) it falls back to __fdiv_rn;
+// x = 0 gives the signed zero x r directly.
+__device__ __forceinline__ float recip_or_zero(float d) {
+  const float a = fabsf(d);
+  return (a > 0x1p-90f && a < 0x1p90f) ? __frcp_rn(d) : 0.0f;
+}
+__device__ __forceinline__ float div_by_recip(float x, float d, float r) {
+  const float q = __fmul_rn(x, r);
+  const float ax = fabsf(x), aq = fabsf(q);
+  if (ax > 0x1p-90f && ax < 0x1p90f && aq > 0x1p-90f && aq < 0x1p90f)
+    return __fmaf_rn(__fmaf_rn(-q, d, x), r, q);
+  if (x == 0.0f && r != 0.0f) return q;
+  return __fdiv_rn(x, d);
+}
+
 // dax::math::Lerp(a, b, w) = a + w * (b - a), dax/math/VectorAnalysis.h:35-50.
 __device__ __forceinline__ float lerp_rn(float a, float b, float w) {
   return __fadd_rn(a, __fmul_rn(w, __fsub_rn(b, a)));

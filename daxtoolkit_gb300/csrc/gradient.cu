@@ -12,11 +12,17 @@
 // +x corners of lane 30's cells, and every +x neighbour comes from the next
 // lane) and keeps the previous plane in registers, so every field value is
 // read from HBM once (plus the band's halo row and the segment's halo
-// plane).  Each lane writes its cell's 12 bytes as one 8-byte store on the
-// 8-byte-aligned half plus one 4-byte store.  (Staging a row through shared
-// memory into fully coalesced stores measured slower on GB300: the warp
-// synchronisation behind the correctly rounded divides costs more than the
-// partial sectors save.)  Algorithmic traffic: 4 B/point + 12 B/cell.
+// plane).  While every value in the two planes is 0 or at least 2^-124 in
+// magnitude (products by +-0.25 exact), the weighted sums use fused
+// multiply-adds, which then round exactly like the reference's separate
+// multiply and add; otherwise the separate operations run.  The three
+// divisions by the cell widths use the widths' correctly rounded
+// reciprocals, one per column, row and plane, with a correction step that
+// keeps each quotient the correctly rounded one (div_by_recip).  Each lane
+// writes its cell's 12 bytes as one 8-byte store on the 8-byte-aligned half
+// plus one 4-byte store.  (Staging a row through shared memory into fully
+// coalesced stores measured slower on GB300, 0.63 against 0.57 ms at 512^3.)
+// Algorithmic traffic: 4 B/point + 12 B/cell.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -43,6 +49,19 @@ __device__ __forceinline__ void load_point_plane(const Grid& g, const float* __r
   }
 }
 
+// True when every value v of the plane is 0 or has |v| >= 2^-124: then
+// v * (+-0.25) is exact, and a fused multiply-add of it rounds exactly like
+// the reference's multiply-then-add.
+__device__ __forceinline__ bool plane_exact_quarter(const float (&F)[kGradBand + 1]) {
+  bool ok = true;
+#pragma unroll
+  for (int t = 0; t <= kGradBand; ++t) {
+    const float a = fabsf(F[t]);
+    ok = ok && (a == 0.0f || a >= 0x1p-124f);
+  }
+  return ok;
+}
+
 __global__ void __launch_bounds__(kMarchWarps * 32, kGradMinBlocks)
     k_cell_gradient(Grid g, const float* __restrict__ f, float* __restrict__ out, MarchTiles mt) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -57,17 +76,33 @@ __global__ void __launch_bounds__(kMarchWarps * 32, kGradMinBlocks)
   const bool own = lane < kMarchCols && i < cx;
   const int j0 = band * kGradBand;
   const int k0 = seg * kSeg, k1 = min(k0 + kSeg, cz);
+  // the cell widths and their reciprocals: one per column, per row of the
+  // band, per plane
   const float wx =
       own ? __fsub_rn(coord(g.ox, g.sx, i + 1, g.mx), coord(g.ox, g.sx, i, g.mx)) : 1.0f;
+  const float rx = recip_or_zero(wx);
+  float wy[kGradBand], ry[kGradBand];
+#pragma unroll
+  for (int t = 0; t < kGradBand; ++t) {
+    wy[t] = __fsub_rn(coord(g.oy, g.sy, j0 + t + 1, g.my), coord(g.oy, g.sy, j0 + t, g.my));
+    ry[t] = recip_or_zero(wy[t]);
+  }
 
   float F0[kGradBand + 1], F1[kGradBand + 1];
   load_point_plane(g, f, i, j0, k0, F0);
+  bool ok0 = plane_exact_quarter(F0);
   for (int kc = k0; kc < k1; ++kc) {
     load_point_plane(g, f, i, j0, kc + 1, F1);
+    const bool ok1 = plane_exact_quarter(F1);
+    // warp-uniform: the weighted sums may use fused multiply-adds
+    const bool fused = __all_sync(kFull, ok0 && ok1);
     const float wz = __fsub_rn(coord(g.oz, g.sz, kc + 1, g.mz), coord(g.oz, g.sz, kc, g.mz));
+    const float rz = recip_or_zero(wz);
     // row t of both planes at columns i and i + 1, carried from row to row
     float a0 = F0[0], b0 = F1[0];
     float a0n = __shfl_down_sync(kFull, a0, 1), b0n = __shfl_down_sync(kFull, b0, 1);
+    float* o = out + 3 * ((long long)i + (long long)cx * (j0 + (long long)cy * kc));
+    bool even = ((i + (long long)cx * (j0 + (long long)cy * kc)) & 1) == 0;
 #pragma unroll
     for (int t = 0; t < kGradBand; ++t) {
       const int jc = j0 + t;
@@ -77,24 +112,34 @@ __global__ void __launch_bounds__(kMarchWarps * 32, kGradMinBlocks)
       if (own) {
         const float v[8] = {a0, a0n, a1n, a1, b0, b0n, b1n, b1};
         float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        if (fused) {
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          sx = __fadd_rn(sx, __fmul_rn(v[n], dw(kNegX, n)));
-          sy = __fadd_rn(sy, __fmul_rn(v[n], dw(kNegY, n)));
-          sz = __fadd_rn(sz, __fmul_rn(v[n], dw(kNegZ, n)));
+          for (int n = 0; n < 8; ++n) {
+            sx = __fmaf_rn(v[n], dw(kNegX, n), sx);
+            sy = __fmaf_rn(v[n], dw(kNegY, n), sy);
+            sz = __fmaf_rn(v[n], dw(kNegZ, n), sz);
+          }
+        } else {
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            sx = __fadd_rn(sx, __fmul_rn(v[n], dw(kNegX, n)));
+            sy = __fadd_rn(sy, __fmul_rn(v[n], dw(kNegY, n)));
+            sz = __fadd_rn(sz, __fmul_rn(v[n], dw(kNegZ, n)));
+          }
         }
-        const float wy = __fsub_rn(coord(g.oy, g.sy, jc + 1, g.my), coord(g.oy, g.sy, jc, g.my));
-        const long long c = (long long)i + (long long)cx * (jc + (long long)cy * kc);
-        float* o = out + 3 * c;
-        const float gx = __fdiv_rn(sx, wx), gy = __fdiv_rn(sy, wy), gz = __fdiv_rn(sz, wz);
-        if ((c & 1) == 0) {  // byte offset 12 c is 8-byte aligned
+        // the correctly rounded quotients (div_by_recip is exact: common.cuh)
+        const float gx = div_by_recip(sx, wx, rx), gy = div_by_recip(sy, wy[t], ry[t]),
+                    gz = div_by_recip(sz, wz, rz);
+        if (even) {  // byte offset 12 c is 8-byte aligned
           *reinterpret_cast<float2*>(o) = make_float2(gx, gy);
           o[2] = gz;
-        } else {             // byte offset 12 c + 4 is 8-byte aligned
+        } else {     // byte offset 12 c + 4 is 8-byte aligned
           o[0] = gx;
           *reinterpret_cast<float2*>(o + 1) = make_float2(gy, gz);
         }
       }
+      o += 3 * (long long)cx;
+      even = even == ((cx & 1) == 0);
       a0 = a1;
       a0n = a1n;
       b0 = b1;
@@ -102,6 +147,7 @@ __global__ void __launch_bounds__(kMarchWarps * 32, kGradMinBlocks)
     }
 #pragma unroll
     for (int t = 0; t <= kGradBand; ++t) F0[t] = F1[t];
+    ok0 = ok1;
   }
 }
 

@@ -66,6 +66,16 @@ int dax_gb300_abi_version(void);
  * blocks = 0 restores "as many as fit".  A limit leaves room on every SM for
  * the passes of other frames running on other streams. */
 int dax_gb300_set_blocks_per_sm(int pass, int blocks);
+
+/* Self-check of the reciprocal-based division the stencil kernels use
+ * (Markstein's correction step) against CUDA's correctly rounded division:
+ * the numerators with bit patterns first + i * step (i < count <= 2^32,
+ * modulo 2^32) against each of the num_divisors divisors (device memory);
+ * *d_mismatches (device, caller-zeroed) gets the number of results whose bits
+ * differ.  Asynchronous. */
+int dax_gb300_selfcheck_division(const float* d_divisors, int num_divisors, uint32_t first,
+                                 uint64_t count, uint32_t step, unsigned long long* d_mismatches,
+                                 void* stream);
 const char* dax_gb300_last_error(void);
 
 /* Blocks until all work on `stream` is done and reports any sticky CUDA
