@@ -113,6 +113,7 @@ SIGNATURES = {
     "dax_gb300_mandelbulb_field": ([gp, vp, vp], i32),
     "dax_gb300_mandelbulb_clip_count": ([gp, vp, f32, vp, vp, vp, vp, vp], i32),
     "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),
+    "dax_gb300_report_error": ([ctypes.c_int, ctypes.c_char_p], i32),
     "dax_gb300_set_blocks_per_sm": ([ctypes.c_int, ctypes.c_int], i32),
     "dax_gb300_selfcheck_division": ([vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
                                       ctypes.c_uint32, vp, vp], i32),

@@ -283,6 +283,11 @@ int dax_gb300_set_blocks_per_sm(int pass, int blocks) {
 
 const char* dax_gb300_last_error(void) { return g_last_error.c_str(); }
 
+int dax_gb300_report_error(int code, const char* message) {
+  g_last_error = message ? message : "";
+  return code;
+}
+
 int dax_gb300_synchronize(void* stream) {
   cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
   if (e == cudaSuccess) e = cudaGetLastError();

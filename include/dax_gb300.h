@@ -78,6 +78,11 @@ int dax_gb300_selfcheck_division(const float* d_divisors, int num_divisors, uint
                                  void* stream);
 const char* dax_gb300_last_error(void);
 
+/* Sets the message dax_gb300_last_error() returns on this thread and returns
+ * code: the error path of the header-only parts of the adapter
+ * (dax_gb300_schedule.cuh). */
+int dax_gb300_report_error(int code, const char* message);
+
 /* Blocks until all work on `stream` is done and reports any sticky CUDA
  * error.  Replaces DeviceAdapterAlgorithm<Tag>::Synchronize
  * (dax/cuda/cont/internal/DeviceAdapterAlgorithmCuda.h:40-43). */
