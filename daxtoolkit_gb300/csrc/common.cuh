@@ -162,6 +162,26 @@ __device__ __forceinline__ float div_by_recip(float x, float d, float r) {
   return __fdiv_rn(x, d);
 }
 
+__device__ __forceinline__ unsigned mag_bits(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+
+// Divisor band of div_fast: 2^-30 <= |w| < 2^30 (magnitude bit patterns).
+constexpr unsigned kFastWidthLo = 0x30800000u;
+constexpr unsigned kFastWidthHi = 0x4e800000u;
+__device__ __forceinline__ bool width_in_band(float w) {
+  return mag_bits(w) - kFastWidthLo < kFastWidthHi - kFastWidthLo;
+}
+
+// x / w for x = 0 or 2^-85 <= |x| < 2^87 and 2^-30 <= |w| < 2^30 with
+// r = RN(1/w): div_by_recip's correction step without its range checks
+// (every intermediate is normal on that domain).  The sign comes from
+// q = RN(x r), which is the correctly signed zero when x is +-0 (where the
+// correction step alone would give +0 for x = -0).
+__device__ __forceinline__ float div_fast(float x, float w, float r) {
+  const float q = __fmul_rn(x, r);
+  const float y = __fmaf_rn(__fmaf_rn(-q, w, x), r, q);
+  return __uint_as_float(mag_bits(y) | (__float_as_uint(q) & 0x80000000u));
+}
+
 // dax::math::Lerp(a, b, w) = a + w * (b - a), dax/math/VectorAnalysis.h:35-50.
 __device__ __forceinline__ float lerp_rn(float a, float b, float w) {
   return __fadd_rn(a, __fmul_rn(w, __fsub_rn(b, a)));

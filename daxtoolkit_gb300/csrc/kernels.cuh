@@ -107,7 +107,8 @@ void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const 
                      const uint32_t* used, Info* info, int32_t* conn, long long kcap,
                      float* coords, float* fout, long long ucap, int num_sms, cudaStream_t s);
 
-// z-marching stencil kernels (CellGradient and its adjoint): one warp per
+// z-marching stencil kernels (the adjoint; CellGradient has its own tile
+// constants below): one warp per
 // tile of kMarchCols columns in x (the 32nd lane supplies the +x/-x
 // neighbour column), a band of rows in y and kSeg planes in z, marched
 // along z; kMarchWarps warps (independent tiles) per block.  Band heights
@@ -116,6 +117,8 @@ constexpr int kMarchCols = 31;
 constexpr int kSeg = 32;
 constexpr int kMarchWarps = 8;
 constexpr int kGradBand = 4;        // cell rows per CellGradient tile
+constexpr int kGradSeg = 16;        // cell planes per CellGradient tile
+constexpr int kGradWarps = 4;       // CellGradient tiles (warps) per block
 constexpr int kGradMinBlocks = 4;
 constexpr int kAdjBand = 8;         // point rows per adjoint tile
 constexpr int kAdjMinBlocks = 3;

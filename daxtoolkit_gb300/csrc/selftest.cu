@@ -1,7 +1,9 @@
 // Self-check of div_by_recip against __fdiv_rn: the numerators with bit
 // patterns first + i * step (i < count, modulo 2^32) against each given
 // divisor, counting the results whose bits differ (NaN results count as
-// equal to each other).  Used by the tests to
+// equal to each other).  Where the numerator and the divisor lie in
+// div_fast's domain (x = 0 or 2^-85 <= |x| < 2^87, 2^-30 <= |d| < 2^30),
+// div_fast is checked against __fdiv_rn too.  Used by the tests to
 // show, exhaustively over the numerators, that the reciprocal-based division
 // of the stencil kernels is the correctly rounded one for the divisors a grid
 // produces.
@@ -22,10 +24,14 @@ __global__ void __launch_bounds__(256) k_division_check(const float* __restrict_
     const unsigned long long di = t / count, i = t - di * count;
     const float d = __ldg(divisors + di);
     const float x = __uint_as_float(first + (unsigned)i * step);
-    const float a = div_by_recip(x, d, recip_or_zero(d));
+    const float r = recip_or_zero(d);
+    const float a = div_by_recip(x, d, r);
     const float b = __fdiv_rn(x, d);
     const bool same = __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
     bad += same ? 0ull : 1ull;
+    const unsigned ux = mag_bits(x);
+    if (width_in_band(d) && (ux == 0u || (ux >= 0x15000000u && ux < 0x6b000000u)))
+      bad += __float_as_uint(div_fast(x, d, r)) == __float_as_uint(b) ? 0ull : 1ull;
   }
   bad += __shfl_xor_sync(kFull, bad, 16);
   bad += __shfl_xor_sync(kFull, bad, 8);

@@ -49,6 +49,35 @@ def sphere(dims, noise=0.01, seed=1234):
     return (r + noise * rng.uniform(-1, 1, size=r.shape)).astype(np.float32).ravel()
 
 
+def wide_exponent_field(dims, seed):
+    """Values of random sign whose exponents spread over the whole float32
+    range, by thirds of the z-planes: magnitudes in [2^-60, 2^86) (the band in
+    which the GPU gradient takes its fused path), then down to subnormals,
+    then up to 2^128 with infinities and NaNs; +0 and -0 throughout, and the
+    band's edge values 2^-60, 2^86 and their neighbours placed explicitly."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = dims
+    n = nx * ny
+    third = max(nz // 3, 1)
+    f = np.empty((nz, n), np.float32)
+    for k in range(nz):
+        lo, hi = (-60, 86) if k < third else ((-150, -40) if k < 2 * third else (40, 128))
+        m = np.exp2(rng.uniform(lo, hi, n)).astype(np.float32)
+        m = np.where(rng.uniform(size=n) < 0.5, -m, m).astype(np.float32)
+        z = rng.uniform(size=n)
+        m[z < 0.08] = 0.0
+        m[(z >= 0.08) & (z < 0.11)] = -0.0
+        f[k] = m
+    edges = np.array([2.0 ** -60, -(2.0 ** -60), np.nextafter(np.float32(2.0 ** 86), np.float32(0))],
+                     np.float32)
+    f[1, :edges.size] = edges
+    f[third, :4] = np.array([np.nextafter(np.float32(2.0 ** -60), np.float32(0)), 2.0 ** 86,
+                             -(2.0 ** 86), 2.0 ** -126], np.float32)
+    if nz > 2 * third:
+        f[2 * third, :3] = np.array([np.inf, -np.inf, np.nan], np.float32)
+    return f.ravel()
+
+
 def mc_cases():
     """(name, dims, origin, spacing, extent_min, field, isovalue)."""
     out = []
@@ -122,6 +151,19 @@ def gradient_cases():
     out.append(("exact_tiles_33x9x34", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 3, 18)))
     out.append(("single_cell", (2, 2, 2), (0.5, 0.5, 0.5), (2.0, 3.0, 4.0), (0, 0, 0),
                 np.arange(8, dtype=np.float32) ** 2))
+    # exponents over the whole float32 range: both of the GPU kernel's paths,
+    # chosen plane by plane, within one grid (2 column tiles, ragged bands, 2
+    # plane segments)
+    d = (40, 11, 37)
+    out.append(("wide_exponents_40x11x37", d, (0, 0, 0), (1, 1, 1), (0, 0, 0),
+                wide_exponent_field(d, 29)))
+    # cell widths at the edges of the fused path's width band [2^-30, 2^30)
+    # and outside it (1e-12 in x, 3e9 in y, exactly 2^30 in z)
+    d = (35, 9, 6)
+    out.append(("widths_in_band_edges", d, (0, 0, 0), (2.0 ** -30, 0.75 * 2.0 ** 30, 1.0), (0, 0, 0),
+                random_blobs(d, 3, 31, noise=0.05)))
+    out.append(("widths_outside_band", d, (0, 0, 0), (1e-12, 3e9, 2.0 ** 30), (0, 0, 0),
+                random_blobs(d, 3, 32, noise=0.05)))
     return out
 
 

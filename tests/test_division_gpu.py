@@ -1,5 +1,6 @@
-"""The reciprocal-based division of the stencil kernels (Markstein's
-correction step on a correctly rounded reciprocal) against CUDA's correctly
+"""The reciprocal-based divisions of the stencil kernels (Markstein's
+correction step on a correctly rounded reciprocal: div_by_recip with its
+range checks, and div_fast on its narrower domain) against CUDA's correctly
 rounded division, exhaustively over all 2^32 numerator bit patterns, for
 every divisor a gradient launch uses on the bench grid and the gradient test
 grids: the differences of neighbouring implicit coordinates along each axis."""
@@ -30,7 +31,9 @@ def _divisors():
                 w = _axis_steps(dims[a], origin[a], spacing[a], emin[a])
                 steps.update(w.view(np.uint32).tolist())
     # plus divisors near the band limits and of every binade's extremes
-    extra = [2.0 ** -89, 2.0 ** 89, 1.0, 1.5, 1.9999999, 3.0, 0.1, 1 / 3, 7e-20, 3e19]
+    extra = [2.0 ** -89, 2.0 ** 89, 1.0, 1.5, 1.9999999, 3.0, 0.1, 1 / 3, 7e-20, 3e19,
+             2.0 ** -30, -(2.0 ** -30), np.nextafter(np.float32(2.0 ** 30), np.float32(0)),
+             0.75 * 2.0 ** 30, -1.75e-9]
     steps.update(np.asarray(extra, np.float32).view(np.uint32).tolist())
     return np.array(sorted(steps), np.uint32).view(np.float32)
 

@@ -130,6 +130,26 @@ def test_cell_gradient(gb300, oracle_best, case):
     assert np.array_equal(_bits(out.cpu().numpy()), _bits(ref))
 
 
+def test_cell_gradient_unaligned_output(gb300, oracle_best):
+    """An output pointer that is 4- but not 8-byte aligned (the kernel's
+    scalar-store variant) gives the same bits."""
+    import ctypes
+    from daxtoolkit_gb300 import capi
+    name, dims, origin, spacing, emin, f = cases.gradient_cases()[3]
+    cont = gb300
+    ref = oracle_best.cell_gradient(_ogrid(dims, origin, spacing, emin), f)
+    grid = _grid(cont, dims, origin, spacing, emin)
+    fd = torch.from_numpy(f).cuda()
+    buf = torch.full((ref.size + 2,), -7.0, device="cuda")
+    out = buf[1:1 + ref.size]
+    assert out.data_ptr() % 8 == 4
+    capi.call("dax_gb300_cell_gradient", ctypes.byref(grid.desc()), ctypes.c_void_p(fd.data_ptr()),
+              ctypes.c_void_p(out.data_ptr()), None)
+    torch.cuda.synchronize()
+    assert np.array_equal(_bits(out.cpu().numpy().reshape(ref.shape)), _bits(ref))
+    assert buf[0].item() == -7.0 and buf[-1].item() == -7.0
+
+
 def test_capacity_error_writes_nothing(gb300):
     """A too-small output buffer is reported, and nothing is written."""
     import ctypes
