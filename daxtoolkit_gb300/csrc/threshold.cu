@@ -13,9 +13,11 @@
 // K2b (k_word_scan, shared with marching cubes): per-word exclusive offsets
 //     wt (kept cells) and wv (used points), the compacted list act of the
 //     words with either, and the totals.
-// K3 (k_thr_emit): a warp loads 32 active words at once (lane = word), then
-//     walks them with lane = bit: the word's used points (coordinates and
-//     field: StreamCompact with the point mask, :237-239 and :98-113) and
+// K3 (k_thr_emit): a warp loads 32 active words at once (lane = word),
+//     starts the copies of the field values of all their used points into
+//     shared memory (cp.async, one wait per batch), then walks the words
+//     with lane = bit: the word's used points (coordinates and field:
+//     StreamCompact with the point mask, :237-239 and :98-113) and
 //     its kept cells, whose 8 corner ids are each corner's rank among the
 //     used points.  That equals the reference's Copy/Sort/Unique/LowerBounds
 //     of the connectivity (:229-258), because the used ids sorted ascending
@@ -35,7 +37,7 @@ __device__ __forceinline__ uint32_t bits_at_u32(const uint32_t* __restrict__ bit
 __global__ void __launch_bounds__(256) k_thr_kept(Grid g, const uint32_t* __restrict__ bits,
                                                   uint32_t* __restrict__ kept) {
   const uint32_t W = (uint32_t)(g.R * g.wr);  // < 2^27 for grids below 2^31 points
-  const uint32_t wr = (uint32_t)g.wr, nx = (uint32_t)g.nx;
+  const uint32_t nx = (uint32_t)g.nx;
   const uint32_t dy = nx, dz = nx * (uint32_t)g.ny;
   for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
     int mi, ji, ki;
@@ -141,6 +143,8 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
   const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const unsigned wr = (unsigned)g.wr;
+  __shared__ float s_field[8][32][32];  // per warp: field value of bit `lane` of batch word s
+  float (*const sf)[32] = s_field[threadIdx.x >> 5];
   for (long long a0 = warp0 * 32; a0 < A; a0 += nwarps * 32) {
     // lane L gathers active word a0 + L
     ThrWord d{};
@@ -171,6 +175,24 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
         }
       }
     }
+    if (fout) {
+      // the field values of the batch's used points, all copies in flight at
+      // once (a field read is a DRAM round trip: K1 streamed it evict-first)
+      for (int s = 0; s < cnt; ++s) {
+        const uint32_t w = __shfl_sync(kFull, d.w, s);
+        const uint32_t u = __shfl_sync(kFull, d.u, s);
+        int mi;
+        const uint32_t r = split_word(g, w, mi);
+        const bool on = (u >> lane) & 1u;
+        const float* src = on ? f + ((long long)r * g.nx + 32 * mi + lane) : f;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&sf[s][lane]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
+                     "r"(on ? 4 : 0)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
     for (int s = 0; s < cnt; ++s) {
       const uint32_t w = __shfl_sync(kFull, d.w, s);
       const uint32_t u = __shfl_sync(kFull, d.u, s);
@@ -180,7 +202,6 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       const uint32_t m = (uint32_t)mi;
       split_row(g, r, j, k);
       const int i = 32 * (int)m + lane;
-      const long long p = (long long)r * g.nx + i;
       const uint32_t v0 = __shfl_sync(kFull, d.v0, s);
       if ((u >> lane) & 1u) {
         const long long id = (long long)v0 + __popc(u & below);
@@ -188,7 +209,7 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
         c[0] = coord(g.ox, g.sx, i, g.mx);
         c[1] = coord(g.oy, g.sy, j, g.my);
         c[2] = coord(g.oz, g.sz, k, g.mz);
-        if (fout) fout[id] = __ldg(f + p);
+        if (fout) fout[id] = sf[s][lane];
       }
       if (kw == 0u) continue;  // uniform across the warp
       const uint32_t t0 = __shfl_sync(kFull, d.t0, s);
