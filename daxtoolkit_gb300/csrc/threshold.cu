@@ -118,6 +118,7 @@ void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint3
 // q = dj + 2 dk (q = 1..3) at word m, and rows q = 0..3 at word m + 1.
 struct ThrWord {
   uint32_t w, u, kw, v0, t0;
+  uint32_t r, m, j, k;  // the word's point row (j, k) and word index in the row
   uint32_t cu[7], cv[7];
 };
 
@@ -155,10 +156,14 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       d.kw = __ldg(kept + d.w);
       d.v0 = __ldg(wv + d.w);
       d.t0 = __ldg(wt + d.w);
+      int mi, ji, ki;
+      d.r = split_word(g, d.w, mi);
+      split_row(g, d.r, ji, ki);
+      d.m = (uint32_t)mi;
+      d.j = (uint32_t)ji;
+      d.k = (uint32_t)ki;
       if (d.kw) {  // a kept cell implies rows j + 1 and k + 1 exist
-        int mi;
-        split_word(g, d.w, mi);
-        const unsigned m = (unsigned)mi;
+        const unsigned m = d.m;
         const uint32_t rows[4] = {d.w, d.w + wr, d.w + (unsigned)g.ny * wr,
                                   d.w + (unsigned)(g.ny + 1) * wr};
 #pragma unroll
@@ -179,12 +184,10 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       // the field values of the batch's used points, all copies in flight at
       // once (a field read is a DRAM round trip: K1 streamed it evict-first)
       for (int s = 0; s < cnt; ++s) {
-        const uint32_t w = __shfl_sync(kFull, d.w, s);
         const uint32_t u = __shfl_sync(kFull, d.u, s);
-        int mi;
-        const uint32_t r = split_word(g, w, mi);
+        const uint32_t r = __shfl_sync(kFull, d.r, s), m = __shfl_sync(kFull, d.m, s);
         const bool on = (u >> lane) & 1u;
-        const float* src = on ? f + ((long long)r * g.nx + 32 * mi + lane) : f;
+        const float* src = on ? f + ((long long)r * g.nx + 32 * m + lane) : f;
         const unsigned dst = (unsigned)__cvta_generic_to_shared(&sf[s][lane]);
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
                      "r"(on ? 4 : 0)
@@ -194,13 +197,10 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
     for (int s = 0; s < cnt; ++s) {
-      const uint32_t w = __shfl_sync(kFull, d.w, s);
       const uint32_t u = __shfl_sync(kFull, d.u, s);
       const uint32_t kw = __shfl_sync(kFull, d.kw, s);
-      int mi, j, k;
-      const uint32_t r = split_word(g, w, mi);
-      const uint32_t m = (uint32_t)mi;
-      split_row(g, r, j, k);
+      const uint32_t m = __shfl_sync(kFull, d.m, s);
+      const int j = (int)__shfl_sync(kFull, d.j, s), k = (int)__shfl_sync(kFull, d.k, s);
       const int i = 32 * (int)m + lane;
       const uint32_t v0 = __shfl_sync(kFull, d.v0, s);
       if ((u >> lane) & 1u) {
@@ -223,25 +223,18 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       }
       if ((kw >> lane) & 1u) {
         const long long cid = (long long)t0 + __popc(kw & below);
-        int32_t ids[8];
+        // used-point ranks of the corners at i (lo) and i + 1 (hi) of corner
+        // rows q = dj + 2 dk: hi = lo + the bit of point i, except on lane
+        // 31, whose i + 1 is bit 0 of word m + 1
+        int32_t lo[4], hi[4];
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
-          // v0..v7: (i,j,k) (i+1,j,k) (i+1,j+1,k) (i,j+1,k), then the same at k+1
-          const int di = ((v & 3) == 1 || (v & 3) == 2) ? 1 : 0;
-          const int dj = ((v & 3) >= 2) ? 1 : 0;
-          const int q = dj + 2 * (v >> 2);
-          uint32_t uq = cu[q], vq = cv[q], lm = below;
-          if (di) {
-            if (lane == 31) {  // corner i + 1 is bit 0 of word m + 1
-              uq = cu[4 + q];
-              vq = cv[4 + q];
-              lm = 0u;
-            } else {
-              lm = (2u << lane) - 1u;
-            }
-          }
-          ids[v] = (int32_t)(vq + (uint32_t)__popc(uq & lm));
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t b = cv[q] + (uint32_t)__popc(cu[q] & below);
+          lo[q] = (int32_t)b;
+          hi[q] = (int32_t)(lane == 31 ? cv[4 + q] : b + ((cu[q] >> lane) & 1u));
         }
+        // v0..v7: (i,j,k) (i+1,j,k) (i+1,j+1,k) (i,j+1,k), then the same at k+1
+        const int32_t ids[8] = {lo[0], hi[0], hi[1], lo[1], lo[2], hi[2], hi[3], lo[3]};
         if (conn16) {
           int4* dst = reinterpret_cast<int4*>(conn + 8 * cid);
           dst[0] = make_int4(ids[0], ids[1], ids[2], ids[3]);
