@@ -164,22 +164,37 @@ __device__ __forceinline__ long long edge_id(const EdgeOwner& o, int b, int axis
   return id;
 }
 
-// Contribution of the edge (pa -> pb) along `axis`, vertex vid, to dL/df at
-// its end `at_a ? pa : pb`; idx_a = pa's index along the axis.
-__device__ __forceinline__ float edge_term(const Grid& g, const float* __restrict__ f, float iso,
-                                           const float* __restrict__ dverts, long long vid,
-                                           int axis, long long pa, long long pb, int idx_a,
+// Contribution to dL/df at one end of an edge along `axis` with end values
+// fa (at the lower end A) and fb, upstream dL/dx_v[axis] dv and axis width
+// h; at_a: the end is A.
+__device__ __forceinline__ float edge_term(float iso, float fa, float fb, float dv, float h,
                                            bool at_a) {
-  const float fa = __ldg(f + pa), fb = __ldg(f + pb);
   const float d = __fsub_rn(fb, fa);
-  const float h = axis == 0 ? width_x(g, idx_a) : (axis == 1 ? width_y(g, idx_a) : width_z(g, idx_a));
-  const float gv = __fmul_rn(__ldg(dverts + 3 * vid + axis), h);
+  const float gv = __fmul_rn(dv, h);
   const float num = at_a ? __fsub_rn(iso, fb) : -__fsub_rn(iso, fa);
   return __fdiv_rn(__fmul_rn(gv, num), __fmul_rn(d, d));
 }
 
+__device__ __forceinline__ uint32_t rank_below(uint32_t X, uint32_t Y, uint32_t Z, uint32_t lm) {
+  return (uint32_t)(__popc(X & lm) + __popc(Y & lm) + __popc(Z & lm));
+}
+
+// Position of the n-th (0-based) set bit of u; n < popc(u).
+__device__ __forceinline__ int nth_set_bit(uint32_t u, int n) {
+  int p = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (__popc(u & ((1u << (p + step)) - 1u)) <= n) p += step;
+  return p;
+}
+
 }  // namespace
 
+// A warp takes 32 consecutive point row words (lane = word) and finds the
+// points with an incident crossing edge and the owner words of their
+// backward edges; those points are then dealt to the lanes (lane = point),
+// which load all of a point's end values and vertex gradients before
+// summing its terms in the fixed order.
 __global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __restrict__ f,
                                                       float iso,
                                                       const uint32_t* __restrict__ bits,
@@ -188,57 +203,122 @@ __global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __res
                                                       float* __restrict__ out) {
   const long long W = g.R * g.wr;  // < 2^27 for grids below 2^31 points
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
-       w += (long long)gridDim.x * blockDim.x) {
-    int m, j, k;
-    const unsigned r = split_word(g, (unsigned)w, m);
-    split_row(g, r, j, k);
-    const long long pos = (long long)r * g.nx + 32ll * m;
-    const uint32_t pm = low_mask(g.nx - 32 * m);
-    uint32_t a, a1;
-    bits_at2(bits, pos, a, a1);
-    // points of this word with an incident crossing edge, per direction
-    const uint32_t xf = (a ^ a1) & low_mask(g.nx - 1 - 32 * m);
-    const uint32_t yf = j < g.ny - 1 ? (a ^ bits_at(bits, pos + dy)) & pm : 0u;
-    const uint32_t zf = k < g.nz - 1 ? (a ^ bits_at(bits, pos + dz)) & pm : 0u;
-    const uint32_t xb = pos > 0 ? (a ^ bits_at(bits, pos - 1)) & pm & (m == 0 ? ~1u : kFull) : 0u;
-    const uint32_t yb = j > 0 ? (a ^ bits_at(bits, pos - dy)) & pm : 0u;
-    const uint32_t zb = k > 0 ? (a ^ bits_at(bits, pos - dz)) & pm : 0u;
-    uint32_t inc = xf | yf | zf | xb | yb | zb;
-    if (inc == 0u) continue;
-    EdgeOwner own;
-    own.X = xf;
-    own.Y = yf;
-    own.Z = zf;
-    own.base = (long long)__ldg(wv + w);
-    EdgeOwner oy{}, oz{};
-    if (yb) oy = edge_owner(g, bits, wv, j - 1, k, m);
-    if (zb) oz = edge_owner(g, bits, wv, j, k - 1, m);
-    while (inc) {
-      const int b = __ffs(inc) - 1;
-      inc &= inc - 1u;
-      const uint32_t bit = 1u << b;
-      const int i = 32 * m + b;
-      const long long p = pos + b;
-      float acc = 0.0f;
-      if (xf & bit) acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, edge_id(own, b, 0), 0, p, p + 1, i, true));
-      if (yf & bit) acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, edge_id(own, b, 1), 1, p, p + dy, j, true));
-      if (zf & bit) acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, edge_id(own, b, 2), 2, p, p + dz, k, true));
-      if (xb & bit) {
-        long long vid;
-        if (b > 0) {
-          vid = edge_id(own, b - 1, 0);
-        } else {  // the owner is the last point of the previous word
-          const EdgeOwner ox = edge_owner(g, bits, wv, j, k, m - 1);
-          vid = edge_id(ox, 31, 0);
-        }
-        acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, vid, 0, p - 1, p, i - 1, false));
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long w0 = warp0 * 32; w0 < W; w0 += nwarps * 32) {
+    // ---- lane = word ------------------------------------------------------
+    const long long w = w0 + lane;
+    uint32_t inc = 0u, xf = 0u, yf = 0u, zf = 0u, xb = 0u, yb = 0u, zb = 0u, base = 0u;
+    uint32_t r = 0u;
+    int m = 0, j = 0, k = 0;
+    if (w < W) {
+      r = split_word(g, (unsigned)w, m);
+      split_row(g, r, j, k);
+      const long long pos = (long long)r * g.nx + 32ll * m;
+      const uint32_t pm = low_mask(g.nx - 32 * m);
+      uint32_t a, a1;
+      bits_at2(bits, pos, a, a1);
+      // points of this word with an incident crossing edge, per direction
+      xf = (a ^ a1) & low_mask(g.nx - 1 - 32 * m);
+      yf = j < g.ny - 1 ? (a ^ bits_at(bits, pos + dy)) & pm : 0u;
+      zf = k < g.nz - 1 ? (a ^ bits_at(bits, pos + dz)) & pm : 0u;
+      xb = pos > 0 ? (a ^ bits_at(bits, pos - 1)) & pm & (m == 0 ? ~1u : kFull) : 0u;
+      yb = j > 0 ? (a ^ bits_at(bits, pos - dy)) & pm : 0u;
+      zb = k > 0 ? (a ^ bits_at(bits, pos - dz)) & pm : 0u;
+      inc = xf | yf | zf | xb | yb | zb;
+    }
+    if (__ballot_sync(kFull, inc != 0u) == 0u) continue;
+    // owner words of the backward edges: (j - 1, k), (j, k - 1), and the
+    // x edge of bit 0, owned by the previous word's point 31
+    uint32_t oyX = 0u, oyY = 0u, oyZ = 0u, oyB = 0u, ozX = 0u, ozY = 0u, ozZ = 0u, ozB = 0u;
+    uint32_t ox31 = 0u;
+    if (inc) {
+      base = __ldg(wv + w);
+      if (yb) {
+        const EdgeOwner o = edge_owner(g, bits, wv, j - 1, k, m);
+        oyX = o.X;
+        oyY = o.Y;
+        oyZ = o.Z;
+        oyB = (uint32_t)o.base;
       }
-      if (yb & bit)
-        acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, edge_id(oy, b, 1), 1, p - dy, p, j - 1, false));
-      if (zb & bit)
-        acc = __fadd_rn(acc, edge_term(g, f, iso, dverts, edge_id(oz, b, 2), 2, p - dz, p, k - 1, false));
-      out[p] = __fadd_rn(out[p], acc);
+      if (zb) {
+        const EdgeOwner o = edge_owner(g, bits, wv, j, k - 1, m);
+        ozX = o.X;
+        ozY = o.Y;
+        ozZ = o.Z;
+        ozB = (uint32_t)o.base;
+      }
+      if (xb & 1u) ox31 = (uint32_t)edge_id(edge_owner(g, bits, wv, j, k, m - 1), 31, 0);
+    }
+    int total;
+    int pre = __popc(inc);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(kFull, pre, d);
+      if (lane >= d) pre += y;
+    }
+    total = __shfl_sync(kFull, pre, 31);
+    pre -= __popc(inc);  // exclusive: incident points of the words before this lane's
+    // ---- lane = incident point ------------------------------------------
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      int s = 0;  // the word holding point t: the last s with pre[s] <= t
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int ps = __shfl_sync(kFull, pre, s + step);
+        if (ps <= t) s += step;
+      }
+      const int rank = t - __shfl_sync(kFull, pre, s);
+      const uint32_t sinc = __shfl_sync(kFull, inc, s);
+      const uint32_t sxf = __shfl_sync(kFull, xf, s), syf = __shfl_sync(kFull, yf, s),
+                     szf = __shfl_sync(kFull, zf, s);
+      const uint32_t sxb = __shfl_sync(kFull, xb, s), syb = __shfl_sync(kFull, yb, s),
+                     szb = __shfl_sync(kFull, zb, s);
+      const uint32_t sbase = __shfl_sync(kFull, base, s);
+      const uint32_t syX = __shfl_sync(kFull, oyX, s), syY = __shfl_sync(kFull, oyY, s),
+                     syZ = __shfl_sync(kFull, oyZ, s), syB = __shfl_sync(kFull, oyB, s);
+      const uint32_t szX = __shfl_sync(kFull, ozX, s), szY = __shfl_sync(kFull, ozY, s),
+                     szZ = __shfl_sync(kFull, ozZ, s), szB = __shfl_sync(kFull, ozB, s);
+      const uint32_t sox = __shfl_sync(kFull, ox31, s), sr = __shfl_sync(kFull, r, s);
+      const int sm = __shfl_sync(kFull, m, s), sj = __shfl_sync(kFull, j, s),
+                sk = __shfl_sync(kFull, k, s);
+      if (t >= total) continue;
+      const int b = nth_set_bit(sinc, rank);
+      const int i = 32 * sm + b;
+      const long long p = (long long)sr * g.nx + i;
+      const bool fx = (sxf >> b) & 1u, fy = (syf >> b) & 1u, fz = (szf >> b) & 1u;
+      const bool bx = (sxb >> b) & 1u, by = (syb >> b) & 1u, bz = (szb >> b) & 1u;
+      // vertex ids, as the forward pass numbered them (owner word offset +
+      // rank of the edge in (point, axis) order)
+      const uint32_t lm = (1u << b) - 1u;
+      const uint32_t own = sbase + rank_below(sxf, syf, szf, lm);
+      const uint32_t vfx = own, vfy = own + (fx ? 1u : 0u), vfz = vfy + (fy ? 1u : 0u);
+      const uint32_t vbx = b > 0 ? sbase + rank_below(sxf, syf, szf, lm >> 1) : sox;
+      const uint32_t vby = syB + rank_below(syX, syY, syZ, lm) + ((syX >> b) & 1u);
+      const uint32_t vbz = szB + rank_below(szX, szY, szZ, lm) + ((szX >> b) & 1u) + ((szY >> b) & 1u);
+      // every load of the point first
+      const float fp = __ldg(f + p);
+      const float fxn = fx ? __ldg(f + p + 1) : 0.0f, fyn = fy ? __ldg(f + p + dy) : 0.0f,
+                  fzn = fz ? __ldg(f + p + dz) : 0.0f;
+      const float fxp = bx ? __ldg(f + p - 1) : 0.0f, fyp = by ? __ldg(f + p - dy) : 0.0f,
+                  fzp = bz ? __ldg(f + p - dz) : 0.0f;
+      const float gfx = fx ? __ldg(dverts + 3ll * vfx + 0) : 0.0f;
+      const float gfy = fy ? __ldg(dverts + 3ll * vfy + 1) : 0.0f;
+      const float gfz = fz ? __ldg(dverts + 3ll * vfz + 2) : 0.0f;
+      const float gbx = bx ? __ldg(dverts + 3ll * vbx + 0) : 0.0f;
+      const float gby = by ? __ldg(dverts + 3ll * vby + 1) : 0.0f;
+      const float gbz = bz ? __ldg(dverts + 3ll * vbz + 2) : 0.0f;
+      const float prev = out[p];
+      // forward x, y, z (the point is the edge's A end), then backward x, y, z
+      float acc = 0.0f;
+      if (fx) acc = __fadd_rn(acc, edge_term(iso, fp, fxn, gfx, width_x(g, i), true));
+      if (fy) acc = __fadd_rn(acc, edge_term(iso, fp, fyn, gfy, width_y(g, sj), true));
+      if (fz) acc = __fadd_rn(acc, edge_term(iso, fp, fzn, gfz, width_z(g, sk), true));
+      if (bx) acc = __fadd_rn(acc, edge_term(iso, fxp, fp, gbx, width_x(g, i - 1), false));
+      if (by) acc = __fadd_rn(acc, edge_term(iso, fyp, fp, gby, width_y(g, sj - 1), false));
+      if (bz) acc = __fadd_rn(acc, edge_term(iso, fzp, fp, gbz, width_z(g, sk - 1), false));
+      out[p] = __fadd_rn(prev, acc);
     }
   }
 }
