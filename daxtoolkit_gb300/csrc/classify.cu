@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long nchunks = S.chunks;
   const float nan = __int_as_float(0x7fc00000);  // classifies as 0 in both modes
+  __shared__ long long s_keys[kStagedSlots];
+  const long long* keys =
+      stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.chunk0; }) ? s_keys : nullptr;
   if (S.count == 1) {
     // one grid: field pointer and thresholds are loop invariants
     const float* __restrict__ f = S.one.field;
@@ -70,6 +73,9 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
       float4 v[UNROLL];
       float a[UNROLL], b[UNROLL];
       long long wout[UNROLL];
+      // one search per warp step (the step's chunks are consecutive), then
+      // a step forward where a chunk starts a later grid
+      int si = keys ? slot_search(keys, S.count, c0) : slot_of_chunk(S, c0);
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const long long c = c0 + u;
@@ -77,7 +83,8 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
         a[u] = b[u] = 0.0f;
         wout[u] = -1;
         if (c < nchunks) {
-          const GridSlot& sl = S.slots[slot_of_chunk(S, c)];
+          while (si + 1 < S.count && (keys ? keys[si + 1] : __ldg(&S.slots[si + 1].chunk0)) <= c) ++si;
+          const GridSlot& sl = S.slots[si];
           const long long lc = c - sl.chunk0;
           const long long base = (lc << 7) + lane * 4;
           const float* f = sl.field;

@@ -110,6 +110,45 @@ __device__ __forceinline__ int slot_of_rowword(const GridSet& S, long long rw) {
   return lo;
 }
 
+// Slot search keys (each slot's first chunk or first row word) staged in a
+// block's shared memory: a grid-set kernel looks up a slot per chunk or per
+// word, and a search through the slot table in global memory is a chain of
+// dependent loads that the field stream evicts from L1.
+constexpr int kStagedSlots = 512;
+
+// Stages key(slot) for every slot when the set has at most kStagedSlots
+// (call from every thread of the block; ends with a block barrier).
+// Returns whether the keys were staged.
+template <typename Key>
+__device__ __forceinline__ bool stage_slot_keys(const GridSet& S, long long* keys, Key key) {
+  const bool staged = S.count > 1 && S.count <= kStagedSlots;
+  if (staged)
+    for (int i = threadIdx.x; i < S.count; i += blockDim.x) keys[i] = key(S.slots[i]);
+  __syncthreads();
+  return staged;
+}
+
+// The last slot whose key is <= x.
+__device__ __forceinline__ int slot_search(const long long* keys, int count, long long x) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (keys[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The slot of x for x at or after slot `from`'s start: steps forward over
+// the slots that start at or before x (keys staged by stage_slot_keys, or
+// null: the slots' first row words, rw0, from global memory).  A warp whose
+// items lie in few slots searches once and steps.
+__device__ __forceinline__ int slot_after(const GridSet& S, const long long* keys, int from,
+                                          long long x) {
+  int si = from;
+  while (si + 1 < S.count && (keys ? keys[si + 1] : __ldg(&S.slots[si + 1].rw0)) <= x) ++si;
+  return si;
+}
+
 __device__ __forceinline__ GridSlot load_slot(const GridSet& S, int i) {
   return S.count == 1 ? S.one : S.slots[i];
 }

@@ -121,9 +121,15 @@ __device__ __forceinline__ WordBits load_word_bits(const Grid& g, const uint32_t
   return wb;
 }
 
+// Slot, point row and word index of global row word gw; keys: the slots'
+// first row words staged in shared memory, or null; from >= 0: a slot that
+// starts at or before gw (the search steps forward from it).
 __device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int& si, unsigned& r,
-                                            int& m) {
-  si = S.count == 1 ? 0 : slot_of_rowword(S, gw);
+                                            int& m, const long long* keys = nullptr,
+                                            int from = -1) {
+  si = S.count == 1 ? 0
+       : from >= 0  ? slot_after(S, keys, from, gw)
+                    : (keys ? slot_search(keys, S.count, gw) : slot_of_rowword(S, gw));
   const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
   const unsigned lw = (unsigned)(gw - sl.rw0);
   r = split_word(sl.g, lw, m);
@@ -170,17 +176,25 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
                                                   uint32_t* __restrict__ tile_tot, int tiles) {
   __shared__ unsigned char s_nf[256];  // NumFaces, indexed by divergent case ids
   __shared__ uint32_t s_red[24];
+  __shared__ long long s_keys[kStagedSlots];
   s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
-  __syncthreads();
+  const long long* keys =
+      stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     uint32_t st = 0, sv = 0, sa = 0;
 #pragma unroll 1
     for (int e = 0; e < kScanItems / kCountWords; ++e) {
       const long long g0 = (long long)tile * kScanTile + (long long)(threadIdx.x + 256 * e) * kCountWords;
+      // the slot of the warp's first group, searched once (the warp's
+      // groups are consecutive); every lane steps forward from it
+      const long long gw0 = g0 - (long long)(threadIdx.x & 31) * kCountWords;
+      const int s0 = S.count == 1 || gw0 >= S.rowwords
+                         ? 0
+                         : (keys ? slot_search(keys, S.count, gw0) : slot_of_rowword(S, gw0));
       if (g0 >= S.rowwords) break;
       int si, m;
       unsigned r;
-      locate_word(S, g0, si, r, m);
+      locate_word(S, g0, si, r, m, keys, s0);
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
       const Grid& g = sl.g;
       uint32_t out[kCountWords] = {0, 0, 0, 0};
@@ -214,7 +228,7 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
           if (gw >= S.rowwords) break;
           int sq, mq;
           unsigned rq;
-          locate_word(S, gw, sq, rq, mq);
+          locate_word(S, gw, sq, rq, mq, keys, si);
           const GridSlot& slq = S.count == 1 ? S.one : S.slots[sq];
           if (slq.g.nx >= 2 && slq.g.ny >= 2 && slq.g.nz >= 2) {
             const WordBits wb = load_word_bits(slq.g, bits + slq.word0, rq, mq);
@@ -547,9 +561,11 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
   __shared__ int s_prev[kEmitWarps][33];   // owned vertices before word s
   __shared__ uint32_t s_cell[kEmitWarps][kCellChunk];     // word | bit << 5 | case << 10
   __shared__ int s_tpre[kEmitWarps][kCellChunk + 1];      // triangles before cell
+  __shared__ long long s_keys[kStagedSlots];
   s_case[threadIdx.x] = kMcCase[threadIdx.x];
   if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
-  __syncthreads();
+  const long long* keys =
+      stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
   long long A;
   if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -573,7 +589,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
       t0 = __ldg(o.wt + gw);
       int si, m;
       unsigned r;
-      locate_word(S, gw, si, r, m);
+      locate_word(S, gw, si, r, m, keys);
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
       const Grid& g = sl.g;
       int j, k;
