@@ -135,6 +135,15 @@ __device__ __forceinline__ void locate_word(const GridSet& S, long long gw, int&
   r = split_word(sl.g, lw, m);
 }
 
+// Position of the n-th (0-based) set bit of u; n < popc(u).
+__device__ __forceinline__ int nth_bit(uint32_t u, int n) {
+  int p = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (__popc(u & ((1u << (p + step)) - 1u)) <= n) p += step;
+  return p;
+}
+
 // Counts of one word from its eight corner words.
 __device__ __forceinline__ uint32_t packed_counts(const CornerWords& w, bool hy, bool hz,
                                                   uint32_t pmask, uint32_t xmask,
@@ -391,11 +400,160 @@ void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* ti
   k_word_scan<<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info);
 }
 
+// K2a for grid sets: the same counts, with the triangles of the active
+// cells dealt across the warp.  Batches of small grids have short rows (the
+// 4-word groups straddle rows) and, with noisy fields, many active cells,
+// so a lane looping over its own words' active cells would hold its warp
+// for the busiest lane.  Here a lane gathers its 4 words' corner bits and
+// counts their crossing edges; the warp then deals the active cells of its
+// 128 words to the lanes, a cell per lane per round: each reads its word's
+// corner bits from the warp's staging area and adds NumFaces of its case to
+// the word's total there.  (For one large grid the per-lane loop is faster:
+// its surface is sparse, and this kernel's staging costs occupancy.)
+__global__ void __launch_bounds__(256) k_mc_count_dealt(GridSet S, const uint32_t* __restrict__ bits,
+                                                        uint32_t* __restrict__ wc,
+                                                        uint32_t* __restrict__ tile_tot, int tiles) {
+  constexpr int kSlots = 32 * kCountWords;  // words per warp step
+  __shared__ unsigned char s_nf[256];        // NumFaces
+  __shared__ uint32_t s_red[24];
+  __shared__ long long s_keys[kStagedSlots];
+  __shared__ uint32_t s_win[8][8 * kSlots];  // corner word f of slot (4 lane + q) at f * kSlots + slot
+  __shared__ uint32_t s_tri[8][kSlots];      // triangles of slot
+  s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
+  const long long* keys =
+      stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t* const win = s_win[wib];
+  uint32_t* const tri = s_tri[wib];
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    uint32_t st = 0, sv = 0, sa = 0;
+#pragma unroll 1
+    for (int e = 0; e < kScanItems / kCountWords; ++e) {
+      const long long gw0 = (long long)tile * kScanTile + (long long)(256 * e + 32 * wib) * kCountWords;
+      if (gw0 >= S.rowwords) break;  // uniform across the warp
+      const long long g0 = gw0 + (long long)lane * kCountWords;
+      const int s0 = keys ? slot_search(keys, S.count, gw0) : slot_of_rowword(S, gw0);
+      // ---- lane = 4 words: corner bits, crossing edges, active cells ------
+      CornerWords w[kCountWords];
+      uint32_t v[kCountWords], am[kCountWords], t[kCountWords] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < kCountWords; ++q) {
+        w[q] = CornerWords{};
+        v[q] = am[q] = 0u;
+        const long long gw = g0 + q;
+        if (gw < S.rowwords) {
+          int sq, mq;
+          unsigned rq;
+          locate_word(S, gw, sq, rq, mq, keys, s0);
+          const GridSlot& slq = S.slots[sq];
+          if (slq.g.nx >= 2 && slq.g.ny >= 2 && slq.g.nz >= 2) {
+            const WordBits wb = load_word_bits(slq.g, bits + slq.word0, rq, mq);
+            w[q] = wb.w;
+            int vv = __popc((wb.w.a ^ wb.w.a1) & wb.xmask);
+            if (wb.hy) vv += __popc((wb.w.a ^ wb.w.b) & wb.pmask);
+            if (wb.hz) vv += __popc((wb.w.a ^ wb.w.c) & wb.pmask);
+            v[q] = (uint32_t)vv;
+            am[q] = (wb.hy && wb.hz) ? active_cells(wb.w, wb.xmask) : 0u;
+          }
+        }
+      }
+      // ---- lane = active cell -------------------------------------------
+      const int cnt = __popc(am[0]) + __popc(am[1]) + __popc(am[2]) + __popc(am[3]);
+      int pre = cnt;  // inclusive scan of the lanes' active cells
+#pragma unroll
+      for (int dd = 1; dd < 32; dd <<= 1) {
+        const int y = __shfl_up_sync(kFull, pre, dd);
+        if (lane >= dd) pre += y;
+      }
+      const int total = __shfl_sync(kFull, pre, 31);
+      pre -= cnt;
+      if (total > 0) {
+#pragma unroll
+        for (int q = 0; q < kCountWords; ++q) {
+          const int slot = kCountWords * lane + q;
+          tri[slot] = 0u;
+          if (am[q]) {
+            win[0 * kSlots + slot] = w[q].a;
+            win[1 * kSlots + slot] = w[q].a1;
+            win[2 * kSlots + slot] = w[q].b;
+            win[3 * kSlots + slot] = w[q].b1;
+            win[4 * kSlots + slot] = w[q].c;
+            win[5 * kSlots + slot] = w[q].c1;
+            win[6 * kSlots + slot] = w[q].d;
+            win[7 * kSlots + slot] = w[q].d1;
+          }
+        }
+        __syncwarp();
+        for (int t0 = 0; t0 < total; t0 += 32) {
+          const int tt = t0 + lane;
+          int s = 0;  // the lane holding cell tt: the last s with pre[s] <= tt
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const int ps = __shfl_sync(kFull, pre, s + step);
+            if (ps <= tt) s += step;
+          }
+          int rnk = tt - __shfl_sync(kFull, pre, s);
+          const uint32_t m0 = __shfl_sync(kFull, am[0], s), m1 = __shfl_sync(kFull, am[1], s),
+                         m2 = __shfl_sync(kFull, am[2], s), m3 = __shfl_sync(kFull, am[3], s);
+          if (tt < total) {
+            // the word q of lane s holding the cell, and the cell's rank in it
+            int q = 0;
+            uint32_t mq = m0;
+            const int c0 = __popc(m0), c01 = c0 + __popc(m1), c012 = c01 + __popc(m2);
+            if (rnk >= c012) {
+              q = 3;
+              mq = m3;
+              rnk -= c012;
+            } else if (rnk >= c01) {
+              q = 2;
+              mq = m2;
+              rnk -= c01;
+            } else if (rnk >= c0) {
+              q = 1;
+              mq = m1;
+              rnk -= c0;
+            }
+            const int slot = kCountWords * s + q;
+            const CornerWords cw{win[0 * kSlots + slot], win[1 * kSlots + slot],
+                                 win[2 * kSlots + slot], win[3 * kSlots + slot],
+                                 win[4 * kSlots + slot], win[5 * kSlots + slot],
+                                 win[6 * kSlots + slot], win[7 * kSlots + slot]};
+            atomicAdd(&tri[slot], (uint32_t)s_nf[case_of(cw, nth_bit(mq, rnk))]);
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kCountWords; ++q) t[q] = tri[kCountWords * lane + q];
+        __syncwarp();
+      }
+#pragma unroll
+      for (int q = 0; q < kCountWords; ++q) {
+        const uint32_t out = (t[q] << 16) | v[q];
+        if (g0 + q < S.rowwords) wc[g0 + q] = out;
+        st += t[q];
+        sv += v[q];
+        sa += out ? 1u : 0u;
+      }
+    }
+    block_sum3(st, sv, sa, s_red);
+    if (threadIdx.x == 0) {
+      tile_tot[tile] = st;
+      tile_tot[tiles + tile] = sv;
+      tile_tot[2 * tiles + tile] = sa;
+    }
+  }
+}
+
 void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
                     int num_sms, cudaStream_t s) {
   const int tiles = word_scan_tiles(S.rowwords);
-  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles, kPassCount);
-  k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
+  if (S.count > 1) {
+    const int b1 = resident_blocks(k_mc_count_dealt, 256, 0, num_sms, tiles, kPassCount);
+    k_mc_count_dealt<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
+  } else {
+    const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles, kPassCount);
+    k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
+  }
   launch_word_scan(S.rowwords, o.wc, o.tile, o.wt, o.wv, o.act, info, s);
 }
 
@@ -518,15 +676,6 @@ __device__ __forceinline__ int search32(const int* pre, int x) {
   for (int step = 16; step > 0; step >>= 1)
     if (pre[s + step] <= x) s += step;
   return s;
-}
-
-// Position of the n-th (0-based) set bit of u; n < popc(u).
-__device__ __forceinline__ int nth_bit(uint32_t u, int n) {
-  int p = 0;
-#pragma unroll
-  for (int step = 16; step > 0; step >>= 1)
-    if (__popc(u & ((1u << (p + step)) - 1u)) <= n) p += step;
-  return p;
 }
 
 // Exclusive warp scan of v; *total receives the warp's sum.
