@@ -69,13 +69,18 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
       }
     }
   } else {
-    for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
+    // one search per warp step (the step's chunks are consecutive), then a
+    // step forward where a chunk starts a later grid; the next step's search
+    // runs while this step's loads are in flight
+    const long long stride = nwarps * UNROLL;
+    int snext = warp * UNROLL < nchunks
+                    ? (keys ? slot_search(keys, S.count, warp * UNROLL) : slot_of_chunk(S, warp * UNROLL))
+                    : 0;
+    for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += stride) {
       float4 v[UNROLL];
       float a[UNROLL], b[UNROLL];
       long long wout[UNROLL];
-      // one search per warp step (the step's chunks are consecutive), then
-      // a step forward where a chunk starts a later grid
-      int si = keys ? slot_search(keys, S.count, c0) : slot_of_chunk(S, c0);
+      int si = snext;
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const long long c = c0 + u;
@@ -102,6 +107,8 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
           }
         }
       }
+      if (c0 + stride < nchunks)
+        snext = keys ? slot_search(keys, S.count, c0 + stride) : slot_of_chunk(S, c0 + stride);
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const uint32_t nib = classify_point<MODE>(v[u].x, a[u], b[u]) |
