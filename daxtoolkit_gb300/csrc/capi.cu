@@ -204,6 +204,7 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
   int st = make_grid(grid, g);
   if (st) return st;
   if (!field || !scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if (!aligned16(scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if ((st = device_view(field, "field"))) return st;
   const size_t need = mode == 0 ? mc_layout(g).total : layout(g).total;
   if (bytes < need) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than *_scratch_bytes()");
@@ -356,6 +357,7 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if ((st = device_view(d_field, "field"))) return st;
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
       tri_capacity < 0)
@@ -393,6 +395,7 @@ int dax_gb300_slice_count(const dax_gb300_uniform_grid* grid, const float* origi
   if (st) return st;
   if (!origin || !normal || !d_scratch)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL origin, normal or scratch");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   const McLayout L = mc_layout(g);
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
@@ -428,6 +431,7 @@ int dax_gb300_slice_generate(const dax_gb300_uniform_grid* grid, const float* or
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!origin || !normal || !d_scratch)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL origin, normal or scratch");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
       tri_capacity < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
@@ -672,6 +676,7 @@ int dax_gb300_mc_counted_scan(const dax_gb300_uniform_grid* grid, const int32_t*
   const CountedLayout L = counted_layout(C);
   if (!d_scratch || scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if (C > 0 && !d_count) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count array");
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
   char* sc = static_cast<char*>(d_scratch);
@@ -702,6 +707,7 @@ int dax_gb300_mc_counted_merge(const dax_gb300_uniform_grid* grid, const float* 
   const CountedLayout L = counted_layout(C);
   if (!d_scratch || scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if (C > 0 && (!d_count || !d_field)) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count or field");
   if ((st = device_view(d_field, "field"))) return st;
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -737,6 +743,7 @@ int dax_gb300_mc_counted_generate(const dax_gb300_uniform_grid* grid, const floa
   const CountedLayout L = counted_layout(C);
   if (!d_scratch || scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_counted_scratch_bytes()");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if (!d_count || !d_field) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL count or field");
   if ((st = device_view(d_field, "field"))) return st;
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
@@ -877,6 +884,7 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
   if (st) return st;
   if (!has_cells(g)) return DAX_GB300_SUCCESS;
   if (!d_field || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
   if ((st = device_view(d_field, "field"))) return st;
   if ((!d_conn && cell_capacity > 0) || (!d_coords && point_capacity > 0) || cell_capacity < 0 ||
       point_capacity < 0)

@@ -157,22 +157,6 @@ __device__ __forceinline__ uint32_t packed_counts(const CornerWords& w, bool hy,
   return ((uint32_t)t << 16) | (uint32_t)v;
 }
 
-// Four consecutive 32-bit windows of a row (x = 32m .. 32m+127) and their +x
-// neighbours, from five word fetches.
-__device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, long long pos,
-                                             uint32_t (&a)[4], uint32_t (&a1)[4]) {
-  const long long w = pos >> 5;
-  const unsigned sh = (unsigned)(pos & 31);
-  uint32_t x[5];
-#pragma unroll
-  for (int e = 0; e < 5; ++e) x[e] = __ldg(bits + w + e);
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    a[e] = __funnelshift_r(x[e], x[e + 1], sh);
-    a1[e] = (a[e] >> 1) | (((x[e + 1] >> sh) & 1u) << 31);
-  }
-}
-
 constexpr int kCountWords = 4;  // consecutive row words per count group
 
 // K2a: one 256-thread block per tile of kScanTile row words (grid-stride

@@ -33,66 +33,155 @@ __device__ __forceinline__ uint32_t bits_at_u32(const uint32_t* __restrict__ bit
   return __funnelshift_r(__ldg(bits + (pos >> 5)), __ldg(bits + (pos >> 5) + 1), pos & 31u);
 }
 
-// K2a, first pass: kept mask of every cell-row word (0 on rows without cells).
+// Kept mask of cell-row word w (0 on rows without cells).
+__device__ __forceinline__ uint32_t kept_word(const Grid& g, const uint32_t* __restrict__ bits,
+                                              uint32_t w) {
+  const uint32_t nx = (uint32_t)g.nx, dy = nx, dz = nx * (uint32_t)g.ny;
+  int mi, ji, ki;
+  const uint32_t r = split_word(g, w, mi);
+  split_row(g, r, ji, ki);
+  const uint32_t m = (uint32_t)mi, j = (uint32_t)ji, k = (uint32_t)ki;
+  if (j + 1 >= (uint32_t)g.ny || k + 1 >= (uint32_t)g.nz) return 0u;
+  const uint32_t pos = r * nx + 32u * m;
+  const uint32_t p0 = pos, p1 = pos + dy, p2 = pos + dz, p3 = pos + dy + dz;
+  return bits_at_u32(bits, p0) & bits_at_u32(bits, p0 + 1) & bits_at_u32(bits, p1) &
+         bits_at_u32(bits, p1 + 1) & bits_at_u32(bits, p2) & bits_at_u32(bits, p2 + 1) &
+         bits_at_u32(bits, p3) & bits_at_u32(bits, p3 + 1) & low_mask(g.nx - 1 - 32 * (int)m);
+}
+
+// K2a, first pass: kept masks of every cell-row word, four consecutive words
+// per thread; four words of one row come from five bit-word fetches per
+// corner row.
 __global__ void __launch_bounds__(256) k_thr_kept(Grid g, const uint32_t* __restrict__ bits,
                                                   uint32_t* __restrict__ kept) {
-  const uint32_t W = (uint32_t)(g.R * g.wr);  // < 2^27 for grids below 2^31 points
-  const uint32_t nx = (uint32_t)g.nx;
-  const uint32_t dy = nx, dz = nx * (uint32_t)g.ny;
-  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
-    int mi, ji, ki;
-    const uint32_t r = split_word(g, w, mi);
-    split_row(g, r, ji, ki);
-    const uint32_t m = (uint32_t)mi, j = (uint32_t)ji, k = (uint32_t)ki;
-    uint32_t K = 0u;
-    if (j + 1 < (uint32_t)g.ny && k + 1 < (uint32_t)g.nz) {
-      const uint32_t pos = r * nx + 32u * m;
-      const uint32_t p0 = pos, p1 = pos + dy, p2 = pos + dz, p3 = pos + dy + dz;
-      K = bits_at_u32(bits, p0) & bits_at_u32(bits, p0 + 1) & bits_at_u32(bits, p1) &
-          bits_at_u32(bits, p1 + 1) & bits_at_u32(bits, p2) & bits_at_u32(bits, p2 + 1) &
-          bits_at_u32(bits, p3) & bits_at_u32(bits, p3 + 1) & low_mask(g.nx - 1 - 32 * (int)m);
+  const long long W = g.R * g.wr;  // < 2^27 for grids below 2^31 points
+  const long long groups = (W + 3) / 4;
+  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+  for (long long q4 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q4 < groups;
+       q4 += (long long)gridDim.x * blockDim.x) {
+    const long long w0 = 4 * q4;
+    int m, j, k;
+    const unsigned r = split_word(g, (unsigned)w0, m);
+    split_row(g, r, j, k);
+    uint32_t K[4] = {0u, 0u, 0u, 0u};
+    if (m + 4 <= g.wr) {  // four words of one row
+      if (j + 1 < g.ny && k + 1 < g.nz) {
+        const long long pos = (long long)r * g.nx + 32ll * m;
+        uint32_t a[4], a1[4], b[4], b1[4], c[4], c1[4], d[4], d1[4];
+        row_windows4(bits, pos, a, a1);
+        row_windows4(bits, pos + dy, b, b1);
+        row_windows4(bits, pos + dz, c, c1);
+        row_windows4(bits, pos + dy + dz, d, d1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          K[q] = a[q] & a1[q] & b[q] & b1[q] & c[q] & c1[q] & d[q] & d1[q] &
+                 low_mask(g.nx - 1 - 32 * (m + q));
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (w0 + q < W) K[q] = kept_word(g, bits, (uint32_t)(w0 + q));
     }
-    kept[w] = K;
+    if (w0 + 4 <= W) {
+      *reinterpret_cast<uint4*>(kept + w0) = make_uint4(K[0], K[1], K[2], K[3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (w0 + q < W) kept[w0 + q] = K[q];
+    }
   }
 }
 
+// Used mask of point-row word w = (row r = (j, k), word m): the OR of the
+// kept masks of cell rows (j - 1 .. j, k - 1 .. k), each with its +x
+// neighbour cell.
+__device__ __forceinline__ uint32_t used_word(const Grid& g, const uint32_t* __restrict__ kept,
+                                              uint32_t w, uint32_t m, uint32_t j, uint32_t k) {
+  const uint32_t wy = (uint32_t)g.wr, wz = (uint32_t)g.wr * (uint32_t)g.ny;
+  uint32_t u = 0u;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {  // cell rows (j - (c & 1), k - (c >> 1))
+    const uint32_t cj = c & 1, ck = c >> 1;
+    if (j < cj || k < ck) continue;
+    const uint32_t wq = w - cj * wy - ck * wz;
+    const uint32_t K = __ldg(kept + wq);
+    const uint32_t Kp = m > 0 ? __ldg(kept + wq - 1) : 0u;
+    u |= K | (K << 1) | (Kp >> 31);
+  }
+  return u & low_mask(g.nx - 32 * (int)m);
+}
+
 // K2a, second pass: one 256-thread block per tile of kScanTile words
-// (grid-stride over tiles): used masks, packed counts and tile totals.
+// (grid-stride over tiles), thread t taking the 4-word groups t + 256 e:
+// used masks, packed counts and tile totals.
 __global__ void __launch_bounds__(256) k_thr_used(Grid g, const uint32_t* __restrict__ kept,
                                                   uint32_t* __restrict__ used,
                                                   uint32_t* __restrict__ wc,
                                                   uint32_t* __restrict__ tile_tot, int tiles) {
   __shared__ uint32_t s_red[24];
-  const uint32_t W = (uint32_t)(g.R * g.wr);
-  const uint32_t wr = (uint32_t)g.wr, wy = wr, wz = wr * (uint32_t)g.ny;
+  const long long W = g.R * g.wr;
+  const uint32_t wy = (uint32_t)g.wr, wz = (uint32_t)g.wr * (uint32_t)g.ny;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     uint32_t sk = 0, su = 0, sa = 0;
-#pragma unroll 4
-    for (int e = 0; e < kScanItems; ++e) {
-      const uint32_t w = (uint32_t)tile * kScanTile + threadIdx.x + 256u * e;
-      if (w >= W) break;
+#pragma unroll 1
+    for (int e = 0; e < kScanItems / 4; ++e) {
+      const long long w0 = (long long)tile * kScanTile + 4ll * (threadIdx.x + 256 * e);
+      if (w0 >= W) break;
       int mi, ji, ki;
-      const uint32_t r = split_word(g, w, mi);
+      const uint32_t r = split_word(g, (uint32_t)w0, mi);
       split_row(g, r, ji, ki);
       const uint32_t m = (uint32_t)mi, j = (uint32_t)ji, k = (uint32_t)ki;
-      const uint32_t own = __ldg(kept + w);
-      uint32_t u = 0u;
+      uint32_t own[4] = {0u, 0u, 0u, 0u}, U[4] = {0u, 0u, 0u, 0u};
+      if (m + 4 <= wy) {  // four words of one row: 5 kept words per cell row
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {  // cell rows (j - (c & 1), k - (c >> 1))
-        const uint32_t cj = c & 1, ck = c >> 1;
-        if (j < cj || k < ck) continue;
-        const uint32_t wq = w - cj * wy - ck * wz;
-        const uint32_t K = c == 0 ? own : __ldg(kept + wq);
-        const uint32_t Kp = m > 0 ? __ldg(kept + wq - 1) : 0u;
-        u |= K | (K << 1) | (Kp >> 31);
+        for (int c = 0; c < 4; ++c) {  // cell rows (j - (c & 1), k - (c >> 1))
+          const uint32_t cj = c & 1, ck = c >> 1;
+          if (j < cj || k < ck) continue;
+          const uint32_t wq = (uint32_t)w0 - cj * wy - ck * wz;
+          uint32_t K[5];
+          K[0] = m > 0 ? __ldg(kept + wq - 1) : 0u;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) K[q + 1] = __ldg(kept + wq + q);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) U[q] |= K[q + 1] | (K[q + 1] << 1) | (K[q] >> 31);
+          if (c == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) own[q] = K[q + 1];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) U[q] &= low_mask(g.nx - 32 * (int)(m + q));
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const long long w = w0 + q;
+          if (w >= W) break;
+          int mq, jq, kq;
+          const uint32_t rq = split_word(g, (uint32_t)w, mq);
+          split_row(g, rq, jq, kq);
+          own[q] = __ldg(kept + w);
+          U[q] = used_word(g, kept, (uint32_t)w, (uint32_t)mq, (uint32_t)jq, (uint32_t)kq);
+        }
       }
-      u &= low_mask(g.nx - 32 * (int)m);
-      used[w] = u;
-      const uint32_t pk = (uint32_t)__popc(own) << 16 | (uint32_t)__popc(u);
-      wc[w] = pk;
-      sk += pk >> 16;
-      su += pk & 0xffffu;
-      sa += pk ? 1u : 0u;
+      uint32_t pk[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        pk[q] = (uint32_t)__popc(own[q]) << 16 | (uint32_t)__popc(U[q]);
+        sk += pk[q] >> 16;
+        su += pk[q] & 0xffffu;
+        sa += pk[q] ? 1u : 0u;
+      }
+      if (w0 + 4 <= W) {
+        *reinterpret_cast<uint4*>(used + w0) = make_uint4(U[0], U[1], U[2], U[3]);
+        *reinterpret_cast<uint4*>(wc + w0) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (w0 + q < W) {
+            used[w0 + q] = U[q];
+            wc[w0 + q] = pk[q];
+          }
+      }
     }
     block_sum3(sk, su, sa, s_red);
     if (threadIdx.x == 0) {
@@ -106,7 +195,7 @@ __global__ void __launch_bounds__(256) k_thr_used(Grid g, const uint32_t* __rest
 void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint32_t* used,
                       uint32_t* wc, uint32_t* tile_tot, int num_sms, cudaStream_t s) {
   const long long W = g.R * g.wr;
-  const int b1 = resident_blocks(k_thr_kept, 256, 0, num_sms, (W + 255) / 256);
+  const int b1 = resident_blocks(k_thr_kept, 256, 0, num_sms, (W + 1023) / 1024);
   k_thr_kept<<<b1, 256, 0, s>>>(g, bits, kept);
   const int tiles = word_scan_tiles(W);
   const int b2 = resident_blocks(k_thr_used, 256, 0, num_sms, tiles);

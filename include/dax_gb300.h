@@ -118,7 +118,9 @@ int dax_gb300_mc_classify_count(const dax_gb300_uniform_grid* grid, const float*
                                 float isovalue, int32_t* d_count, uint8_t* d_cases,
                                 void* stream);
 
-/* Device scratch the fused pipeline needs for this grid (bytes). */
+/* Device scratch the fused pipeline needs for this grid (bytes).  Every
+ * scratch buffer passed to this library must start on a 16-byte boundary
+ * (cudaMalloc's are); others are refused with DAX_GB300_ERROR_BAD_VALUE. */
 size_t dax_gb300_mc_scratch_bytes(const dax_gb300_uniform_grid* grid);
 
 /* Classify every point, count triangles and crossing edges per grid row and

@@ -150,6 +150,31 @@ def test_cell_gradient_unaligned_output(gb300, oracle_best):
     assert buf[0].item() == -7.0 and buf[-1].item() == -7.0
 
 
+@pytest.mark.parametrize("entry", ["dax_gb300_mc_count", "dax_gb300_threshold_count"])
+def test_unaligned_scratch_is_refused(gb300, entry):
+    """A scratch pointer off a 16-byte boundary is refused (the count passes
+    store 16-byte vectors into it), and nothing is written."""
+    import ctypes
+    from daxtoolkit_gb300 import capi
+    cont = gb300
+    dims = (26, 26, 26)
+    grid = cont.UniformGrid(dims)
+    f = torch.from_numpy(cases.linear_field(dims)).cuda()
+    g = grid.desc()
+    n = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    n = max(n, capi.lib().dax_gb300_threshold_scratch_bytes(ctypes.byref(g)))
+    buf = torch.full((n + 16,), 0x5a, dtype=torch.uint8, device="cuda")
+    scratch = buf[4:]
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    args = (70.0,) if entry == "dax_gb300_mc_count" else (70.0, 82.0)
+    st = getattr(capi.lib(), entry)(ctypes.byref(g), p(f), *[ctypes.c_float(a) for a in args],
+                                     p(scratch), ctypes.c_size_t(n), s)
+    torch.cuda.synchronize()
+    assert st == capi.ERROR_BAD_VALUE
+    assert bool((buf == 0x5a).all())
+
+
 def test_capacity_error_writes_nothing(gb300):
     """A too-small output buffer is reported, and nothing is written."""
     import ctypes
