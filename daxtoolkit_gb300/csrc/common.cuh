@@ -260,7 +260,7 @@ __device__ __forceinline__ void bits_at2(const uint32_t* __restrict__ bits, long
   const unsigned sh = (unsigned)(pos & 31);
   const uint32_t w0 = __ldg(bits + w), w1 = __ldg(bits + w + 1);
   a = __funnelshift_r(w0, w1, sh);
-  a1 = (a >> 1) | (((w1 >> sh) & 1u) << 31);
+  a1 = __funnelshift_rc(w0, w1, sh + 1u);  // sh = 31: w1 whole
 }
 
 // Mask of the low n bits (n in [0, 32]).
@@ -276,7 +276,7 @@ __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, 
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     a[e] = __funnelshift_r(x[e], x[e + 1], sh);
-    a1[e] = (a[e] >> 1) | (((x[e + 1] >> sh) & 1u) << 31);
+    a1[e] = __funnelshift_rc(x[e], x[e + 1], sh + 1u);  // sh = 31: the next word whole
   }
 }
 
