@@ -73,6 +73,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(t_ms, world, device="cpu"):
+    """The slowest rank's timed-region length (every rank calls this; one
+    MAX all-reduce when world > 1)."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def weak_value(world, units_per_rank, steps, t_ms):
+    """Whole-job throughput under weak scaling: every rank's units over the
+    slowest rank's time."""
+    return world * units_per_rank * steps / (t_ms / 1e3)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -769,13 +787,9 @@ def main():
     a1, b1 = run_frames(reps1, 1)
     torch.cuda.synchronize()
     ms_one = a1.elapsed_time(b1) / reps1
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = max_over_ranks(t_ms, world, dev)
     ms_per_step = t_ms / args.steps
-    value = world * C * args.steps / (t_ms / 1e3)
+    value = weak_value(world, C, args.steps, t_ms)
 
     # --- per-stage timing: K1 alone, count pass, generate pass -------------
     bits = torch.empty(L.dax_gb300_classify_words(P), dtype=torch.int32, device=dev)
