@@ -25,6 +25,8 @@
 
 #include <stdint.h>
 
+#include <mutex>
+
 #include <cuda_runtime.h>
 
 #include "dax_gb300.h"
@@ -98,11 +100,17 @@ auto give_buffer(F& f, const ErrorMessageBuffer& b, int) -> decltype(f.SetErrorM
 template <class F>
 void give_buffer(F&, const ErrorMessageBuffer&, long) {}
 
-// The calling device's claim word and message, allocated once per device.
+// The calling device's claim word and message, allocated once per device
+// (under a lock, so that host threads starting at once allocate it once).
+// Schedules on one device share it: as in the reference, whose control
+// environment is single-threaded, one host thread schedules on a device at
+// a time.
 inline int device_buffer(int** claim, char** message) {
   static int* claims[64] = {nullptr};
+  static std::mutex lock;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DAX_GB300_ERROR_CUDA;
+  std::lock_guard<std::mutex> guard(lock);
   if (!claims[dev]) {
     void* p = nullptr;
     if (cudaMalloc(&p, sizeof(int) + kMessageSize) != cudaSuccess) return DAX_GB300_ERROR_OUT_OF_MEMORY;
