@@ -38,10 +38,11 @@ __device__ float mandelbulb_value(float cx, float cy, float cz) {
     const float thetaN = __fmul_rn(10.0f, atan2f(t, z));
     const float phiN = __fmul_rn(10.0f, atan2f(y, z));
     const float powR = powf(r2, 5.0f);
-    const float st = sinf(thetaN);
+    float st, ct;  // sincosf: bit for bit sinf and cosf (checked over every float on GB300)
+    sincosf(thetaN, &st, &ct);
     const float px = __fmul_rn(powR, __fmul_rn(st, tanf(phiN)));
     const float py = __fmul_rn(powR, __fmul_rn(st, sinf(phiN)));
-    const float pz = __fmul_rn(powR, cosf(thetaN));
+    const float pz = __fmul_rn(powR, ct);
     x = __fadd_rn(px, cx);
     y = __fadd_rn(py, cy);
     z = __fadd_rn(pz, cz);
