@@ -15,7 +15,8 @@
 //            (warp match + per-warp counts) in element order;
 //   compact  per-tile counts of the kept elements, their scan, and an
 //            order-preserving scatter (Unique = compact of "differs from the
-//            previous element", StreamCompact = compact of "stencil != 0").
+//            previous element", through shared memory for 4-byte keys;
+//            StreamCompact = compact of "stencil != 0").
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -466,6 +467,49 @@ __global__ void __launch_bounds__(kPT) k_keep_scatter(KeepTest keep, const uint3
   }
 }
 
+// The same scatter for 4-byte elements, through shared memory:
+// the tile's elements and keep flags are loaded striped (coalesced), each
+// thread ranks its 16 consecutive elements, the kept ones are gathered in
+// element order in shared memory, and the tile's kept run is written out
+// striped (coalesced) at its offset.
+__global__ void __launch_bounds__(kPT) k_keep_scatter1(KeepTest keep, const uint32_t* __restrict__ in,
+                                                       long long n, uint32_t* __restrict__ out,
+                                                       const unsigned long long* __restrict__ pre,
+                                                       int tiles) {
+  __shared__ unsigned long long s_warp[kPT / 32];
+  __shared__ uint32_t s_v[kPTile + kPTile / 32];  // the tile's elements, padded
+  __shared__ uint32_t s_o[kPTile];                // its kept elements, in order
+  __shared__ unsigned char s_f[kPTile];           // its keep flags
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long b = (long long)tile * kPTile;
+#pragma unroll 4
+    for (int e = 0; e < kPI; ++e) {
+      const int li = e * kPT + threadIdx.x;
+      const long long i = b + li;
+      const bool ok = i < n;
+      s_f[li] = ok && keep(i) ? 1 : 0;
+      s_v[pad(li)] = in ? (ok ? in[i] : 0u) : (uint32_t)i;
+    }
+    __syncthreads();
+    uint32_t flags = 0;
+    unsigned long long c = 0;
+#pragma unroll
+    for (int e = 0; e < kPI; ++e)
+      if (s_f[threadIdx.x * kPI + e]) {
+        flags |= 1u << e;
+        ++c;
+      }
+    unsigned long long tot;
+    unsigned long long pos = block_exclusive(c, s_warp, &tot);
+    for (uint32_t f = flags; f; f &= f - 1, ++pos)
+      s_o[pos] = s_v[pad(threadIdx.x * kPI + __ffs(f) - 1)];
+    __syncthreads();
+    const unsigned long long base = pre[tile];
+    for (int j = threadIdx.x; j < (int)tot; j += kPT) out[base + j] = s_o[j];
+    __syncthreads();
+  }
+}
+
 // Kept elements of `in` (or their indices) into `out`; the count goes to
 // cnt_pre[tiles] on the device.  cnt_pre holds sum_slots(n) entries.
 void keep_pass(const KeepTest& keep, const void* in, int words, long long n, void* out,
@@ -474,8 +518,17 @@ void keep_pass(const KeepTest& keep, const void* in, int words, long long n, voi
   const int b = resident((const void*)k_keep_count, kPT, num_sms, tiles);
   k_keep_count<<<b, kPT, 0, s>>>(keep, n, cnt_pre, tiles);
   scan_sums<unsigned long long>(cnt_pre, tiles, cnt_pre + tiles + 1, s);
-  k_keep_scatter<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), words, n,
-                                   static_cast<uint32_t*>(out), cnt_pre, tiles);
+  // Unique of 4-byte keys through shared memory: its test reads each key and
+  // its predecessor, which the per-thread scatter loads with a 64-byte lane
+  // stride (0.97 -> 0.78 ms for 100 M keys).  A stencil compaction stays on
+  // the per-thread scatter, which reads only the kept values (0.44 ms against
+  // 0.84 ms staged, 30 % kept).
+  if (keep.mode == 2 && words == 1)
+    k_keep_scatter1<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), n,
+                                      static_cast<uint32_t*>(out), cnt_pre, tiles);
+  else
+    k_keep_scatter<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), words, n,
+                                     static_cast<uint32_t*>(out), cnt_pre, tiles);
 }
 
 // ---- sort driver -----------------------------------------------------------
