@@ -75,6 +75,7 @@ SIGNATURES = {
     "dax_gb300_threshold_classify_count": ([gp, vp, f32, f32, vp, vp], i32),
     "dax_gb300_threshold_scratch_bytes": ([gp], sz),
     "dax_gb300_threshold_count": ([gp, vp, f32, f32, vp, sz, vp], i32),
+    "dax_gb300_threshold_compact_point_field": ([gp, vp, sz, vp, ctypes.c_int, vp, i64, vp], i32),
     "dax_gb300_threshold_totals": ([vp, ctypes.POINTER(i64), ctypes.POINTER(i64), vp], i32),
     "dax_gb300_threshold_generate": ([gp, vp, f32, f32, vp, sz, vp, i64, vp, vp, i64, vp], i32),
     "dax_gb300_cell_gradient": ([gp, vp, vp, vp], i32),

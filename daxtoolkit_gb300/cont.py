@@ -570,6 +570,28 @@ def threshold(grid, field, lo, hi, compact_field=True, scratch=None, stream=None
     return dict(conn=conn, coords=coords, field=fout)
 
 
+def threshold_compact_point_field(grid, scratch, used_points, field, out=None, stream=None):
+    """CompactPointField of a threshold (DispatcherGenerateTopology.h:98-113):
+    the point field ``field`` ([P] or [P, k] float32) at the used points, in
+    the order of the threshold's coordinates.  ``scratch`` holds the
+    threshold count pass of the same grid; ``used_points`` is its U."""
+    if not isinstance(field, torch.Tensor) or field.dim() not in (1, 2):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE, "the point field must be [P] or [P, k]")
+    k = 1 if field.dim() == 1 else field.shape[1]
+    if (field.dtype != torch.float32 or not field.is_contiguous() or k < 1
+            or field.shape[0] != grid.GetNumberOfPoints() or not (field.is_cuda or field.is_pinned())):
+        raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
+                                        "the point field must be a contiguous float32 [P] or [P, k] "
+                                        "CUDA (or page-locked) tensor")
+    if out is None:
+        shape = (used_points,) if field.dim() == 1 else (used_points, k)
+        out = torch.empty(shape, dtype=torch.float32, device=_out_device(field))
+    g = grid.desc()
+    capi.call("dax_gb300_threshold_compact_point_field", ctypes.byref(g), _ptr(scratch),
+              scratch.numel(), _ptr(field), k, _ptr(out), used_points, _stream(stream))
+    return out
+
+
 def cell_gradient(grid, field, out=None, stream=None):
     _require_field(field, grid)
     g = grid.desc()
@@ -709,13 +731,23 @@ class DispatcherGenerateTopology:
         if self.threshold is None:
             raise capi.ErrorControlBadValue(capi.ERROR_BAD_VALUE,
                                             "the GB300 path needs the ThresholdCount worklet")
+        self._scratch = Scratch()  # kept: CompactPointField reads its count pass
         out = threshold(grid, field, self.threshold.ThresholdMin, self.threshold.ThresholdMax,
-                        stream=stream)
+                        scratch=self._scratch, stream=stream)
         self._field = out["field"]
+        self._grid = grid
+        self._used = out["coords"].shape[0]
         return UnstructuredGrid(out["coords"], out["conn"])
 
-    def CompactPointField(self, field=None):
-        return self._field
+    def CompactPointField(self, field=None, stream=None):
+        """The input point field ([P] or [P, k]) at the used points, in the
+        order of the output coordinates (DispatcherGenerateTopology.h:98-113);
+        with no argument, the thresholded field itself."""
+        if field is None:
+            return self._field
+        buf = self._scratch.get(capi.lib().dax_gb300_threshold_scratch_bytes(
+            ctypes.byref(self._grid.desc())))
+        return threshold_compact_point_field(self._grid, buf, self._used, field, stream=stream)
 
 
 class MarchingCubesBatch:

@@ -873,6 +873,30 @@ int dax_gb300_threshold_totals(const void* d_scratch, int64_t* kept_cells, int64
   return read_totals(d_scratch, kept_cells, used_points, static_cast<cudaStream_t>(stream));
 }
 
+int dax_gb300_threshold_compact_point_field(const dax_gb300_uniform_grid* grid,
+                                            const void* d_scratch, size_t scratch_bytes,
+                                            const float* d_in, int components, float* d_out,
+                                            int64_t point_capacity, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!has_cells(g)) return DAX_GB300_SUCCESS;
+  if (!d_scratch || !d_in || (!d_out && point_capacity > 0))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL scratch, input or output");
+  if (components < 1 || point_capacity < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "components must be >= 1 and the capacity >= 0");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
+  if ((st = device_view(d_in, "point field"))) return st;
+  const Layout L = layout(g);
+  if (scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_threshold_scratch_bytes()");
+  void* sc = const_cast<void*>(d_scratch);
+  daxgb::launch_thr_compact_field(g, at<uint32_t>(sc, L.used), L.m.offsets(sc).wv,
+                                  at<Info>(sc, L.m.info), d_in, components, d_out, point_capacity,
+                                  num_sms(), static_cast<cudaStream_t>(stream));
+  return check_launch("threshold point-field compaction kernel");
+}
+
 int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
                                  float lo, float hi, void* d_scratch, size_t scratch_bytes,
                                  int32_t* d_conn, int64_t cell_capacity, float* d_coords,

@@ -103,6 +103,11 @@ void launch_interpolate_n(const int32_t* ra, const int32_t* rb, const float* rw,
 // launch_word_scan; then the emit.
 void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint32_t* used,
                       uint32_t* wc, uint32_t* tile_tot, int num_sms, cudaStream_t s);
+// CompactPointField of the threshold: `comps` floats per point of `in`,
+// compacted to the used points (after the count pass on the same scratch).
+void launch_thr_compact_field(const Grid& g, const uint32_t* used, const uint32_t* wv, Info* info,
+                              const float* in, int comps, float* out, long long cap, int num_sms,
+                              cudaStream_t s);
 void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const uint32_t* kept,
                      const uint32_t* used, Info* info, int32_t* conn, long long kcap,
                      float* coords, float* fout, long long ucap, int num_sms, cudaStream_t s);

@@ -337,6 +337,46 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
   }
 }
 
+// CompactPointField of DispatcherGenerateTopology (:98-113): any point
+// field of `comps` floats per point, compacted to the used points in point
+// order -- the order of the threshold's output coordinates.  A warp per row
+// word, lane = bit: a used point's output index is its word's used-point
+// offset plus its rank in the word.  Needs the count pass (used masks, word
+// offsets, totals) on the same scratch; writes nothing when the used points
+// exceed `cap`.
+__global__ void __launch_bounds__(256) k_thr_compact_field(Grid g, const uint32_t* __restrict__ used,
+                                                           const uint32_t* __restrict__ wv,
+                                                           Info* __restrict__ info,
+                                                           const float* __restrict__ in, int comps,
+                                                           float* __restrict__ out, long long cap) {
+  const long long U = info->total_b;
+  if (U > cap || (info->error & (kErrOverflow | kErrTimeout))) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && U > cap) atomicOr(&info->error, kErrCapacity);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const long long W = g.R * g.wr;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long w = warp0; w < W; w += nwarps) {
+    const uint32_t u = __ldg(used + w);
+    if (!((u >> lane) & 1u)) continue;
+    int m;
+    const unsigned r = split_word(g, (unsigned)w, m);
+    const long long p = (long long)r * g.nx + 32ll * m + lane;
+    const long long id = (long long)__ldg(wv + w) + __popc(u & ((1u << lane) - 1u));
+    for (int c = 0; c < comps; ++c) out[id * comps + c] = __ldg(in + p * comps + c);
+  }
+}
+
+void launch_thr_compact_field(const Grid& g, const uint32_t* used, const uint32_t* wv, Info* info,
+                              const float* in, int comps, float* out, long long cap, int num_sms,
+                              cudaStream_t s) {
+  const long long want = (g.R * g.wr + 7) / 8;  // a warp per word, 8 warps a block
+  const int blocks = resident_blocks(k_thr_compact_field, 256, 0, num_sms, want);
+  k_thr_compact_field<<<blocks, 256, 0, s>>>(g, used, wv, info, in, comps, out, cap);
+}
+
 void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const uint32_t* kept,
                      const uint32_t* used, Info* info, int32_t* conn, long long kcap,
                      float* coords, float* fout, long long ucap, int num_sms, cudaStream_t s) {

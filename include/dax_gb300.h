@@ -440,6 +440,20 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
                                  int32_t* d_conn, int64_t cell_capacity, float* d_coords,
                                  float* d_field_out, int64_t point_capacity, void* stream);
 
+/* CompactPointField(input, output) of the threshold dispatcher
+ * (dax/cont/DispatcherGenerateTopology.h:98-113, a StreamCompact of the
+ * point field with the used-point mask): `components` floats per point of
+ * d_in, written for the used points in point order -- the order of the
+ * compacted coordinates -- to d_out (float[U][components]).  Needs
+ * dax_gb300_threshold_count on the same scratch and grid; independent of
+ * dax_gb300_threshold_generate.  A capacity below U writes nothing and
+ * reports DAX_GB300_ERROR_CAPACITY at the next dax_gb300_threshold_totals.
+ * Asynchronous. */
+int dax_gb300_threshold_compact_point_field(const dax_gb300_uniform_grid* grid,
+                                            const void* d_scratch, size_t scratch_bytes,
+                                            const float* d_in, int components, float* d_out,
+                                            int64_t point_capacity, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* CellGradient                                                              */
 /* ------------------------------------------------------------------------ */

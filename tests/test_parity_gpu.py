@@ -120,6 +120,56 @@ def test_threshold(gb300, oracle_best, case):
     assert np.array_equal(_bits(out["field"].cpu().numpy()), _bits(ref["field"]))
 
 
+@pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
+def test_threshold_compact_point_field(gb300, oracle_best, case):
+    """DispatcherGenerateTopology::CompactPointField with any point field:
+    compacting the thresholded field itself gives the compacted field, and
+    compacting a [P, 3] field of the grid's point coordinates gives the
+    compacted coordinates, bit for bit."""
+    name, dims, origin, spacing, emin, f, lo, hi = case
+    cont = gb300
+    og = _ogrid(dims, origin, spacing, emin)
+    ref = oracle_best.threshold_generate(og, f, oracle_best.threshold_count(og, f, lo, hi))
+    grid = _grid(cont, dims, origin, spacing, emin)
+    fd = torch.from_numpy(f).cuda()
+    w = cont.ThresholdCount(lo, hi)
+    disp = cont.DispatcherGenerateTopology(cont.DispatcherMapCell(w).Invoke(grid, fd),
+                                           threshold_worklet=w)
+    disp.Invoke(grid, fd)
+    got = disp.CompactPointField(fd)
+    assert np.array_equal(_bits(got.cpu().numpy()), _bits(ref["field"]))
+    ax = [np.float32(origin[a]) + np.float32(spacing[a]) *
+          (np.arange(dims[a]) + emin[a]).astype(np.float32) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1).astype(np.float32)
+    got3 = disp.CompactPointField(torch.from_numpy(pts).cuda())
+    assert got3.shape == ref["coords"].shape
+    assert np.array_equal(_bits(got3.cpu().numpy()), _bits(ref["coords"]))
+
+
+def test_threshold_compact_point_field_capacity(gb300):
+    """Too small an output is refused at the totals, and nothing is written."""
+    import ctypes
+    from daxtoolkit_gb300 import capi
+    cont = gb300
+    dims = (26, 26, 26)
+    grid = cont.UniformGrid(dims)
+    f = torch.from_numpy(cases.linear_field(dims)).cuda()
+    g = grid.desc()
+    n = capi.lib().dax_gb300_threshold_scratch_bytes(ctypes.byref(g))
+    scratch = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    capi.call("dax_gb300_threshold_count", ctypes.byref(g), p(f), 70.0, 82.0, p(scratch), n, s)
+    out = torch.full((3,), -7.0, device="cuda")
+    capi.call("dax_gb300_threshold_compact_point_field", ctypes.byref(g), p(scratch), n, p(f), 1,
+              p(out), 3, s)
+    K, U = ctypes.c_int64(0), ctypes.c_int64(0)
+    st = capi.lib().dax_gb300_threshold_totals(p(scratch), ctypes.byref(K), ctypes.byref(U), s)
+    assert st == capi.ERROR_CAPACITY and U.value > 3
+    assert bool((out == -7.0).all())
+
+
 @pytest.mark.parametrize("case", cases.gradient_cases(), ids=lambda c: c[0])
 def test_cell_gradient(gb300, oracle_best, case):
     name, dims, origin, spacing, emin, f = case
