@@ -737,12 +737,30 @@ class DispatcherGenerateTopology:
         self._field = out["field"]
         self._grid = grid
         self._used = out["coords"].shape[0]
-        return UnstructuredGrid(out["coords"], out["conn"])
+        if self.RemoveDuplicatePoints:
+            return UnstructuredGrid(out["coords"], out["conn"])
+        # without point removal the connectivity keeps the input's point ids
+        # (DispatcherGenerateTopology.h:199-203 skips FillPointMask and
+        # ResolveDuplicatePoints): the used points' own ids, compacted as raw
+        # 32-bit words, map the compacted ids back
+        P = grid.GetNumberOfPoints()
+        dev = out["conn"].device
+        buf = self._scratch.get(capi.lib().dax_gb300_threshold_scratch_bytes(
+            ctypes.byref(grid.desc())))
+        ids = torch.arange(P, dtype=torch.int32, device=dev).view(torch.float32)
+        used = threshold_compact_point_field(grid, buf, self._used, ids, stream=stream)
+        conn = used.view(torch.int32)[out["conn"].long()]
+        pts = torch.empty((P, 3), dtype=torch.float32, device=dev)
+        capi.call("dax_gb300_point_coordinates", ctypes.byref(grid.desc()), _ptr(pts), _stream(stream))
+        return UnstructuredGrid(pts, conn)
 
     def CompactPointField(self, field=None, stream=None):
         """The input point field ([P] or [P, k]) at the used points, in the
         order of the output coordinates (DispatcherGenerateTopology.h:98-113);
-        with no argument, the thresholded field itself."""
+        with no argument, the thresholded field itself.  Without point
+        removal nothing is compacted (the reference returns false): None."""
+        if not self.RemoveDuplicatePoints:
+            return None
         if field is None:
             return self._field
         buf = self._scratch.get(capi.lib().dax_gb300_threshold_scratch_bytes(

@@ -147,6 +147,33 @@ def test_threshold_compact_point_field(gb300, oracle_best, case):
     assert np.array_equal(_bits(got3.cpu().numpy()), _bits(ref["coords"]))
 
 
+@pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
+def test_threshold_without_point_removal(gb300, oracle_best, case):
+    """SetRemoveDuplicatePoints(false): the kept cells' connectivity in the
+    input's own point ids (the reference skips FillPointMask and
+    ResolveDuplicatePoints), and CompactPointField compacts nothing."""
+    name, dims, origin, spacing, emin, f, lo, hi = case
+    cont = gb300
+    og = _ogrid(dims, origin, spacing, emin)
+    count_ref = oracle_best.threshold_count(og, f, lo, hi)
+    nx, ny, nz = dims
+    cx, cy = nx - 1, ny - 1
+    kept = np.nonzero(count_ref)[0]
+    p = kept % cx + nx * ((kept // cx) % cy + ny * (kept // (cx * cy)))
+    off = np.array([0, 1, nx + 1, nx, nx * ny, nx * ny + 1, nx * ny + nx + 1, nx * ny + nx])
+    ref_conn = (p[:, None] + off[None, :]).astype(np.int32)
+    grid = _grid(cont, dims, origin, spacing, emin)
+    fd = torch.from_numpy(f).cuda()
+    w = cont.ThresholdCount(lo, hi)
+    disp = cont.DispatcherGenerateTopology(cont.DispatcherMapCell(w).Invoke(grid, fd),
+                                           threshold_worklet=w)
+    disp.SetRemoveDuplicatePoints(False)
+    out = disp.Invoke(grid, fd)
+    assert np.array_equal(out.GetCellConnections().cpu().numpy(), ref_conn.reshape(-1, 8))
+    assert out.GetNumberOfPoints() == nx * ny * nz
+    assert disp.CompactPointField(fd) is None
+
+
 def test_threshold_compact_point_field_capacity(gb300):
     """Too small an output is refused at the totals, and nothing is written."""
     import ctypes
