@@ -170,6 +170,25 @@ class Oracle:
         U = pu.value
         return dict(conn=conn[:8 * K].reshape(K, 8), coords=coords[:U], field=fout[:U])
 
+    @staticmethod
+    def threshold_compact_point_field(g, count, field):
+        """CompactPointField of the threshold dispatcher
+        (dax/cont/DispatcherGenerateTopology.h:98-113): FillPointMask over the
+        kept cells' 8 corner ids (:206-227, corners in TopologyUniform order,
+        dax/exec/internal/TopologyUniform.h:150-157), then StreamCompact of
+        the point field ([P] or [P, k]) with that mask
+        (DeviceAdapterAlgorithmGeneral.h:769-830): the used points' values
+        in point order."""
+        nx, ny, nz = grid_dims(g)
+        cx, cy = nx - 1, ny - 1
+        kept = np.nonzero(np.asarray(count))[0].astype(np.int64)
+        p = kept % cx + nx * ((kept // cx) % cy + ny * (kept // (cx * cy)))
+        off = np.array([0, 1, nx + 1, nx, nx * ny, nx * ny + 1, nx * ny + nx + 1, nx * ny + nx],
+                       np.int64)
+        mask = np.zeros(nx * ny * nz, bool)
+        mask[(p[:, None] + off[None, :]).ravel()] = True
+        return np.asarray(field)[mask]
+
     def slice_count(self, g, origin, normal):
         o = np.asarray(origin, np.float32)
         nrm = np.asarray(normal, np.float32)

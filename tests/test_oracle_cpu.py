@@ -189,3 +189,23 @@ def test_gradient_port_matches_reference_build(case):
     a = oracle.Oracle("port").cell_gradient(g, f)
     b = oracle.Oracle("reference").cell_gradient(g, f)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
+def test_threshold_compact_point_field_restatement(case):
+    """The numpy CompactPointField (FillPointMask + StreamCompact) of the
+    threshold field and of the point coordinates equals the C oracle's
+    compacted field and coordinates (both from ResolveDuplicatePoints)."""
+    name, dims, origin, spacing, emin, f, lo, hi = case
+    port = oracle.Oracle("port")
+    g = oracle.make_grid(dims, origin, spacing, emin)
+    count = port.threshold_count(g, f, lo, hi)
+    out = port.threshold_generate(g, f, count)
+    got = oracle.Oracle.threshold_compact_point_field(g, count, f)
+    assert np.array_equal(got.view(np.uint32), out["field"].view(np.uint32))
+    ax = [np.float32(origin[a]) + np.float32(spacing[a]) *
+          (np.arange(dims[a]) + emin[a]).astype(np.float32) for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1).astype(np.float32)
+    got3 = oracle.Oracle.threshold_compact_point_field(g, count, pts)
+    assert np.array_equal(got3.view(np.uint32), out["coords"].view(np.uint32))

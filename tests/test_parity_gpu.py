@@ -145,6 +145,13 @@ def test_threshold_compact_point_field(gb300, oracle_best, case):
     got3 = disp.CompactPointField(torch.from_numpy(pts).cuda())
     assert got3.shape == ref["coords"].shape
     assert np.array_equal(_bits(got3.cpu().numpy()), _bits(ref["coords"]))
+    # any k-component field, against the oracle's FillPointMask + StreamCompact
+    import oracle
+    rnd = np.random.default_rng(7).standard_normal((f.size, 4)).astype(np.float32)
+    want = oracle.Oracle.threshold_compact_point_field(og, oracle_best.threshold_count(og, f, lo, hi),
+                                                       rnd)
+    got4 = disp.CompactPointField(torch.from_numpy(rnd).cuda())
+    assert np.array_equal(_bits(got4.cpu().numpy()), _bits(want))
 
 
 @pytest.mark.parametrize("case", cases.threshold_cases(), ids=lambda c: c[0])
