@@ -126,6 +126,18 @@ def threshold_cases():
     d = (130, 9, 6)
     out.append(("x130", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 5, 16, noise=0.2),
                 0.2, 0.8))
+    # rows of exactly 4 and of 8 bit words (the count passes take four words
+    # of one row at a time), with an extent offset; and a row of 3 words,
+    # whose 4-word groups all straddle rows
+    d = (100, 11, 7)
+    out.append(("wr4_100x11x7_offset", d, (0.5, -1.0, 2.0), (0.01, 0.1, 0.2), (-7, 3, 1),
+                random_blobs(d, 4, 21, noise=0.1), -0.2, 0.5))
+    d = (250, 6, 5)
+    out.append(("wr8_250x6x5", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 6, 22, noise=0.1),
+                -0.05, 0.4))
+    d = (70, 13, 9)
+    out.append(("wr3_70x13x9", d, (0, 0, 0), (1, 1, 1), (0, 0, 0), random_blobs(d, 3, 23, noise=0.1),
+                -0.2, 0.5))
     out.append(("none_kept", (9, 8, 7), (0, 0, 0), (1, 1, 1), (0, 0, 0),
                 np.ones(9 * 8 * 7, np.float32), 2.0, 3.0))
     out.append(("all_kept", (9, 8, 7), (0, 0, 0), (1, 1, 1), (0, 0, 0),
