@@ -9,7 +9,7 @@ flush is needed between steps.
 
 Reported:
   value        cells/s over all ranks, device-timed (CUDA events, field in HBM),
-               with --frames frames in flight (default 3): consecutive frames go
+               with --frames frames in flight (default 4): consecutive frames go
                to separate streams, each with its own field copy, scratch and
                outputs, so one frame's bandwidth-bound classification overlaps
                the latency-bound count/scan/emit of the previous ones; the
@@ -200,6 +200,27 @@ def cpu_baseline(field_host, dims, spacing, iso, target_s, kind_pref="reference"
             "sample": "first %d of %d z-planes of the same field (%dx%dx%d points), "
                       "count + merged generate" % (kz, nz, nx, ny, kz),
             "seconds": t}
+
+
+def reference_parity(field_host, dims, spacing, iso, verts, conn):
+    """The timed frames' merged surface against the CPU implementation
+    (the reference's own worklets where they compiled) on the whole field,
+    bit for bit; run after the timed region."""
+    import numpy as np
+    import oracle
+    O, cores = _ref_oracle()
+    g = oracle.make_grid(dims, spacing=spacing)
+    count, _ = O.mc_count(g, field_host, iso)
+    ref = O.mc_generate(g, field_host, iso, count, merge=True)
+    c = conn.cpu().numpy()
+    v = verts.cpu().numpy()
+    topo = c.shape == ref["conn"].shape and bool(np.array_equal(c, ref["conn"]))
+    pos = v.shape == ref["verts"].shape and bool(
+        np.array_equal(v.view(np.uint32), ref["verts"].view(np.uint32)))
+    return {"against": "reference" if O.kind == "reference" else "port",
+            "what": "merged triangles and vertices of the whole %dx%dx%d field" % tuple(dims),
+            "topology": topo, "positions_bits": pos,
+            "triangles": int(ref["conn"].shape[0]), "merged_vertices": int(ref["verts"].shape[0])}
 
 
 def _ref_oracle(threads=None):
@@ -925,10 +946,17 @@ def main():
     }
     if not args.no_extras:
         line.update(extra_measurements(field, grid, dims, iso, peak, stream, dev))
+    if rank == 0:
+        line["parity"] = reference_parity(field.cpu().numpy(), dims, spacing, iso, verts, conn)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fh = field.cpu().numpy()
         cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cs = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds, threads=1)
+        line["cpu_baseline_serial"] = {k: cs[k] for k in ("value", "unit", "cores", "kind",
+                                                          "sample")}
+        line["cpu_baseline_serial"]["adapter"] = (
+            "Serial: one thread, the std:: algorithms of DeviceAdapterAlgorithmSerial.h")
         if "slice" in line:
             sl = cpu_slice_baseline(dims, spacing, (0.45, 0.5, 0.55), (0.3, 0.9, -0.3), 4.0)
             sl["gpu_over_cpu"] = line["slice"]["cells_per_s"] / sl["value"]

@@ -181,8 +181,6 @@ int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
   if (e != cudaSuccess) return cuda_fail(e, "reading totals");
   if (a) *a = h.total_a;
   if (b) *b = h.total_b;
-  if (h.error & daxgb::kErrTimeout)
-    return fail(DAX_GB300_ERROR_TIMEOUT, "scan look-back wait expired on the device");
   if (h.error & daxgb::kErrOverflow)
     return fail(DAX_GB300_ERROR_UNSUPPORTED, "more than 2^31-1 triangles or vertices");
   if (h.error & daxgb::kErrBadCount)
@@ -874,7 +872,7 @@ int dax_gb300_threshold_totals(const void* d_scratch, int64_t* kept_cells, int64
 }
 
 int dax_gb300_threshold_compact_point_field(const dax_gb300_uniform_grid* grid,
-                                            const void* d_scratch, size_t scratch_bytes,
+                                            void* d_scratch, size_t scratch_bytes,
                                             const float* d_in, int components, float* d_out,
                                             int64_t point_capacity, void* stream) {
   Grid g;
@@ -890,7 +888,7 @@ int dax_gb300_threshold_compact_point_field(const dax_gb300_uniform_grid* grid,
   const Layout L = layout(g);
   if (scratch_bytes < L.total)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_threshold_scratch_bytes()");
-  void* sc = const_cast<void*>(d_scratch);
+  void* sc = d_scratch;  // the kernel raises kErrCapacity in the Info block
   daxgb::launch_thr_compact_field(g, at<uint32_t>(sc, L.used), L.m.offsets(sc).wv,
                                   at<Info>(sc, L.m.info), d_in, components, d_out, point_capacity,
                                   num_sms(), static_cast<cudaStream_t>(stream));

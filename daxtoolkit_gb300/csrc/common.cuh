@@ -7,7 +7,6 @@
 //            (r, m) covers points 32m..32m+31 of point row r and the cells
 //            with those first points; per-word counts, exclusive offsets and
 //            masks are uint32[W] arrays in that order
-//   status : uint64[chains][tiles]      decoupled look-back state
 // "Row" always means a row of POINTS (fixed j, k); the cells whose first point
 // lies in point row r form cell row r (valid when j < ny-1 and k < nz-1).
 // Cell id order (dax/Extent.h:128-137) equals row-word order restricted to
@@ -164,7 +163,6 @@ struct Info {
   int pad[7];
 };
 
-constexpr int kErrTimeout = 1;     // a look-back wait gave up
 constexpr int kErrCapacity = 2;    // output buffer too small
 constexpr int kErrOverflow = 4;    // more than 2^31 - 1 triangles or vertices
 constexpr int kErrBadIndex = 8;    // a cell lists a point id outside [0, P)
@@ -282,23 +280,6 @@ __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, 
 
 __device__ __forceinline__ uint32_t low_mask(int n) {
   return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
-}
-
-// ---- decoupled look-back ------------------------------------------------
-// Status word: bits 63..62 = flag (0 none, 1 aggregate, 2 inclusive prefix),
-// bits 61..0 = value.
-constexpr unsigned long long kFlagAgg = 1ull << 62;
-constexpr unsigned long long kFlagInc = 2ull << 62;
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr int kSpinLimit = 1 << 22;   // ~0.3 s of 64 ns sleeps, then give up
-
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // Block-wide sums of three per-thread values (256 threads); all threads get

@@ -617,7 +617,7 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
   const long long T = info->total_a;
   const long long V = merge ? info->total_b : 3 * T;
   A = info->total_c;
-  if (T > tcap || V > vcap || (info->error & (kErrOverflow | kErrTimeout))) {
+  if (T > tcap || V > vcap || (info->error & kErrOverflow)) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
       atomicOr(&info->error, kErrCapacity);
     return false;

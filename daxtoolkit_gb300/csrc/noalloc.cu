@@ -35,6 +35,9 @@ void* g_scratch_ptr[kMaxDevices] = {nullptr};
 // Device address of the scratch on the current device, looked up once per
 // device with that device current (the first call on each device does this
 // set-up, which is why that first call belongs outside any stream capture).
+// The address is kept for the life of the process, so a cudaDeviceReset
+// after the first call on a device is not supported: the reset unloads the
+// module that holds the array.
 int scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -58,6 +61,32 @@ int scratch_address(void** out) {
   }
   *out = g_scratch_ptr[dev];
   return DAX_GB300_SUCCESS;
+}
+
+// d_totals must be memory the device can write 8-byte words to: device or
+// managed memory, or page-locked host memory with a device mapping (then its
+// device address is used).  Pageable host memory and pointers off an 8-byte
+// boundary are refused before anything is queued.
+int totals_view(int64_t** p) {
+  if (reinterpret_cast<uintptr_t>(*p) & 7) {
+    daxgb::set_last_error("d_totals must be 8-byte aligned");
+    return DAX_GB300_ERROR_BAD_VALUE;
+  }
+  cudaPointerAttributes a;
+  const cudaError_t e = cudaPointerGetAttributes(&a, *p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    daxgb::set_last_error("d_totals is not memory known to CUDA");
+    return DAX_GB300_ERROR_BAD_VALUE;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return DAX_GB300_SUCCESS;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    *p = static_cast<int64_t*>(a.devicePointer);
+    return DAX_GB300_SUCCESS;
+  }
+  daxgb::set_last_error("d_totals is pageable host memory: pass device memory or page-locked "
+                        "host memory");
+  return DAX_GB300_ERROR_BAD_VALUE;
 }
 
 // Copies the pipeline's totals and device error bits out of the scratch.
@@ -89,8 +118,10 @@ int dax_gb300_mc_noalloc(const dax_gb300_uniform_grid* grid, const float* d_fiel
                           std::to_string(kNoAllocScratchBytes) + " bytes (32 MiB)");
     return DAX_GB300_ERROR_UNSUPPORTED;
   }
+  int st = totals_view(&d_totals);
+  if (st) return st;
   void* scratch = nullptr;
-  int st = scratch_address(&scratch);
+  st = scratch_address(&scratch);
   if (st) return st;
   // the count pass writes every scratch byte the generate pass reads
   st = dax_gb300_mc_count(grid, d_field, isovalue, scratch, kNoAllocScratchBytes, stream);

@@ -43,7 +43,8 @@ typedef enum dax_gb300_status {
   DAX_GB300_ERROR_CUDA = 4,
   /* an output buffer is smaller than the result; nothing was written */
   DAX_GB300_ERROR_CAPACITY = 5,
-  /* a bounded device-side wait (scan look-back) gave up */
+  /* reserved for a bounded device-side wait that gave up; no entry point of
+     this version waits on the device, so none returns it */
   DAX_GB300_ERROR_TIMEOUT = 6,
   /* grid shape outside what the kernels support (see each call) */
   DAX_GB300_ERROR_UNSUPPORTED = 7
@@ -182,9 +183,13 @@ int dax_gb300_interpolate_point_field(const int32_t* d_rec_first, const int32_t*
  * on the GPU -- on different streams, or from different host threads -- race
  * and must be serialised by the caller.  The first call on each device looks
  * up the array's device address; make that first call outside any stream
- * capture.  d_totals (device int64[3]) receives the triangle count, the
- * vertex count of the merged output, and the device error bits (0 = ok; 2 =
- * an output capacity was too small and nothing was written).
+ * capture, and do not reset the device (cudaDeviceReset) after it: the
+ * looked-up address is kept for the life of the process.  d_totals (int64[3],
+ * 8-byte aligned, in device or managed memory or in page-locked host memory
+ * with a device mapping; anything else is refused with
+ * DAX_GB300_ERROR_BAD_VALUE before any work is queued) receives the triangle
+ * count, the vertex count of the merged output, and the device error bits
+ * (0 = ok; 2 = an output capacity was too small and nothing was written).
  * Asynchronous. */
 int dax_gb300_mc_noalloc(const dax_gb300_uniform_grid* grid, const float* d_field, float isovalue,
                          int merge, float* d_verts, int64_t vert_capacity, int32_t* d_conn,
@@ -450,7 +455,7 @@ int dax_gb300_threshold_generate(const dax_gb300_uniform_grid* grid, const float
  * reports DAX_GB300_ERROR_CAPACITY at the next dax_gb300_threshold_totals.
  * Asynchronous. */
 int dax_gb300_threshold_compact_point_field(const dax_gb300_uniform_grid* grid,
-                                            const void* d_scratch, size_t scratch_bytes,
+                                            void* d_scratch, size_t scratch_bytes,
                                             const float* d_in, int components, float* d_out,
                                             int64_t point_capacity, void* stream);
 

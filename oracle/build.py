@@ -10,8 +10,8 @@ Two libraries come out of this:
   headers (``Configure.h`` and the ``VectorOperations.h`` instances) that the
   reference's CMake would normally produce.
 
-The reference tree is read in place (``DAX_REFERENCE_DIR``, default
-``/root/reference``); nothing from it is copied into the repository.  Where the
+The reference tree is read in place (``DAX_REFERENCE_DIR``, else a
+``reference`` directory beside the repository); nothing from it is copied into the repository.  Where the
 tree is absent the reference library is simply not built and callers fall back
 to the C restatement.  Everything compiles with ``-ffp-contract=off`` so that
 float expressions round exactly as written (no fused multiply-add), which is
@@ -27,7 +27,18 @@ BUILD = os.path.join(HERE, "build")
 REF_OUT = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 REF_SO = os.path.join(REF_OUT, "libdaxref.so")
-REFERENCE_DIR = os.environ.get("DAX_REFERENCE_DIR", "/root/reference")
+
+
+def _reference_dir():
+    """The DaxToolkit source tree: ``DAX_REFERENCE_DIR`` when set, else a
+    ``reference`` directory beside this repository's root."""
+    env = os.environ.get("DAX_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+
+
+REFERENCE_DIR = _reference_dir()
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fPIC", "-shared"]
 

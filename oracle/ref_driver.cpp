@@ -8,7 +8,7 @@
 // algorithms step by step.
 //
 // TEST INFRASTRUCTURE ONLY: used to pin the C oracle (dax_oracle.c) and as
-// the timed CPU baseline.  Built by build_ref.sh into oracle/_ref/.
+// the timed CPU baseline.  Built by oracle/build.py into oracle/_ref/.
 //
 // With threads > 1 the per-cell / per-output loops run under OpenMP and the
 // scan and sort use libstdc++'s parallel mode, the CPU analogue of the

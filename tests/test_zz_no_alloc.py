@@ -79,3 +79,37 @@ def test_noalloc_rejects_grid_beyond_scratch(gb300):
                                          ctypes.c_void_p(16), None)
     assert st == capi.ERROR_UNSUPPORTED
     assert b"32 MiB" in capi.lib().dax_gb300_last_error()
+
+
+def test_noalloc_refuses_totals_it_cannot_write(gb300):
+    """d_totals off an 8-byte boundary, or in pageable host memory, is refused
+    before any work is queued; the outputs stay untouched."""
+    from daxtoolkit_gb300 import capi
+    cont = gb300
+    dims = (40, 36, 30)
+    grid = _desc(cont, dims)
+    g = grid.desc()
+    field = torch.from_numpy(cases.random_blobs(dims, 3, 12, noise=0.05)).cuda()
+    verts = torch.full((4096, 3), -1.0, dtype=torch.float32, device="cuda")
+    conn = torch.full((4096, 3), -1, dtype=torch.int32, device="cuda")
+    dev_totals = torch.zeros(4, dtype=torch.int64, device="cuda")
+    host_totals = np.zeros(3, np.int64)  # pageable: the device cannot write it
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L = capi.lib()
+    for bad in (ctypes.c_void_p(dev_totals.data_ptr() + 4),
+                ctypes.c_void_p(host_totals.ctypes.data)):
+        st = L.dax_gb300_mc_noalloc(ctypes.byref(g), p(field), 0.5, 1, p(verts), 4096, p(conn),
+                                    4096, bad, s)
+        assert st == capi.ERROR_BAD_VALUE, L.dax_gb300_last_error()
+    torch.cuda.synchronize()
+    assert bool((conn == -1).all()) and bool((verts == -1.0).all())
+    assert not host_totals.any() and not bool(dev_totals.any())
+    # page-locked host memory with a device mapping is accepted
+    pinned = torch.full((3,), -1, dtype=torch.int64, pin_memory=True)
+    st = L.dax_gb300_mc_noalloc(ctypes.byref(g), p(field), 0.5, 1, p(verts), 4096, p(conn), 4096,
+                                ctypes.c_void_p(pinned.data_ptr()), s)
+    assert st == 0, L.dax_gb300_last_error()
+    torch.cuda.synchronize()
+    ref = cont.marching_cubes(grid, field, 0.5, merge=True)
+    assert pinned[0].item() == ref["conn"].shape[0] and pinned[2].item() == 0
