@@ -9,11 +9,13 @@ flush is needed between steps.
 
 Reported:
   value        cells/s over all ranks, device-timed (CUDA events, field in HBM),
-               with --frames frames in flight (default 4): consecutive frames go
-               to separate streams, each with its own field copy, scratch and
-               outputs, so one frame's bandwidth-bound classification overlaps
-               the latency-bound count/scan/emit of the previous ones; the
-               one-frame-at-a-time time is reported beside it
+               one frame at a time: each frame is one dax_gb300_mc_pipeline
+               call (count + merged generate of the whole grid, its z-slabs
+               overlapping inside the call), replayed from a CUDA graph
+               captured once (--no-graph: direct calls); "frames" reports the
+               direct calls, the frame with a host read of the sizes, and the
+               two-call path one frame at a time and with --frames frames in
+               flight (default 4, each with its own field copy and stream)
   e2e          the same metric through the C ABI from page-locked host memory: every
                step copies its whole field to the device, sizes, generates and
                copies the surface back to host memory; two steps in flight on
@@ -58,6 +60,10 @@ def parse_args():
     p.add_argument("--classify-blocks-per-sm", type=int, default=3,
                    help="per-SM block limit of the classification pass while frames are in "
                         "flight, leaving room for the other frames' passes (0 = no limit)")
+    p.add_argument("--slabs", type=int, default=0,
+                   help="slabs of the pipelined frame (1..16; 0 = the library default)")
+    p.add_argument("--no-graph", action="store_true",
+                   help="time direct pipelined calls instead of a CUDA-graph replay of one")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -734,50 +740,49 @@ def main():
     verts = torch.empty((V, 3), dtype=torch.float32, device=dev)
     conn = torch.empty((T, 3), dtype=torch.int32, device=dev)
 
-    # Frames in flight: each slot is one complete frame -- its own copy of the
-    # field (so no frame reuses another's cache lines), its own scratch and
-    # outputs and its own stream.  Consecutive frames go to consecutive slots,
-    # so the bandwidth-bound classification of one frame overlaps the
-    # latency-bound count, scan and emit of the frames before it.
-    F = max(1, args.frames)
-    slots = []
-    for f in range(F):
-        slots.append(dict(
-            field=field if f == 0 else field.clone(),
-            scratch=scratch if f == 0 else torch.empty_like(scratch),
-            verts=verts if f == 0 else torch.empty_like(verts),
-            conn=conn if f == 0 else torch.empty_like(conn),
-            stream=torch.cuda.Stream(device=dev)))
-    for sl in slots:
-        sl["s"] = ctypes.c_void_p(sl["stream"].cuda_stream)
+    # The headline frame: dax_gb300_mc_pipeline, one complete count +
+    # generate of the whole grid per call (its slabs overlap inside the
+    # call), one frame at a time: each frame's passes are all queued on the
+    # stream after the previous frame's have finished, so nothing of two
+    # frames overlaps.  The frame's calls are captured once in a CUDA graph
+    # and replayed (the same kernels, without the host enqueue cost of the
+    # slab launches); --no-graph times the direct calls.
+    capi.call("dax_gb300_set_pipeline_slabs", args.slabs)
+    plan = (ctypes.c_int64 * 52)()
+    capi.call("dax_gb300_mc_pipeline_plan", ctypes.byref(g), 0, plan)
+    slab_count = int(plan[0])
 
-    def frame(k, inflight=F):
-        sl = slots[k % inflight]
-        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(sl["field"]), iso, ptr(sl["scratch"]),
-                  nbytes, sl["s"])
-        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(sl["field"]), iso, 1,
-                  ptr(sl["scratch"]), nbytes, ptr(sl["verts"]), V, ptr(sl["conn"]), T, None, None,
-                  None, sl["s"])
+    def pipe_frame(st=s):
+        capi.call("dax_gb300_mc_pipeline", ctypes.byref(g), ptr(field), iso, 1, ptr(scratch),
+                  nbytes, ptr(verts), V, ptr(conn), T, None, None, None, st)
 
-    def run_frames(count, inflight=F):
-        """Enqueue `count` frames between two events on the current stream."""
-        cur = torch.cuda.current_stream()
+    pipe_frame()
+    torch.cuda.synchronize()
+    graph = None
+    if not args.no_graph:
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(stream)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side, capture_error_mode="thread_local"):
+            pipe_frame(ctypes.c_void_p(side.cuda_stream))
+        torch.cuda.synchronize()
+
+    def frame():
+        if graph is not None:
+            graph.replay()
+        else:
+            pipe_frame()
+
+    def run_timed(count, fn):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(cur)
-        for sl in slots:
-            sl["stream"].wait_stream(cur)
-        for k in range(count):
-            frame(k, inflight)
-        for sl in slots:
-            cur.wait_stream(sl["stream"])
-        b.record(cur)
+        a.record(stream)
+        for _ in range(count):
+            fn()
+        b.record(stream)
         return a, b
 
-    # in flight, the classification leaves room on every SM for the other
-    # frames' count and emit passes (one frame at a time it runs unlimited)
-    capi.call("dax_gb300_set_blocks_per_sm", 0, max(0, args.classify_blocks_per_sm))
-    for k in range(max(3, args.warmup) * F):
-        frame(k)
+    for _ in range(max(3, args.warmup)):
+        frame()
     torch.cuda.synchronize()
 
     def barrier():
@@ -790,27 +795,91 @@ def main():
     time.sleep(0.3)
     barrier()
     torch.cuda.synchronize()
-    e0, e1 = run_frames(args.steps)
+    e0, e1 = run_timed(args.steps, frame)
     torch.cuda.synchronize()
     barrier()
     t_ms = e0.elapsed_time(e1)
     clocks = sampler.stop()
-    # device totals/errors and outputs of every slot after the timed region
-    for sl in slots:
-        T2, V2 = ctypes.c_int64(0), ctypes.c_int64(0)
-        capi.call("dax_gb300_mc_totals", ptr(sl["scratch"]), ctypes.byref(T2), ctypes.byref(V2),
-                  sl["s"])
-        assert (T2.value, V2.value) == (T, V)
-        assert torch.equal(sl["verts"], verts) and torch.equal(sl["conn"], conn)
-    # one frame at a time: the single-frame latency
-    capi.call("dax_gb300_set_blocks_per_sm", 0, 0)
-    reps1 = max(5, min(args.steps, 300))
-    a1, b1 = run_frames(reps1, 1)
-    torch.cuda.synchronize()
-    ms_one = a1.elapsed_time(b1) / reps1
+    T2, V2 = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(T2), ctypes.byref(V2), s)
+    assert (T2.value, V2.value) == (T, V)
+    verts_pipe, conn_pipe = verts.clone(), conn.clone()
     t_ms = max_over_ranks(t_ms, world, dev)
     ms_per_step = t_ms / args.steps
     value = weak_value(world, C, args.steps, t_ms)
+    reps1 = max(5, min(args.steps, 300))
+
+    def timed_frames(count, fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = run_timed(count, fn)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / count
+
+    # the same pipelined frame, direct calls (no graph), and with the host
+    # reading the sizes after every frame (the reference's timer window
+    # holds its one host sync, Benchmarks/MarchingCubes/Pipeline.h:110-132)
+    ms_direct = timed_frames(reps1, pipe_frame)
+
+    def frame_and_sizes():
+        frame()
+        Tq, Vq = ctypes.c_int64(0), ctypes.c_int64(0)
+        capi.call("dax_gb300_mc_totals", ptr(scratch), ctypes.byref(Tq), ctypes.byref(Vq), s)
+
+    ms_with_sizes = timed_frames(reps1, frame_and_sizes)
+
+    # The two-call path (dax_gb300_mc_count, then dax_gb300_mc_generate), one
+    # frame at a time, and with --frames frames in flight: consecutive frames
+    # go to separate streams, each with its own copy of the field, scratch and
+    # outputs, so one frame's classification overlaps the count, scan and
+    # emit of the frames before it.
+    F = max(1, args.frames)
+    slots = []
+    for f in range(F):
+        slots.append(dict(
+            field=field if f == 0 else field.clone(),
+            scratch=scratch if f == 0 else torch.empty_like(scratch),
+            verts=verts if f == 0 else torch.empty_like(verts),
+            conn=conn if f == 0 else torch.empty_like(conn),
+            stream=torch.cuda.Stream(device=dev)))
+    for sl in slots:
+        sl["s"] = ctypes.c_void_p(sl["stream"].cuda_stream)
+
+    def two_call_frame(k, inflight):
+        sl = slots[k % inflight]
+        capi.call("dax_gb300_mc_count", ctypes.byref(g), ptr(sl["field"]), iso, ptr(sl["scratch"]),
+                  nbytes, sl["s"])
+        capi.call("dax_gb300_mc_generate", ctypes.byref(g), ptr(sl["field"]), iso, 1,
+                  ptr(sl["scratch"]), nbytes, ptr(sl["verts"]), V, ptr(sl["conn"]), T, None, None,
+                  None, sl["s"])
+
+    def run_frames(count, inflight):
+        cur = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(cur)
+        for sl in slots:
+            sl["stream"].wait_stream(cur)
+        for k in range(count):
+            two_call_frame(k, inflight)
+        for sl in slots:
+            cur.wait_stream(sl["stream"])
+        b.record(cur)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / count
+
+    run_frames(2, 1)
+    ms_one = run_frames(reps1, 1)
+    capi.call("dax_gb300_set_blocks_per_sm", 0, max(0, args.classify_blocks_per_sm))
+    run_frames(3 * F, F)
+    ms_inflight = run_frames(reps1, F)
+    capi.call("dax_gb300_set_blocks_per_sm", 0, 0)
+    for sl in slots:
+        T3, V3 = ctypes.c_int64(0), ctypes.c_int64(0)
+        capi.call("dax_gb300_mc_totals", ptr(sl["scratch"]), ctypes.byref(T3), ctypes.byref(V3),
+                  sl["s"])
+        assert (T3.value, V3.value) == (T, V)
+        assert torch.equal(sl["verts"], verts_pipe) and torch.equal(sl["conn"], conn_pipe)
+    del slots
 
     # --- per-stage timing: K1 alone, count pass, generate pass -------------
     bits = torch.empty(L.dax_gb300_classify_words(P), dtype=torch.int32, device=dev)
@@ -919,11 +988,17 @@ def main():
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": dict(config_dict(n), frames_in_flight=F,
-                       classify_blocks_per_sm_in_flight=args.classify_blocks_per_sm,
-                       frames_note="each in-flight frame has its own field copy, scratch, "
-                                   "outputs and stream; every frame is a complete pass"),
-        "ms_per_frame_one_in_flight": ms_one,
+        "config": dict(config_dict(n), frames_in_flight=1, slabs=slab_count,
+                       call="dax_gb300_mc_pipeline (count + merged generate, slab-pipelined)",
+                       replay="CUDA graph of the frame's call, captured once" if graph is not None
+                       else "direct call per frame"),
+        "frames": {"pipelined_direct_calls_ms": ms_direct,
+                   "pipelined_with_host_size_read_ms": ms_with_sizes,
+                   "two_call_one_at_a_time_ms": ms_one,
+                   "two_call_in_flight_ms": ms_inflight, "two_call_frames_in_flight": F,
+                   "two_call_classify_blocks_per_sm_in_flight": args.classify_blocks_per_sm,
+                   "note": "ms per frame; 'in flight' frames each have their own field copy, "
+                           "scratch, outputs and stream"},
         "triangles": T, "merged_vertices": V,
         "triangles_per_s": world * T / (ms_per_step / 1e3),
         "roofline": {"bound": "hbm", "kernel": "k_classify_bits", "achieved": achieved,
@@ -940,14 +1015,15 @@ def main():
                 "steps": e2e_steps, "steps_in_flight": E,
                 "path": "C ABI; per step the field is copied from page-locked host memory to the "
                         "device and the surface back to page-locked host memory"},
-        # K1, K2a, K2b and K3 per step
-        "gpu_launches": 4 * args.steps,
+        # K1, K2a, K2b and K3 per slab, per step
+        "gpu_launches": 4 * slab_count * args.steps,
         "clocks": clocks,
     }
     if not args.no_extras:
         line.update(extra_measurements(field, grid, dims, iso, peak, stream, dev))
     if rank == 0:
-        line["parity"] = reference_parity(field.cpu().numpy(), dims, spacing, iso, verts, conn)
+        line["parity"] = reference_parity(field.cpu().numpy(), dims, spacing, iso, verts_pipe,
+                                          conn_pipe)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fh = field.cpu().numpy()
         cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)

@@ -71,6 +71,7 @@ SIGNATURES = {
     "dax_gb300_mc_count": ([gp, vp, f32, vp, sz, vp], i32),
     "dax_gb300_mc_totals": ([vp, ctypes.POINTER(i64), ctypes.POINTER(i64), vp], i32),
     "dax_gb300_mc_generate": ([gp, vp, f32, i32, vp, sz, vp, i64, vp, i64, vp, vp, vp, vp], i32),
+    "dax_gb300_mc_pipeline": ([gp, vp, f32, i32, vp, sz, vp, i64, vp, i64, vp, vp, vp, vp], i32),
     "dax_gb300_interpolate_point_field": ([vp, vp, vp, i64, vp, vp, vp], i32),
     "dax_gb300_threshold_classify_count": ([gp, vp, f32, f32, vp, vp], i32),
     "dax_gb300_threshold_scratch_bytes": ([gp], sz),
@@ -116,6 +117,10 @@ SIGNATURES = {
     "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),
     "dax_gb300_report_error": ([ctypes.c_int, ctypes.c_char_p], i32),
     "dax_gb300_set_blocks_per_sm": ([ctypes.c_int, ctypes.c_int], i32),
+    "dax_gb300_set_pipeline_slabs": ([ctypes.c_int], i32),
+    "dax_gb300_set_pipeline_options": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], i32),
+    "dax_gb300_pipeline_timeline": ([ctypes.c_int, vp, ctypes.c_int, vp], i32),
+    "dax_gb300_mc_pipeline_plan": ([gp, ctypes.c_int, vp], i32),
     "dax_gb300_selfcheck_division": ([vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
                                       ctypes.c_uint32, vp, vp], i32),
     "dax_gb300_scan_scratch_bytes": ([i64], sz),

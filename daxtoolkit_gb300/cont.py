@@ -27,7 +27,7 @@ __all__ = [
     "Tetrahedralize", "tetrahedralize", "marching_cubes_counted", "Mandlebulb",
     "MandlebulbClipCount", "MandlebulbVolume", "MandlebulbSurface", "mandlebulb_field",
     "compute_mandlebulb", "colors_and_norms", "extract_surface", "extract_cut", "point_magnitude",
-    "write_vtk",
+    "write_vtk", "marching_cubes_pipelined",
 ]
 
 
@@ -244,6 +244,30 @@ def marching_cubes(grid, field, isovalue, merge=True, records=False, scratch=Non
     if records:
         out.update(rec_first=ra, rec_second=rb, rec_weight=rw)
     return out
+
+
+def marching_cubes_pipelined(grid, field, isovalue, verts, conn, merge=True, records=None,
+                             scratch=None, stream=None, read_sizes=True):
+    """Count and generate in one slab-pipelined call (``dax_gb300_mc_pipeline``)
+    into caller-held outputs ``verts`` [>= V, 3] and ``conn`` [>= T, 3] (and,
+    if given, ``records`` = (first, second, weight) of >= V entries).  With
+    ``read_sizes`` the totals are read back (one host sync, which raises
+    ErrorControlBadValue-family errors such as the capacity error) and
+    (T, V) is returned; otherwise nothing blocks and None is returned."""
+    _require_field(field, grid)
+    g = grid.desc()
+    s = _stream(stream)
+    nbytes = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(g))
+    buf = (scratch or _scratch_for("mc")).get(nbytes)
+    ra, rb, rw = records if records is not None else (None, None, None)
+    capi.call("dax_gb300_mc_pipeline", ctypes.byref(g), _ptr(field), float(isovalue),
+              int(bool(merge)), _ptr(buf), buf.numel(), _ptr(verts), verts.shape[0], _ptr(conn),
+              conn.shape[0], _ptr(ra), _ptr(rb), _ptr(rw), s)
+    if not read_sizes:
+        return None
+    T, Vm = ctypes.c_int64(0), ctypes.c_int64(0)
+    capi.call("dax_gb300_mc_totals", _ptr(buf), ctypes.byref(T), ctypes.byref(Vm), s)
+    return T.value, (Vm.value if merge else 3 * T.value)
 
 
 def slice_field(grid, origin, normal, out=None, stream=None):

@@ -4,13 +4,16 @@
 // W = R x wr row words:
 //   marching cubes: [Info][tile totals: 3 x tiles x u32][wc: W x u32]
 //                   [wt: (W+1) x u32][wv: (W+1) x u32][act: W x u32]
-//                   [bits: bit_words(P) x u32]
+//                   [slab: 64 x u32][bits: bit_words(P) x u32]
 //   threshold:      the same, then [kept: W x u32][used: W x u32]
 // Nothing is cleared per call: every byte, the Info block included, is
 // written by the count pass before anything reads it.
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/dax_gb300.h"
@@ -88,11 +91,12 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Marching-cubes scratch: [Info][tile totals 3 x tiles][wc][wt][wv][act][bits].
+// Marching-cubes scratch: [Info][tile totals 3 x tiles][wc][wt][wv][act]
+// [slab: active-word prefixes of the pipelined call's slabs][bits].
 struct McLayout {
   long long rowwords;
   int tiles;
-  size_t info, tile, wc, wt, wv, act, bits, total;
+  size_t info, tile, wc, wt, wv, act, slab, bits, total;
   daxgb::WordOffsets offsets(void* base) const;
 };
 
@@ -106,7 +110,8 @@ McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head) {
   L.wt = align256(L.wc + 4 * (size_t)rowwords);
   L.wv = align256(L.wt + 4 * (size_t)(rowwords + 1));
   L.act = align256(L.wv + 4 * (size_t)(rowwords + 1));
-  L.bits = align256(L.act + 4 * (size_t)rowwords);
+  L.slab = align256(L.act + 4 * (size_t)rowwords);
+  L.bits = align256(L.slab + 4 * (size_t)daxgb::kSlabWords);
   L.total = align256(L.bits + 4 * (size_t)bitwords);
   return L;
 }
@@ -238,8 +243,26 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
 namespace daxgb {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
+int cached_occupancy(const void* kernel, int threads, size_t smem) {
+  static std::mutex m;
+  static std::map<std::tuple<int, const void*, int, size_t>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const auto key = std::make_tuple(dev, kernel, threads, smem);
+  std::lock_guard<std::mutex> lock(m);
+  const auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  cache[key] = per_sm;
+  return per_sm;
+}
+
 namespace {
-int g_blocks_per_sm[kTunedPasses] = {0, 0, 0};
+int g_blocks_per_sm[kTunedPasses] = {0, 0, 0, 3, 0, 1};
 }
 int tuned_blocks_per_sm(int pass) {
   return pass >= 0 && pass < kTunedPasses ? g_blocks_per_sm[pass] : 0;
@@ -369,6 +392,77 @@ int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_fie
                         d_rec_first, d_rec_second, d_rec_weight, num_sms(),
                         static_cast<cudaStream_t>(stream));
   return check_launch("mc generate kernel");
+}
+
+int dax_gb300_mc_pipeline(const dax_gb300_uniform_grid* grid, const float* d_field,
+                          float isovalue, int merge, void* d_scratch, size_t scratch_bytes,
+                          float* d_verts, int64_t vert_capacity, int32_t* d_conn,
+                          int64_t tri_capacity, int32_t* d_rec_first, int32_t* d_rec_second,
+                          float* d_rec_weight, void* stream) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!d_field || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL field or scratch");
+  if (!aligned16(d_scratch)) return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch must be 16-byte aligned");
+  if ((st = device_view(d_field, "field"))) return st;
+  if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0) || vert_capacity < 0 ||
+      tri_capacity < 0)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
+  const McLayout L = mc_layout(g);
+  if (scratch_bytes < L.total)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "scratch smaller than dax_gb300_mc_scratch_bytes()");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!has_cells(g)) {  // no cells: totals stay 0
+    cudaError_t e = cudaMemsetAsync(d_scratch, 0, sizeof(Info), s);
+    return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing scratch");
+  }
+  return daxgb::launch_mc_pipeline(g, d_field, aligned16(d_field), isovalue, merge != 0,
+                                   at<uint32_t>(d_scratch, L.bits), daxgb::bit_words(g.P),
+                                   L.offsets(d_scratch), at<Info>(d_scratch, L.info),
+                                   at<uint32_t>(d_scratch, L.slab), d_verts, vert_capacity, d_conn,
+                                   tri_capacity, d_rec_first, d_rec_second, d_rec_weight,
+                                   num_sms(), s);
+}
+
+int dax_gb300_mc_pipeline_plan(const dax_gb300_uniform_grid* grid, int slabs, int64_t* out) {
+  Grid g;
+  int st = make_grid(grid, g);
+  if (st) return st;
+  if (!out) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output");
+  const daxgb::SlabPlan p = daxgb::plan_slabs(g, slabs > 0 ? slabs : daxgb::pipeline_slabs());
+  const int n = daxgb::kMaxSlabs + 1;
+  out[0] = p.S;
+  for (int i = 0; i < n; ++i) {
+    const bool in = i <= p.S;
+    out[1 + i] = in ? p.W[i] : -1;
+    out[1 + n + i] = in ? p.E[i] : -1;
+    out[1 + 2 * n + i] = in ? p.K[i] : -1;
+  }
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_set_pipeline_options(int emit_batch, int emit_streams, int keep_field_in_l2) {
+  if (emit_batch < 0 || emit_batch > 32 || emit_streams < 0 ||
+      emit_streams > daxgb::kMaxEmitStreams || keep_field_in_l2 < -1 || keep_field_in_l2 > 1)
+    return fail(DAX_GB300_ERROR_BAD_VALUE,
+                "emit_batch in [0, 32], emit_streams in [0, 4], keep_field_in_l2 in [-1, 1]");
+  daxgb::PipeOptions o;
+  if (emit_batch > 0) o.emit_batch = emit_batch;
+  if (emit_streams > 0) o.emit_streams = emit_streams;
+  if (keep_field_in_l2 >= 0) o.keep_field = keep_field_in_l2 != 0;
+  daxgb::set_pipeline_options(o);
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_pipeline_timeline(int enable, float* h_ms, int n, int* h_slabs) {
+  return daxgb::pipeline_timeline(enable, h_ms, n, h_slabs);
+}
+
+int dax_gb300_set_pipeline_slabs(int slabs) {
+  if (slabs < 0 || slabs > daxgb::kMaxSlabs)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "slabs must be in [0, 16]");
+  daxgb::set_pipeline_slabs(slabs);
+  return DAX_GB300_SUCCESS;
 }
 
 int dax_gb300_slice_field(const dax_gb300_uniform_grid* grid, const float* origin,

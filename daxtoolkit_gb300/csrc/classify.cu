@@ -24,9 +24,24 @@ __device__ __forceinline__ uint32_t classify_point(float v, float a, float b) {
 // step keep several 512 B loads in flight per warp.  Chunks are global over
 // the grid set; each grid's chunks start on a fresh chunk, so a chunk never
 // straddles two grids and each grid's bits start on a word boundary.
-template <int MODE, bool VEC>
+//
+// [c_begin, c_end) restricts a one-grid launch to a range of chunks (the
+// slabs of the pipelined marching cubes); `init`, when not null, is the Info
+// block whose error word and emit counters this launch clears (the first
+// slab's classification runs before every other pass of a pipelined call).
+//
+// KEEP: the field is read with the default cache policy instead of
+// evict-first, so that a slab's values can still be in L2 when the emit of
+// that slab gathers its crossing-edge end points (pipelined calls).
+template <typename T>
+__device__ __forceinline__ T ld_field(const T* p, bool keep) {
+  return keep ? __ldg(p) : __ldcs(p);
+}
+
+template <int MODE, bool VEC, bool KEEP>
 __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __restrict__ bits,
-                                                       long long nwords) {
+                                                       long long nwords, long long c_begin,
+                                                       long long c_end, Info* init) {
   constexpr int UNROLL = 4;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -41,18 +56,25 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
     const float* __restrict__ f = S.one.field;
     const long long P = S.one.g.P;
     const float a = S.one.iso, b = S.one.iso_hi;
-    for (long long c0 = warp * UNROLL; c0 < nchunks; c0 += nwarps * UNROLL) {
+    if (init && blockIdx.x == 0 && threadIdx.x == 0) {
+      init->error = 0;
+      init->ticket = 0;
+      init->done = 0;
+    }
+    for (long long c0 = c_begin + warp * UNROLL; c0 < c_end; c0 += nwarps * UNROLL) {
       float4 v[UNROLL];
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const long long base = ((c0 + u) << 7) + lane * 4;
-        if (VEC && base + 3 < P) {
-          v[u] = __ldcs(reinterpret_cast<const float4*>(f + base));
+        if (c0 + u >= c_end) {
+          v[u] = make_float4(nan, nan, nan, nan);
+        } else if (VEC && base + 3 < P) {
+          v[u] = ld_field(reinterpret_cast<const float4*>(f + base), KEEP);
         } else {
-          v[u].x = base + 0 < P ? __ldcs(f + base + 0) : nan;
-          v[u].y = base + 1 < P ? __ldcs(f + base + 1) : nan;
-          v[u].z = base + 2 < P ? __ldcs(f + base + 2) : nan;
-          v[u].w = base + 3 < P ? __ldcs(f + base + 3) : nan;
+          v[u].x = base + 0 < P ? ld_field(f + base + 0, KEEP) : nan;
+          v[u].y = base + 1 < P ? ld_field(f + base + 1, KEEP) : nan;
+          v[u].z = base + 2 < P ? ld_field(f + base + 2, KEEP) : nan;
+          v[u].w = base + 3 < P ? ld_field(f + base + 3, KEEP) : nan;
         }
       }
 #pragma unroll
@@ -65,7 +87,7 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
         w |= __shfl_xor_sync(kFull, w, 1);
         w |= __shfl_xor_sync(kFull, w, 2);
         w |= __shfl_xor_sync(kFull, w, 4);
-        if ((lane & 7) == 0 && c0 + u < nchunks) bits[((c0 + u) << 2) + (lane >> 3)] = w;
+        if ((lane & 7) == 0 && c0 + u < c_end) bits[((c0 + u) << 2) + (lane >> 3)] = w;
       }
     }
   } else {
@@ -124,7 +146,7 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
     }
   }
   // zero the padding words after the last chunk (read by unaligned fetches)
-  if (blockIdx.x == 0 && threadIdx.x < 8) {
+  if (blockIdx.x == 0 && threadIdx.x < 8 && c_end == nchunks) {
     const long long w = (nchunks << 2) + threadIdx.x;
     if (w < nwords) bits[w] = 0u;
   }
@@ -132,16 +154,26 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
 
 void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
                           long long nwords, int num_sms, cudaStream_t s) {
-  const long long want = (S.chunks + 4 * 8 - 1) / (4 * 8);  // blocks of 8 warps x 4 chunks
-#define DAXGB_K1(M, V)                                                         \
+  launch_classify_range(mode, S, all_aligned, bits, nwords, 0, S.chunks, nullptr, kPassClassify,
+                        false, num_sms, s);
+}
+
+void launch_classify_range(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
+                           long long nwords, long long c_begin, long long c_end, Info* init,
+                           int pass, bool keep, int num_sms, cudaStream_t s) {
+  // blocks of 8 warps x 4 chunks
+  const long long want = (c_end - c_begin + 4 * 8 - 1) / (4 * 8);
+#define DAXGB_K1(M, V, K)                                                      \
   {                                                                            \
-    const int blocks = resident_blocks(k_classify_bits<M, V>, 256, 0, num_sms, want, kPassClassify); \
-    k_classify_bits<M, V><<<blocks, 256, 0, s>>>(S, bits, nwords);             \
+    const int blocks = resident_blocks(k_classify_bits<M, V, K>, 256, 0, num_sms, want, pass); \
+    k_classify_bits<M, V, K><<<blocks, 256, 0, s>>>(S, bits, nwords, c_begin, c_end, init); \
   }
-  if (mode == 0) {
-    if (all_aligned) DAXGB_K1(0, true) else DAXGB_K1(0, false)
+  if (mode == 0 && keep) {
+    if (all_aligned) DAXGB_K1(0, true, true) else DAXGB_K1(0, false, true)
+  } else if (mode == 0) {
+    if (all_aligned) DAXGB_K1(0, true, false) else DAXGB_K1(0, false, false)
   } else {
-    if (all_aligned) DAXGB_K1(1, true) else DAXGB_K1(1, false)
+    if (all_aligned) DAXGB_K1(1, true, false) else DAXGB_K1(1, false, false)
   }
 #undef DAXGB_K1
 }

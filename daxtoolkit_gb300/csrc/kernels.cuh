@@ -37,25 +37,46 @@ inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
 
 void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
                           long long nwords, int num_sms, cudaStream_t s);
+// One grid's chunks [c_begin, c_end) only; init != NULL clears that Info
+// block's error word and emit counters first; `pass` selects the per-SM
+// limit; keep (mode 0) reads the field with the default cache policy
+// instead of evict-first.
+void launch_classify_range(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
+                           long long nwords, long long c_begin, long long c_end, Info* init,
+                           int pass, bool keep, int num_sms, cudaStream_t s);
 void launch_cell_count(int mode, const Grid& g, const float* f, float a, float b, int32_t* count,
                        uint8_t* cases, int num_sms, cudaStream_t s);
 
 // Per-SM block limits of the marching-cubes passes (dax_gb300_set_blocks_per_sm):
 // 0 = as many as fit.  Below that, a pass leaves room on every SM for the
-// kernels of other frames in flight on other streams.
-enum TunedPass { kPassClassify = 0, kPassCount = 1, kPassEmit = 2, kTunedPasses = 3 };
+// kernels of other frames in flight on other streams.  kPassPipeClassify is
+// the classification inside the pipelined call (default 3 blocks per SM),
+// which leaves room for the count, scan and emit passes of earlier slabs.
+enum TunedPass {
+  kPassClassify = 0,
+  kPassCount = 1,
+  kPassEmit = 2,
+  kPassPipeClassify = 3,
+  kPassPipeCount = 4,
+  kPassPipeEmit = 5,
+  kTunedPasses = 6
+};
 int tuned_blocks_per_sm(int pass);
 
 // Blocks of a grid-stride kernel that are resident at once on `num_sms` SMs
 // (never more than `want`): one wave, no tail.  `pass` >= 0 applies that
 // pass's per-SM limit.
+// Occupancy of a kernel (blocks per SM at `threads` and `smem`) on the current
+// device, queried once per (device, kernel, shape) and cached: the query
+// costs microseconds of host time, which the many launches of a pipelined
+// call would otherwise pay each time.
+int cached_occupancy(const void* kernel, int threads, size_t smem);
+
 template <typename K>
 inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long long want,
                            int pass = -1) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  int per_sm = cached_occupancy(reinterpret_cast<const void*>(kernel), threads, smem);
+  if (per_sm < 1) per_sm = 1;
   if (pass >= 0) {
     const int lim = tuned_blocks_per_sm(pass);
     if (lim > 0 && lim < per_sm) per_sm = lim;
@@ -80,6 +101,49 @@ struct WordOffsets {
   uint32_t* tile;  // [3][tiles] per-tile totals
 };
 
+// Slab boundaries of the pipelined marching cubes (pipeline.cu): n
+// boundary row words e[0..n) whose active-word prefixes the scan records.
+constexpr int kMaxSlabs = 16;
+struct SlabBounds {
+  int n;
+  long long e[kMaxSlabs];
+};
+// S slabs: count/scan slab s covers tiles [tile[s], tile[s+1]) = row words
+// [W[s], W[s+1]); its emit covers the active words in [E[s], E[s+1]); its
+// classification covers chunks [K[s], K[s+1]).
+struct SlabPlan {
+  int S;
+  int tile[kMaxSlabs + 1];
+  long long W[kMaxSlabs + 1];
+  long long E[kMaxSlabs + 1];
+  long long K[kMaxSlabs + 1];
+};
+SlabPlan plan_slabs(const Grid& g, int wanted);
+void set_pipeline_slabs(int slabs);
+int pipeline_slabs();
+// The slab section of the marching-cubes scratch: slab_act[kMaxSlabs + 1],
+// then at kSlabCounters each slab's emit ticket and done counters.
+constexpr int kSlabCounters = 32;
+constexpr int kSlabWords = kSlabCounters + 2 * kMaxSlabs;
+// Pipelined call options: active words per emit batch (1..32), streams the
+// slabs' emits are dealt to (1..kMaxEmitStreams), and whether the
+// classification keeps the field in L2 for the emit's gathers.
+constexpr int kMaxEmitStreams = 4;
+// Timeline of a pipelined call, per slab: ends of K1, of the wait before the
+// count, of the count, of the scan, of the wait before the emit, of the emit.
+constexpr int kTimelinePoints = 6;
+// enable: 1 records the timeline of later calls, 0 stops, -1 leaves it; out
+// (n floats): ms since the last recorded call's start, kTimelinePoints per
+// slab; *slabs: that call's slab count.
+int pipeline_timeline(int enable, float* out, int n, int* slabs);
+struct PipeOptions {
+  int emit_batch = 8;
+  int emit_streams = 2;
+  bool keep_field = true;
+};
+void set_pipeline_options(const PipeOptions& o);
+PipeOptions pipeline_options();
+
 int word_scan_tiles(long long rowwords);
 void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
                       uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s);
@@ -89,6 +153,32 @@ void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o
 void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
                     Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
                     int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s);
+// One slab of the pipelined marching cubes (one grid): counts and scan of
+// tiles [tile_begin, tile_end); the scan records the active-word prefixes of
+// the boundaries B in slab_act.
+void launch_mc_scan_slab(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
+                         int tile_begin, int tile_end, const SlabBounds& B, uint32_t* slab_act,
+                         int pass, int num_sms, cudaStream_t s,
+                         cudaEvent_t after_count = nullptr);
+// The emit of the active words act[slab_act[0] .. slab_act[1]) of row words
+// [word_begin, word_end), capacity-checked at the offsets of range_end
+// (range_end < 0: every active word, after a complete count pass).
+// Warps take `batch` active words at a time from *ticket (reset to 0 with
+// *done by the launch's last block).  kEmitBatch: the batch of a whole-grid
+// emit.
+constexpr int kEmitBatch = 16;
+void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
+                          Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
+                          int32_t* ra, int32_t* rb, float* rw, long long word_begin,
+                          long long word_end, long long range_end, const uint32_t* slab_act,
+                          unsigned* ticket, unsigned* done, int batch, int pass, int num_sms,
+                          cudaStream_t s);
+// The whole count + generate of one grid, slab-pipelined (pipeline.cu).
+int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, bool merge,
+                       uint32_t* bits, long long nwords, const WordOffsets& o, Info* info,
+                       uint32_t* slab_act, float* verts, long long vcap, int32_t* conn,
+                       long long tcap, int32_t* ra, int32_t* rb, float* rw, int num_sms,
+                       cudaStream_t s);
 // goff[2g], goff[2g+1]: first triangle / merged vertex of grid g; then totals.
 void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff,
                          cudaStream_t s);

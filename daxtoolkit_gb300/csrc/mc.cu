@@ -166,14 +166,15 @@ constexpr int kCountWords = 4;  // consecutive row words per count group
 // tile_tot[0 / 1 / 2][tile] for the scan.
 __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __restrict__ bits,
                                                   uint32_t* __restrict__ wc,
-                                                  uint32_t* __restrict__ tile_tot, int tiles) {
+                                                  uint32_t* __restrict__ tile_tot, int tiles,
+                                                  int tile_begin, int tile_end) {
   __shared__ unsigned char s_nf[256];  // NumFaces, indexed by divergent case ids
   __shared__ uint32_t s_red[24];
   __shared__ long long s_keys[kStagedSlots];
   s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  for (int tile = tile_begin + blockIdx.x; tile < tile_end; tile += gridDim.x) {
     uint32_t st = 0, sv = 0, sa = 0;
 #pragma unroll 1
     for (int e = 0; e < kScanItems / kCountWords; ++e) {
@@ -207,11 +208,23 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
         if (hy) row_windows4(gb, pos + dy, b, b1);
         if (hz) row_windows4(gb, pos + dz, c, c1);
         if (hy && hz) row_windows4(gb, pos + dy + dz, d, d1);
+        // most groups lie wholly inside or outside: every corner window of
+        // every word equal means no crossing edge and no active cell
+        uint32_t diff = 0;
 #pragma unroll
         for (int q = 0; q < kCountWords; ++q) {
-          const CornerWords w{a[q], a1[q], b[q], b1[q], c[q], c1[q], d[q], d1[q]};
-          out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + q)),
-                                 low_mask(g.nx - 1 - 32 * (m + q)), s_nf);
+          diff |= a[q] ^ a1[q];
+          if (hy) diff |= (a[q] ^ b[q]) | (a[q] ^ b1[q]);
+          if (hz) diff |= (a[q] ^ c[q]) | (a[q] ^ c1[q]);
+          if (hy && hz) diff |= (a[q] ^ d[q]) | (a[q] ^ d1[q]);
+        }
+        if (diff) {
+#pragma unroll
+          for (int q = 0; q < kCountWords; ++q) {
+            const CornerWords w{a[q], a1[q], b[q], b1[q], c[q], c1[q], d[q], d1[q]};
+            out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + q)),
+                                   low_mask(g.nx - 1 - 32 * (m + q)), s_nf);
+          }
         }
       } else {
         // words that straddle a row or grid end: one at a time
@@ -259,17 +272,27 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
 // own kScanTile words and writes the exclusive offsets wt (a) and wv (b),
 // the compacted list act of its non-zero words, and -- the last tile -- the
 // totals, the end entries wt[rowwords] / wv[rowwords] and the error word.
+//
+// PIPE (the pipelined marching cubes): blocks cover tiles tile_begin + b of
+// one slab, later slabs run later; each block flags an offset above 2^31 - 1
+// itself (emits of earlier slabs run before the last tile), the error word
+// and emit counters were cleared by the first slab's classification, and
+// for every boundary word B.e[i] in its words a thread records the number
+// of active words before it in slab_act[i] (the last tile: slab_act[B.n] =
+// all active words).
+template <bool PIPE>
 __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
                                                    const uint32_t* __restrict__ wc,
                                                    const uint32_t* __restrict__ tile_tot,
                                                    int tiles, uint32_t* __restrict__ wt,
                                                    uint32_t* __restrict__ wv,
                                                    uint32_t* __restrict__ act,
-                                                   Info* __restrict__ info) {
+                                                   Info* __restrict__ info, int tile_begin,
+                                                   SlabBounds B, uint32_t* __restrict__ slab_act) {
   __shared__ uint32_t s_red[24];
   __shared__ unsigned long long s_pre[3 * 8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int tile = blockIdx.x;
+  const int tile = tile_begin + blockIdx.x;
   // exclusive prefix over the tiles before this one (64-bit: totals may pass 2^32)
   unsigned long long pt = 0, pv = 0, pa = 0;
   for (int x = tid; x < tile; x += 256) {
@@ -337,6 +360,20 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
   uint32_t ot = (uint32_t)et + bt + it - st;
   uint32_t ov = (uint32_t)ev + bv + iv - sv;
   long long oa = (long long)ea + ba + ia - sa;
+  if (PIPE) {
+    if (tid == 0 && (et + tt > 2147483647ull || ev + tv > 2147483647ull))
+      atomicOr(&info->error, kErrOverflow);
+    for (int i = 0; i < B.n; ++i) {
+      const long long d = B.e[i] - w0;
+      if (d >= 0 && d < kScanItems) {
+        long long p = oa;
+#pragma unroll
+        for (int e = 0; e < kScanItems; ++e)
+          if (e < d && c[e]) ++p;
+        slab_act[i] = (uint32_t)p;
+      }
+    }
+  }
 #pragma unroll
   for (int q = 0; q < kScanItems / 4; ++q) {
     uint32_t t4[4], v4[4];
@@ -368,9 +405,13 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
     info->total_a = T;
     info->total_b = V;
     info->total_c = (long long)(ea + ta);
-    info->error = (T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0;
-    info->ticket = 0;
-    info->done = 0;
+    if (PIPE) {
+      slab_act[B.n] = (uint32_t)(ea + ta);
+    } else {
+      info->error = (T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0;
+      info->ticket = 0;
+      info->done = 0;
+    }
   }
 }
 
@@ -381,7 +422,8 @@ int word_scan_tiles(long long rowwords) {
 void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
                       uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s) {
   const int tiles = word_scan_tiles(rowwords);
-  k_word_scan<<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info);
+  k_word_scan<false><<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info, 0,
+                                           SlabBounds{}, nullptr);
 }
 
 // K2a for grid sets: the same counts, with the triangles of the active
@@ -536,9 +578,23 @@ void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o
     k_mc_count_dealt<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
   } else {
     const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, tiles, kPassCount);
-    k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
+    k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles, 0, tiles);
   }
   launch_word_scan(S.rowwords, o.wc, o.tile, o.wt, o.wv, o.act, info, s);
+}
+
+// One slab of the pipelined marching cubes (one grid): the counts of tiles
+// [tile_begin, tile_end), then their scan.
+void launch_mc_scan_slab(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
+                         int tile_begin, int tile_end, const SlabBounds& B, uint32_t* slab_act,
+                         int pass, int num_sms, cudaStream_t s, cudaEvent_t after_count) {
+  const int tiles = word_scan_tiles(S.rowwords);
+  const int n = tile_end - tile_begin;
+  const int b1 = resident_blocks(k_mc_count, 256, 0, num_sms, n, pass);
+  k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles, tile_begin, tile_end);
+  if (after_count) cudaEventRecord(after_count, s);
+  k_word_scan<true><<<n, 256, 0, s>>>(S.rowwords, o.wc, o.tile, tiles, o.wt, o.wv, o.act, info,
+                                      tile_begin, B, slab_act);
 }
 
 // ---------------------------------------------------------------------------
@@ -581,36 +637,6 @@ __device__ __forceinline__ long long word_v(const WordOffsets& o, long long gw) 
   return (long long)__ldg(o.wv + gw);
 }
 
-// Crossing masks of one owner word plus its global vertex offset.
-struct OwnerWord {
-  uint32_t X, Y, Z;
-  long long base;
-};
-
-__device__ __forceinline__ OwnerWord owner_word(const Grid& g, const uint32_t* bits,
-                                                const WordOffsets& o, long long rw0, int jq,
-                                                int kq, int wq) {
-  const long long rq = (long long)kq * g.ny + jq;
-  const long long pos = rq * g.nx + 32ll * wq;
-  uint32_t a, a1;
-  bits_at2(bits, pos, a, a1);
-  const uint32_t pm = low_mask(g.nx - 32 * wq);
-  OwnerWord ow;
-  ow.X = (a ^ a1) & low_mask(g.nx - 1 - 32 * wq);
-  ow.Y = jq < g.ny - 1 ? (a ^ bits_at(bits, pos + g.nx)) & pm : 0u;
-  ow.Z = kq < g.nz - 1 ? (a ^ bits_at(bits, pos + (long long)g.nx * g.ny)) & pm : 0u;
-  ow.base = word_v(o, rw0 + rq * g.wr + wq);
-  return ow;
-}
-
-__device__ __forceinline__ long long owner_rank_id(const OwnerWord& o, int b, int axis) {
-  const uint32_t lm = (1u << b) - 1u;
-  long long id = o.base + __popc(o.X & lm) + __popc(o.Y & lm) + __popc(o.Z & lm);
-  if (axis >= 1) id += (o.X >> b) & 1u;
-  if (axis >= 2) id += (o.Y >> b) & 1u;
-  return id;
-}
-
 // Capacity and error check before any output is written; A = active words.
 __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long vcap, bool merge,
                                            long long& A) {
@@ -625,13 +651,66 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
   return true;
 }
 
-// One warp's staging of 32 active words, structure-of-arrays so that lane L
-// writes column L without bank conflicts: per word the corner bit words, the
-// crossing masks and first vertex ids of the four owner rows q = dj + 2 dk
-// (rows (j + dj, k + dk) at word m), the active-cell mask, the global row
-// word, the grid slot, the word's first point (i0 = 32 m, j, k), and -- when
-// the word's last cell is active -- the owned edges and first vertex id of
-// point 32m + 32 of each owner row, which that cell's +x corners need.
+// The crossing edges owned by point (i, j, k) (own: bit 0 = x, 1 = y, 2 = z),
+// written as vertices vid0, vid0 + 1, ... in axis order -- the merged
+// order.  The point's value is loaded once and all end values are loaded
+// before any is used; each vertex is the one emit_vertex would write.
+__device__ __forceinline__ void emit_point_vertices(const GridSlot& sl, int i, int j, int k,
+                                                    uint32_t own, long long vid0,
+                                                    float* __restrict__ verts,
+                                                    int32_t* __restrict__ ra,
+                                                    int32_t* __restrict__ rb,
+                                                    float* __restrict__ rw) {
+  const Grid& g = sl.g;
+  const long long pa = ((long long)k * g.ny + j) * g.nx + i;
+  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
+  const float fa = slot_value(sl, pa, i, j, k);
+  float fb[3];
+  fb[0] = (own & 1u) ? slot_value(sl, pa + 1, i + 1, j, k) : 0.0f;
+  fb[1] = (own & 2u) ? slot_value(sl, pa + dy, i, j + 1, k) : 0.0f;
+  fb[2] = (own & 4u) ? slot_value(sl, pa + dz, i, j, k + 1) : 0.0f;
+  const float xa = coord(g.ox, g.sx, i, g.mx), ya = coord(g.oy, g.sy, j, g.my),
+              za = coord(g.oz, g.sz, k, g.mz);
+  long long vid = vid0;
+#pragma unroll
+  for (int axis = 0; axis < 3; ++axis) {
+    if (!((own >> axis) & 1u)) continue;
+    const float w = __fdiv_rn(__fsub_rn(sl.iso, fa), __fsub_rn(fb[axis], fa));
+    const float xb = axis == 0 ? coord(g.ox, g.sx, i + 1, g.mx) : xa;
+    const float yb = axis == 1 ? coord(g.oy, g.sy, j + 1, g.my) : ya;
+    const float zb = axis == 2 ? coord(g.oz, g.sz, k + 1, g.mz) : za;
+    verts[3 * vid + 0] = lerp_rn(xa, xb, w);
+    verts[3 * vid + 1] = lerp_rn(ya, yb, w);
+    verts[3 * vid + 2] = lerp_rn(za, zb, w);
+    if (ra) ra[vid] = (int32_t)pa;
+    if (rb) rb[vid] = (int32_t)(pa + (axis == 0 ? 1ll : (axis == 1 ? dy : dz)));
+    if (rw) rw[vid] = w;
+    ++vid;
+  }
+}
+
+// Bit of the flat bit stream at position p.
+__device__ __forceinline__ uint32_t bit_at(const uint32_t* __restrict__ bits, long long p) {
+  return (__ldg(bits + (p >> 5)) >> (unsigned)(p & 31)) & 1u;
+}
+
+// x (bit 0) and y (bit 1) crossing bits of point i of row (jq, kq).
+__device__ __forceinline__ uint32_t point_xy_bits(const Grid& g, const uint32_t* bits, int jq,
+                                                  int kq, int i) {
+  const long long pos = ((long long)kq * g.ny + jq) * g.nx + i;
+  const uint32_t a = bit_at(bits, pos);
+  uint32_t r = (i + 1 < g.nx) ? (a ^ bit_at(bits, pos + 1)) : 0u;
+  if (jq < g.ny - 1) r |= (a ^ bit_at(bits, pos + g.nx)) << 1;
+  return r;
+}
+
+// One warp's staging of up to 32 active words, structure-of-arrays so that
+// lane L writes column L without bank conflicts: per word the corner bit
+// words, the crossing masks and first vertex ids of the four owner rows
+// q = dj + 2 dk (rows (j + dj, k + dk) at word m), the active-cell mask, the
+// global row word, the grid slot, the word's first point (i0 = 32 m, j, k),
+// and -- when the word's last cell is active -- the x and y crossing bits of
+// point 32m + 32 of owner rows 0..2, which that cell's +x corners need.
 enum EmitField {
   kFWin = 0,     // 8: a, a1, b, b1, c, c1, d, d1
   kFOx = 8,      // 4
@@ -644,12 +723,10 @@ enum EmitField {
   kFI0 = 27,
   kFJ = 28,
   kFK = 29,
-  kFNx = 30,     // point 32m + 32 of owner row q: X, Y, Z bits at 3q .. 3q + 2
-  kFNv = 31,     // 4: first vertex id of word m + 1 of owner row q
-  kFields = 35
+  kFNx = 30,     // point 32m + 32 of owner row q <= 2: x bit at 2q, y bit at 2q + 1
+  kFields = 31
 };
 constexpr int kEmitWarps = 8;
-constexpr int kCellChunk = 64;  // active cells tabulated per triangle pass
 
 __device__ __forceinline__ uint32_t window(const uint32_t* st, int f, int s) { return st[f * 32 + s]; }
 
@@ -674,6 +751,67 @@ __device__ __forceinline__ int warp_exclusive(int v, int lane, int* total) {
   return x - v;
 }
 
+// Merged vertex ids of the 12 edges of cell q of staged word s, into
+// ids[e * 32 + lane] (meaningful for the cell's crossing edges only).  Edge
+// e belongs to owner point (q + di) of owner row dj + 2 dk (kEdgeOwner); its
+// id is the row word's first id, plus the edges its earlier points own,
+// plus its own x (and y) edge before a y (z) edge.  Point q + 1 = 32 is the
+// next word's first point: its first id is this word's first id plus all the
+// word's edges, since ids are dense in point order.
+__device__ __forceinline__ void cell_edge_ids(const uint32_t* st, int s, int q, uint32_t* ids,
+                                              int lane) {
+  const uint32_t lm = (1u << q) - 1u;
+  uint32_t R[4], x[4], y[4], z[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t X = window(st, kFOx + r, s), Y = window(st, kFOy + r, s),
+                   Z = window(st, kFOz + r, s);
+    R[r] = window(st, kFOv + r, s) + __popc(X & lm) + __popc(Y & lm) + __popc(Z & lm);
+    x[r] = (X >> q) & 1u;
+    y[r] = (Y >> q) & 1u;
+    z[r] = (Z >> q) & 1u;
+  }
+  uint32_t x1[3], y1[3];
+  if (q < 31) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      x1[r] = (window(st, kFOx + r, s) >> (q + 1)) & 1u;
+      y1[r] = (window(st, kFOy + r, s) >> (q + 1)) & 1u;
+    }
+  } else {
+    const uint32_t nb = window(st, kFNx, s);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      x1[r] = (nb >> (2 * r)) & 1u;
+      y1[r] = (nb >> (2 * r + 1)) & 1u;
+    }
+  }
+  const uint32_t R1_0 = R[0] + x[0] + y[0] + z[0], R1_1 = R[1] + x[1] + y[1] + z[1],
+                 R1_2 = R[2] + x[2] + y[2] + z[2];
+  ids[0 * 32 + lane] = R[0];                          // row 0, q,     x
+  ids[1 * 32 + lane] = R1_0 + x1[0];                  // row 0, q + 1, y
+  ids[2 * 32 + lane] = R[1];                          // row 1, q,     x
+  ids[3 * 32 + lane] = R[0] + x[0];                   // row 0, q,     y
+  ids[4 * 32 + lane] = R[2];                          // row 2, q,     x
+  ids[5 * 32 + lane] = R1_2 + x1[2];                  // row 2, q + 1, y
+  ids[6 * 32 + lane] = R[3];                          // row 3, q,     x
+  ids[7 * 32 + lane] = R[2] + x[2];                   // row 2, q,     y
+  ids[8 * 32 + lane] = R[0] + x[0] + y[0];            // row 0, q,     z
+  ids[9 * 32 + lane] = R1_0 + x1[0] + y1[0];          // row 0, q + 1, z
+  ids[10 * 32 + lane] = R1_1 + x1[1] + y1[1];         // row 1, q + 1, z
+  ids[11 * 32 + lane] = R[1] + x[1] + y[1];           // row 1, q,     z
+}
+
+// A warp takes `batch` (1..32) active words at a time from the counter
+// *ticket; the last block to finish resets *ticket and *done.  Smaller
+// batches shorten each warp's chain of dependent steps (the kernel's
+// duration when its words are few), larger ones share each step over more
+// words.
+// range_end < 0: every active word, after a complete count pass.
+// range_end >= 0 (one slab of the pipelined marching cubes, one grid): the
+// active words act[slab_act[0] .. slab_act[1]), which lie below row word
+// range_end; the capacity check uses the offsets at range_end, so a slab
+// writes nothing unless everything up to its end fits.
 template <bool MERGE>
 __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
                                                             const uint32_t* __restrict__ bits,
@@ -685,39 +823,54 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
                                                             long long tcap,
                                                             int32_t* __restrict__ ra,
                                                             int32_t* __restrict__ rb,
-                                                            float* __restrict__ rw) {
+                                                            float* __restrict__ rw,
+                                                            long long range_end,
+                                                            const uint32_t* __restrict__ slab_act,
+                                                            unsigned* __restrict__ ticket,
+                                                            unsigned* __restrict__ done,
+                                                            int batch) {
   // case and edge tables in shared memory: lanes index them divergently
   __shared__ uint64_t s_case[256];
   __shared__ unsigned char s_edge[12];
   __shared__ uint32_t s_stage[kEmitWarps][kFields * 32];
   __shared__ int s_pre[kEmitWarps][33];    // active cells before word s
-  __shared__ int s_prev[kEmitWarps][33];   // owned vertices before word s
-  __shared__ uint32_t s_cell[kEmitWarps][kCellChunk];     // word | bit << 5 | case << 10
-  __shared__ int s_tpre[kEmitWarps][kCellChunk + 1];      // triangles before cell
+  __shared__ int s_ppre[kEmitWarps][33];   // owner points (points with owned edges) before word s
+  __shared__ uint32_t s_ids[kEmitWarps][MERGE ? 12 * 32 : 1];  // a cell's 12 edge ids per lane
   __shared__ long long s_keys[kStagedSlots];
   s_case[threadIdx.x] = kMcCase[threadIdx.x];
   if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
-  long long A;
-  if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
+  long long A0 = 0, A;
+  if (range_end < 0) {
+    if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
+  } else {
+    const long long T = word_t(o, range_end);
+    const long long V = MERGE ? word_v(o, range_end) : 3 * T;
+    if (T > tcap || V > vcap || (info->error & kErrOverflow)) {
+      if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
+        atomicOr(&info->error, kErrCapacity);
+      return;
+    }
+    A0 = __ldg(slab_act);
+    A = __ldg(slab_act + 1);
+  }
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint32_t* st = s_stage[wib];
   int* pre = s_pre[wib];
-  int* pv = s_prev[wib];
-  uint32_t* cell = s_cell[wib];
-  int* tpre = s_tpre[wib];
+  int* ppre = s_ppre[wib];
+  uint32_t* ids = s_ids[wib];
   while (true) {
-    // the next batch of 32 active words, taken dynamically (batches differ
+    // the next batch of active words, taken dynamically (batches differ
     // widely in cost)
     long long a0 = 0;
-    if (lane == 0) a0 = 32ll * atomicAdd(&info->ticket, 1u);
+    if (lane == 0) a0 = A0 + (long long)batch * atomicAdd(ticket, 1u);
     a0 = __shfl_sync(kFull, a0, 0);
     if (a0 >= A) break;
     // ---- lane = word: gather the word's bits, masks and offsets ----------
     uint32_t am = 0, t0 = 0;
-    int nv = 0;
-    if (a0 + lane < A) {
+    int np = 0;
+    if (lane < batch && a0 + lane < A) {
       const uint32_t gw = __ldg(o.act + a0 + lane);
       t0 = __ldg(o.wt + gw);
       int si, m;
@@ -726,7 +879,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
       const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
       const Grid& g = sl.g;
       int j, k;
-  split_row(g, r, j, k);
+      split_row(g, r, j, k);
       const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
       const uint32_t* gb = bits + sl.word0;
       const long long dy = g.nx, dz = (long long)g.nx * g.ny;
@@ -749,7 +902,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
         st[(kFOy + 0) * 32 + lane] = Y;
         st[(kFOz + 0) * 32 + lane] = Z;
         st[(kFOv + 0) * 32 + lane] = __ldg(o.wv + gw);
-        nv = __popc(X) + __popc(Y) + __popc(Z);
+        np = __popc(X | Y | Z);
       }
       if (hy && hz) {  // the row has cells
         bits_at2(gb, pos + dy + dz, w.d, w.d1);
@@ -783,136 +936,90 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
           st[(kFOv + 2) * 32 + lane] = __ldg(o.wv + gw + rwz);
           st[(kFOv + 3) * 32 + lane] = __ldg(o.wv + gw + rwy + rwz);
           if (am >> 31) {  // the last cell's +x corners lie in word m + 1
-            uint32_t nx3 = 0;
-#pragma unroll
-            for (int qq = 0; qq < 4; ++qq) {
-              const OwnerWord on = owner_word(g, gb, o, sl.rw0, j + (qq & 1), k + (qq >> 1), m + 1);
-              nx3 |= ((on.X & 1u) | ((on.Y & 1u) << 1) | ((on.Z & 1u) << 2)) << (3 * qq);
-              st[(kFNv + qq) * 32 + lane] = (uint32_t)on.base;
-            }
-            st[kFNx * 32 + lane] = nx3;
+            const int i1 = 32 * m + 32;
+            st[kFNx * 32 + lane] = point_xy_bits(g, gb, j, k, i1) |
+                                   (point_xy_bits(g, gb, j + 1, k, i1) << 2) |
+                                   (point_xy_bits(g, gb, j, k + 1, i1) << 4);
           }
         }
       }
     }
     st[kFAm * 32 + lane] = am;
-    int total_c, total_v;
+    int total_c, total_p;
     pre[lane + 1] = warp_exclusive(__popc(am), lane, &total_c) + __popc(am);
-    pv[lane + 1] = warp_exclusive(nv, lane, &total_v) + nv;
-    if (lane == 0) pre[0] = pv[0] = 0;
+    ppre[lane + 1] = warp_exclusive(np, lane, &total_p) + np;
+    if (lane == 0) pre[0] = ppre[0] = 0;
     // the batch's triangles are contiguous from its first word's offset
     long long tri_base = __shfl_sync(kFull, t0, 0);
     __syncwarp();
     if (MERGE) {
-      // ---- lane = merged vertex: each owned crossing edge of the words'
-      // own points, in (point, axis) order -----------------------------------
-      for (int v = lane; v < total_v; v += 32) {
-        const int s = search32(pv, v);
-        const int rnk = v - pv[s];
-        OwnerWord ow;
-        ow.X = window(st, kFOx, s);
-        ow.Y = window(st, kFOy, s);
-        ow.Z = window(st, kFOz, s);
-        ow.base = window(st, kFOv, s);
-        // the owner point: the last bit b whose earlier points own <= rnk edges
-        int b = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          const uint32_t lm = (1u << (b + step)) - 1u;
-          if (__popc(ow.X & lm) + __popc(ow.Y & lm) + __popc(ow.Z & lm) <= rnk) b += step;
-        }
+      // ---- lane = owner point: the points of the words that own crossing
+      // edges, in point order; each writes its edges' vertices ---------------
+      for (int t = lane; t < total_p; t += 32) {
+        const int s = search32(ppre, t);
+        const uint32_t X = window(st, kFOx, s), Y = window(st, kFOy, s), Z = window(st, kFOz, s);
+        const int b = nth_bit(X | Y | Z, t - ppre[s]);
         const uint32_t lm = (1u << b) - 1u;
-        const int left = rnk - (__popc(ow.X & lm) + __popc(ow.Y & lm) + __popc(ow.Z & lm));
-        const uint32_t own =
-            ((ow.X >> b) & 1u) | (((ow.Y >> b) & 1u) << 1) | (((ow.Z >> b) & 1u) << 2);
-        const int axis = nth_bit(own, left);
+        const long long vid0 =
+            (long long)window(st, kFOv, s) + __popc(X & lm) + __popc(Y & lm) + __popc(Z & lm);
+        const uint32_t own = ((X >> b) & 1u) | (((Y >> b) & 1u) << 1) | (((Z >> b) & 1u) << 2);
         const GridSlot& sl = S.count == 1 ? S.one : S.slots[window(st, kFSlot, s)];
-        emit_vertex(sl, (int)window(st, kFI0, s) + b, (int)window(st, kFJ, s),
-                    (int)window(st, kFK, s), axis, ow.base + rnk, verts, ra, rb, rw);
+        emit_point_vertices(sl, (int)window(st, kFI0, s) + b, (int)window(st, kFJ, s),
+                            (int)window(st, kFK, s), own, vid0, verts, ra, rb, rw);
       }
     }
-    // ---- triangles, in chunks of kCellChunk active cells -----------------
-    for (int c0 = 0; c0 < total_c; c0 += kCellChunk) {
-      // lane = cell: its word, bit and case, and the chunk's triangle prefix
-      int chunk_tri = 0;
-#pragma unroll
-      for (int h = 0; h < kCellChunk / 32; ++h) {
-        const int c = c0 + 32 * h + lane;
-        int nt = 0;
-        uint32_t packed = 0;
-        if (c < total_c) {
-          const int s = search32(pre, c);
-          const int q = nth_bit(window(st, kFAm, s), c - pre[s]);
-          CornerWords w;
-          w.a = window(st, kFWin + 0, s);
-          w.a1 = window(st, kFWin + 1, s);
-          w.b = window(st, kFWin + 2, s);
-          w.b1 = window(st, kFWin + 3, s);
-          w.c = window(st, kFWin + 4, s);
-          w.c1 = window(st, kFWin + 5, s);
-          w.d = window(st, kFWin + 6, s);
-          w.d1 = window(st, kFWin + 7, s);
-          const int cs = case_of(w, q);
-          nt = (int)(s_case[cs] >> 60);
-          packed = (uint32_t)s | ((uint32_t)q << 5) | ((uint32_t)cs << 10);
-        }
-        int sum;
-        const int ex = warp_exclusive(nt, lane, &sum);
-        cell[32 * h + lane] = packed;
-        tpre[32 * h + lane] = chunk_tri + ex;
-        chunk_tri += sum;
+    // ---- lane = active cell: its case, then all its triangles -------------
+    for (int c0 = 0; c0 < total_c; c0 += 32) {
+      const int c = c0 + lane;
+      int nt = 0, s = 0, q = 0;
+      uint64_t cw = 0;
+      if (c < total_c) {
+        s = search32(pre, c);
+        q = nth_bit(window(st, kFAm, s), c - pre[s]);
+        CornerWords w;
+        w.a = window(st, kFWin + 0, s);
+        w.a1 = window(st, kFWin + 1, s);
+        w.b = window(st, kFWin + 2, s);
+        w.b1 = window(st, kFWin + 3, s);
+        w.c = window(st, kFWin + 4, s);
+        w.c1 = window(st, kFWin + 5, s);
+        w.d = window(st, kFWin + 6, s);
+        w.d1 = window(st, kFWin + 7, s);
+        cw = s_case[case_of(w, q)];
+        nt = (int)(cw >> 60);
       }
-      if (lane == 0) tpre[kCellChunk] = chunk_tri;
-      __syncwarp();
-      // lane = triangle of the chunk
-      for (int t = lane; t < chunk_tri; t += 32) {
-        int ci = 0;
-#pragma unroll
-        for (int step = kCellChunk / 2; step > 0; step >>= 1)
-          if (tpre[ci + step] <= t) ci += step;
-        const uint32_t packed = cell[ci];
-        const int s = (int)(packed & 31u), q = (int)((packed >> 5) & 31u), cs = (int)(packed >> 10);
-        const int tt = t - tpre[ci];
-        const uint64_t cw = s_case[cs];
-        const long long tri = tri_base + t;
-        const int si = (int)window(st, kFSlot, s);
-        const GridSlot& sl = S.count == 1 ? S.one : S.slots[si];
-        const int i = (int)window(st, kFI0, s) + q, j = (int)window(st, kFJ, s),
-                  k = (int)window(st, kFK, s);
+      int chunk_tri;
+      const int ex = warp_exclusive(nt, lane, &chunk_tri);
+      if (nt > 0) {
+        const long long tri0 = tri_base + ex;
+        const GridSlot& sl = S.count == 1 ? S.one : S.slots[window(st, kFSlot, s)];
         // first vertex of this grid in the concatenated output (0 for one grid)
         const long long vbase0 =
             S.count == 1 ? 0 : (MERGE ? word_v(o, sl.rw0) : 3 * word_t(o, sl.rw0));
+        if (MERGE) {
+          cell_edge_ids(st, s, q, ids, lane);
+          for (int t = 0; t < nt; ++t) {
+            int32_t* out = conn + 3 * (tri0 + t);
 #pragma unroll
-        for (int corner = 0; corner < 3; ++corner) {
-          const int e = mc_edge(cw, 3 * tt + corner);
-          const int info_e = s_edge[e];
-          const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
-          const int axis = info_e >> 3;
-          if (MERGE) {
-            const int qq = dj + 2 * dk, ii = q + di;
-            long long vid;
-            if (ii < 32) {
-              OwnerWord ow;
-              ow.X = window(st, kFOx + qq, s);
-              ow.Y = window(st, kFOy + qq, s);
-              ow.Z = window(st, kFOz + qq, s);
-              ow.base = window(st, kFOv + qq, s);
-              vid = owner_rank_id(ow, ii, axis);
-            } else {  // the owner point is the first point of the next word
-              const uint32_t nb = window(st, kFNx, s) >> (3 * qq);
-              vid = (long long)window(st, kFNv + qq, s) + (axis >= 1 ? (nb & 1u) : 0u) +
-                    (axis >= 2 ? ((nb >> 1) & 1u) : 0u);
+            for (int corner = 0; corner < 3; ++corner)
+              out[corner] = (int32_t)((long long)ids[mc_edge(cw, 3 * t + corner) * 32 + lane] - vbase0);
+          }
+        } else {
+          const int i = (int)window(st, kFI0, s) + q, j = (int)window(st, kFJ, s),
+                    k = (int)window(st, kFK, s);
+          for (int t = 0; t < nt; ++t) {
+#pragma unroll
+            for (int corner = 0; corner < 3; ++corner) {
+              const int info_e = s_edge[mc_edge(cw, 3 * t + corner)];
+              const int di = info_e & 1, dj = (info_e >> 1) & 1, dk = (info_e >> 2) & 1;
+              const long long vid = 3 * (tri0 + t) + corner;
+              conn[vid] = (int32_t)(vid - vbase0);
+              emit_vertex(sl, i + di, j + dj, k + dk, info_e >> 3, vid, verts, ra, rb, rw);
             }
-            conn[3 * tri + corner] = (int32_t)(vid - vbase0);
-          } else {
-            const long long vid = 3 * tri + corner;
-            conn[vid] = (int32_t)(vid - vbase0);
-            emit_vertex(sl, i + di, j + dj, k + dk, axis, vid, verts, ra, rb, rw);
           }
         }
       }
       tri_base += chunk_tri;
-      __syncwarp();
     }
     __syncwarp();
   }
@@ -921,9 +1028,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    if (atomicAdd(&info->done, 1u) == gridDim.x - 1) {
-      info->ticket = 0;
-      info->done = 0;
+    if (atomicAdd(done, 1u) == gridDim.x - 1) {
+      *ticket = 0;
+      *done = 0;
       __threadfence();
     }
   }
@@ -932,16 +1039,30 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
 void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
                     Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
                     int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s) {
+  launch_mc_emit_range(S, merge, bits, o, info, verts, vcap, conn, tcap, ra, rb, rw, 0,
+                       S.rowwords, -1, nullptr, &info->ticket, &info->done, kEmitBatch,
+                       kPassEmit, num_sms, s);
+}
+
+void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
+                          Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
+                          int32_t* ra, int32_t* rb, float* rw, long long word_begin,
+                          long long word_end, long long range_end, const uint32_t* slab_act,
+                          unsigned* ticket, unsigned* done, int batch, int pass, int num_sms,
+                          cudaStream_t s) {
   // the active count lives on the device: one resident wave, warp-stride
-  const long long want = (S.rowwords + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
+  const long long words = word_end - word_begin;
+  const long long want = (words + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
   if (merge) {
-    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want, kPassEmit);
+    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want, pass);
     k_mc_emit<true><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
-                                                  rb, rw);
+                                                  rb, rw, range_end, slab_act, ticket, done,
+                                                  batch);
   } else {
-    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want, kPassEmit);
+    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want, pass);
     k_mc_emit<false><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
-                                                   rb, rw);
+                                                   rb, rw, range_end, slab_act, ticket, done,
+                                                  batch);
   }
 }
 

@@ -64,9 +64,42 @@ int dax_gb300_abi_version(void);
 
 /* Per-SM block limit of one marching-cubes pass for later launches in this
  * process: pass 0 = classification (K1), 1 = count (K2a), 2 = generate (K3);
+ * inside dax_gb300_mc_pipeline 3 = classification (default 3), 4 = count
+ * (default: no limit), 5 = generate (default 1);
  * blocks = 0 restores "as many as fit".  A limit leaves room on every SM for
- * the passes of other frames running on other streams. */
+ * the passes of other frames, or other slabs, running on other streams. */
 int dax_gb300_set_blocks_per_sm(int pass, int blocks);
+
+/* Slabs dax_gb300_mc_pipeline cuts a grid into (1..16; 0 restores the
+ * default, 1: no overlap, the passes take the whole device).  Fewer are used
+ * where a grid is too small for them.  Process-wide tuning knob; results do
+ * not depend on it. */
+int dax_gb300_set_pipeline_slabs(int slabs);
+
+/* Further dax_gb300_mc_pipeline tuning knobs, process-wide; results do not
+ * depend on them.  emit_batch: active row words a warp of the emit pass takes
+ * at a time (1..32; 0 = default 8).  emit_streams: internal streams the
+ * slabs' emit passes are dealt to (1..4; 0 = default 2).  keep_field_in_l2:
+ * 1 = the classification reads the field with the default cache policy so
+ * that a slab's values are still in L2 when its emit gathers them, 0 =
+ * evict-first, -1 = default (1). */
+int dax_gb300_set_pipeline_options(int emit_batch, int emit_streams, int keep_field_in_l2);
+
+/* Timeline of dax_gb300_mc_pipeline calls on the current device, for
+ * profiling: enable = 1 records CUDA timing events in the calls that follow,
+ * 0 stops, -1 leaves the setting.  h_ms (n floats, may be NULL) receives,
+ * for the last recorded call, per slab the milliseconds from the call's
+ * start to the ends of: the classification, the wait before the count, the
+ * count, the scan, the wait before the emit, the emit (6 per slab); the call
+ * waits for those events.  *h_slabs (may be NULL) receives its slab count. */
+int dax_gb300_pipeline_timeline(int enable, float* h_ms, int n, int* h_slabs);
+
+/* The slabs a dax_gb300_mc_pipeline call on this grid uses with `slabs`
+ * requested (0 = the current setting), computed on the host: out (int64[52])
+ * receives S, then 17 count/scan boundaries (row words), 17 emit boundaries
+ * (row words) and 17 classification boundaries (128-point chunks), each list
+ * S + 1 long and padded with -1. */
+int dax_gb300_mc_pipeline_plan(const dax_gb300_uniform_grid* grid, int slabs, int64_t* out);
 
 /* Self-check of the reciprocal-based division the stencil kernels use
  * (Markstein's correction step) against CUDA's correctly rounded division:
@@ -154,6 +187,30 @@ int dax_gb300_mc_totals(const void* d_scratch, int64_t* num_triangles,
  * Must follow dax_gb300_mc_count on the same scratch, grid, field, isovalue
  * and stream.  Asynchronous. */
 int dax_gb300_mc_generate(const dax_gb300_uniform_grid* grid, const float* d_field,
+                          float isovalue, int merge, void* d_scratch, size_t scratch_bytes,
+                          float* d_verts, int64_t vert_capacity, int32_t* d_conn,
+                          int64_t tri_capacity, int32_t* d_rec_first, int32_t* d_rec_second,
+                          float* d_rec_weight, void* stream);
+
+/* dax_gb300_mc_count followed by dax_gb300_mc_generate in one call, for a
+ * caller that already holds output buffers large enough (from an earlier
+ * frame, or the upper bounds 5 x cells triangles and 3 x triangles
+ * vertices): DispatcherMapCell<MarchingCubesCount> and
+ * DispatcherGenerateInterpolatedCells<MarchingCubesGenerate>
+ * (dax/cont/DispatcherGenerateInterpolatedCells.h:145-301) without the host
+ * reading the sizes in between.  The grid is cut into z-ordered slabs whose
+ * passes overlap: the classification of one slab streams the field while
+ * the earlier slabs are counted, scanned and emitted, on two internal
+ * streams that fork from `stream` and join back into it, so work queued on
+ * `stream` afterwards sees the complete result.  Same outputs, bit for bit,
+ * as the two calls; the same scratch (dax_gb300_mc_scratch_bytes); the
+ * totals and error bits are read afterwards with dax_gb300_mc_totals.  When
+ * a capacity is too small, DAX_GB300_ERROR_CAPACITY is reported there and
+ * nothing is written past the capacities, but the slabs before the first
+ * one that did not fit may have been written.  The first call on a device
+ * creates the internal streams and events: make it outside any stream
+ * capture.  Calls from several host threads are serialised.  Asynchronous. */
+int dax_gb300_mc_pipeline(const dax_gb300_uniform_grid* grid, const float* d_field,
                           float isovalue, int merge, void* d_scratch, size_t scratch_bytes,
                           float* d_verts, int64_t vert_capacity, int32_t* d_conn,
                           int64_t tri_capacity, int32_t* d_rec_first, int32_t* d_rec_second,
