@@ -229,6 +229,41 @@ def reference_parity(field_host, dims, spacing, iso, verts, conn):
             "triangles": int(ref["conn"].shape[0]), "merged_vertices": int(ref["verts"].shape[0])}
 
 
+def fp64_error_statement(field_host, dims, spacing, iso, grid, field, verts, conn, scratch):
+    """Error of the float32 surface and cell gradients against the FP64 twin
+    of the reference (its worklets built with DAX_USE_DOUBLE_PRECISION, same
+    float32 inputs): marching-cubes weights and positions over the whole
+    field, CellGradient over a 32-plane z-slab through the middle."""
+    import ctypes as C_
+    import numpy as np
+    import torch
+    import oracle
+    from oracle import fp64_error
+    from daxtoolkit_gb300 import cont
+    try:
+        tw = oracle.Fp64Twin()
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    nx, ny, nz = dims
+    g = oracle.make_grid(dims, spacing=spacing)
+    r64 = tw.mc_generate(g, field_host, iso, merge=True)
+    rec = cont.marching_cubes(grid, field, iso, merge=True, records=True)
+    same = bool(np.array_equal(rec["conn"].cpu().numpy(), r64["conn"]))
+    mc = fp64_error.mc_error_stats(rec["verts"].cpu().numpy(), rec["rec_weight"].cpu().numpy(),
+                                   r64, (0, 0, 0), spacing, (0, 0, 0), dims)
+    k0, kp = nz // 2 - 16, 33
+    sub = np.ascontiguousarray(field_host.reshape(nz, ny, nx)[k0:k0 + kp]).ravel()
+    sg = cont.UniformGrid((nx, ny, kp), spacing=spacing, extent_min=(0, 0, k0))
+    g32 = cont.cell_gradient(sg, torch.from_numpy(sub).to(field.device)).cpu().numpy()
+    og = oracle.make_grid((nx, ny, kp), spacing=spacing, extent_min=(0, 0, k0))
+    gr = fp64_error.gradient_error_stats(g32, tw.cell_gradient(og, sub), sub, (0, 0, 0), spacing,
+                                         (0, 0, k0), (nx, ny, kp))
+    gr["sample"] = "cell planes %d..%d of the %d^3 grid" % (k0, k0 + kp - 2, nx)
+    return {"against": "reference worklets built with DAX_USE_DOUBLE_PRECISION, same float32 "
+                       "inputs", "unit_roundoff": 2.0 ** -24, "topology_equal": same,
+            "marching_cubes": mc, "cell_gradient": gr}
+
+
 def _ref_oracle(threads=None):
     import oracle
     try:
@@ -1021,11 +1056,14 @@ def main():
     }
     if not args.no_extras:
         line.update(extra_measurements(field, grid, dims, iso, peak, stream, dev))
-    if rank == 0:
-        line["parity"] = reference_parity(field.cpu().numpy(), dims, spacing, iso, verts_pipe,
-                                          conn_pipe)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU-baseline leg: the reference on the whole field checks the
+        # timed frames' surface bit for bit, its FP64 twin states the float32
+        # error, and the bounded samples time the CPU implementation
         fh = field.cpu().numpy()
+        line["parity"] = reference_parity(fh, dims, spacing, iso, verts_pipe, conn_pipe)
+        line["fp64_error"] = fp64_error_statement(fh, dims, spacing, iso, grid, field, verts_pipe,
+                                                  conn_pipe, scratch)
         cb = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
         cs = cpu_baseline(fh, dims, spacing, iso, args.cpu_seconds, threads=1)

@@ -293,3 +293,58 @@ class Oracle:
         out = np.zeros((self._cells(g), 3), np.float32)
         self._grad(ctypes.byref(g), _ptr(field), _ptr(out))
         return out
+
+
+class Fp64Twin:
+    """The reference-built driver compiled with the DaxToolkit's own
+    DAX_USE_DOUBLE_PRECISION option (dax::Scalar = double): the same worklets
+    on the same float32 field and grid description, evaluated in double.  Its
+    marching-cubes weights and positions and its cell gradients are returned
+    as float64 -- the FP64 values that the float32 results' errors are stated
+    against.  Topology and output order equal the float32 driver's whenever
+    the case decisions do (they compare the same float32 values)."""
+
+    def __init__(self):
+        path = _build.build_ref(variant="f64")
+        if path is None or not os.path.exists(path):
+            raise RuntimeError("FP64 reference twin not built (DaxToolkit tree unavailable)")
+        L = self.lib = ctypes.CDLL(path)
+        vp, f32, i64 = ctypes.c_void_p, ctypes.c_float, ctypes.c_int64
+        gp = ctypes.POINTER(GridDesc)
+        L.ref64_mc_count.argtypes = [gp, vp, f32, vp, vp]
+        L.ref64_mc_generate.argtypes = [gp, vp, f32, vp, ctypes.c_int, vp, vp, vp, vp, vp,
+                                        ctypes.POINTER(i64)]
+        L.ref64_mc_generate.restype = i64
+        L.ref64_cell_gradient.argtypes = [gp, vp, vp]
+        L.ref64_set_threads.argtypes = [ctypes.c_int]
+        L.ref64_max_threads.restype = ctypes.c_int
+        L.ref64_set_threads(int(L.ref64_max_threads()))
+
+    def mc_generate(self, g, field, iso, merge=True):
+        """Count and generate in FP64: dict(verts [V,3] f64, conn [T,3] i32,
+        rec_a, rec_b, rec_w f64)."""
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        C = Oracle._cells(g)
+        count = np.zeros(C, np.int32)
+        self.lib.ref64_mc_count(ctypes.byref(g), _ptr(field), float(iso), _ptr(count), None)
+        T = int(count.astype(np.int64).sum())
+        cap = max(3 * T, 1)
+        verts = np.zeros((cap, 3), np.float64)
+        conn = np.zeros(cap, np.int32)
+        ra = np.zeros(cap, np.int32)
+        rb = np.zeros(cap, np.int32)
+        rw = np.zeros(cap, np.float64)
+        nv = ctypes.c_int64(0)
+        t = self.lib.ref64_mc_generate(ctypes.byref(g), _ptr(field), float(iso), _ptr(count),
+                                       int(bool(merge)), _ptr(verts), _ptr(conn), _ptr(ra),
+                                       _ptr(rb), _ptr(rw), ctypes.byref(nv))
+        assert t == T
+        V = nv.value
+        return dict(verts=verts[:V], conn=conn[:3 * T].reshape(T, 3), rec_a=ra[:V], rec_b=rb[:V],
+                    rec_w=rw[:V])
+
+    def cell_gradient(self, g, field):
+        field = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        out = np.zeros((Oracle._cells(g), 3), np.float64)
+        self.lib.ref64_cell_gradient(ctypes.byref(g), _ptr(field), _ptr(out))
+        return out

@@ -5,7 +5,9 @@ Two libraries come out of this:
 * ``oracle/build/liboracle.so`` -- the plain-C restatement in ``dax_oracle.c``.
 * ``oracle/_ref/libdaxref.so`` -- ``ref_driver.cpp`` compiled against the
   DaxToolkit's own headers (worklets, uniform topology and its point
-  coordinates, Lerp), with
+  coordinates, Lerp), and ``oracle/_ref/libdaxref64.so``, the same driver
+  with the reference's ``DAX_USE_DOUBLE_PRECISION`` option (the FP64 twin),
+  with
   the five std-based Boost stand-ins in ``ref_shim/`` and the three generated
   headers (``Configure.h`` and the ``VectorOperations.h`` instances) that the
   reference's CMake would normally produce.
@@ -116,6 +118,14 @@ def reference_available():
 REF_PP = os.path.join(REF_OUT, "ref_driver_pp.cpp")
 REF_DEFS = ["-std=c++11", "-w", "-DDAX_USE_VARIADIC_TEMPLATE=1",
             "-DDAX_DEVICE_ADAPTER=DAX_DEVICE_ADAPTER_SERIAL"]
+# The FP64 twin: the same driver with the reference's DAX_USE_DOUBLE_PRECISION
+# option (dax::Scalar = double) and double outputs, entry points ref64_*.
+REF64_SO = os.path.join(REF_OUT, "libdaxref64.so")
+REF64_PP = os.path.join(REF_OUT, "ref_driver64_pp.cpp")
+VARIANTS = {
+    "f32": (REF_SO, REF_PP, []),
+    "f64": (REF64_SO, REF64_PP, ["-DDAX_USE_DOUBLE_PRECISION", "-DDAXREF_F64"]),
+}
 
 
 def _system_include_dirs():
@@ -132,15 +142,16 @@ def _system_include_dirs():
     return sorted(dirs, key=len, reverse=True)
 
 
-def _export_portable_source(gen, omp):
+def _export_portable_source(gen, omp, defs=(), out_pp=REF_PP):
     """Write oracle/_ref/ref_driver_pp.cpp: ref_driver.cpp with the reference
     headers expanded by the preprocessor and every system header left as an
     #include line, so that the same reference-built driver can be compiled on
     a host without the reference tree (e.g. an aarch64 GPU host).  The file is
     a build output: it lives in the git-ignored oracle/_ref/ only."""
     src = os.path.join(HERE, "ref_driver.cpp")
-    r = subprocess.run(["g++"] + REF_DEFS + omp + ["-E", "-I", os.path.join(HERE, "ref_shim"),
-                                                   "-I", gen, "-I", REFERENCE_DIR, src],
+    r = subprocess.run(["g++"] + REF_DEFS + list(defs) + omp +
+                       ["-E", "-I", os.path.join(HERE, "ref_shim"), "-I", gen, "-I",
+                        REFERENCE_DIR, src],
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, check=True)
     sysdirs = _system_include_dirs()
     marker = re.compile(r'^# (\d+) "([^"]*)"((?: \d)*)$')
@@ -169,43 +180,45 @@ def _export_portable_source(gen, omp):
             continue
         if not stack[-1]:
             out.append(line)
-    open(REF_PP, "w").write("\n".join(out) + "\n")
+    open(out_pp, "w").write("\n".join(out) + "\n")
 
 
-def build_ref(force=False):
-    """Compile the reference-side driver; returns the .so path or None.
+def build_ref(force=False, variant="f32"):
+    """Compile the reference-side driver (variant "f32", or "f64" for the
+    FP64 twin); returns the .so path or None.
 
     With the reference tree present: configure, export the portable
     preprocessed source, compile.  Without it: compile the exported source if
     an earlier export travelled here; otherwise None."""
+    so, pp, defs = VARIANTS[variant]
     omp = ["-fopenmp"] if _openmp_ok() else []
+    import platform
+    stamp = os.path.join(REF_OUT, "host_arch_" + variant)
     if not reference_available():
-        if os.path.exists(REF_PP):
-            stamp = os.path.join(REF_OUT, "host_arch")
-            import platform
-            fresh = (os.path.exists(REF_SO) and os.path.exists(stamp) and
+        if os.path.exists(pp):
+            fresh = (os.path.exists(so) and os.path.exists(stamp) and
                      open(stamp).read().strip() == platform.machine() and
-                     os.path.getmtime(REF_SO) >= os.path.getmtime(REF_PP))
+                     os.path.getmtime(so) >= os.path.getmtime(pp))
             if force or not fresh:
                 subprocess.check_call(["g++", "-std=c++11", "-w"] + CFLAGS + omp +
-                                      ["-x", "c++", REF_PP, "-o", REF_SO])
+                                      ["-x", "c++", pp, "-o", so])
                 open(stamp, "w").write(platform.machine())
-            return REF_SO
+            return so
         return None
     src = os.path.join(HERE, "ref_driver.cpp")
-    if not force and _newer(REF_SO, [src]) and os.path.exists(REF_PP):
-        return REF_SO
+    fresh = (os.path.exists(stamp) and open(stamp).read().strip() == platform.machine())
+    if not force and fresh and _newer(so, [src]) and os.path.exists(pp):
+        return so
     gen = os.path.join(REF_OUT, "gen")
     os.makedirs(REF_OUT, exist_ok=True)
     _configure_headers(gen)
-    cmd = (["g++"] + REF_DEFS + CFLAGS + omp +
+    cmd = (["g++"] + REF_DEFS + defs + CFLAGS + omp +
            ["-I", os.path.join(HERE, "ref_shim"), "-I", gen, "-I", REFERENCE_DIR, src,
-            "-o", REF_SO])
+            "-o", so])
     subprocess.check_call(cmd)
-    _export_portable_source(gen, omp)
-    import platform
-    open(os.path.join(REF_OUT, "host_arch"), "w").write(platform.machine())
-    return REF_SO
+    _export_portable_source(gen, omp, defs, pp)
+    open(stamp, "w").write(platform.machine())
+    return so
 
 
 def clean():
@@ -217,3 +230,4 @@ def clean():
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref(force=True, variant="f64"))

@@ -37,6 +37,19 @@
 #include <parallel/numeric>
 #endif
 
+// DAXREF_F64: the FP64 twin.  Built with the reference's own
+// DAX_USE_DOUBLE_PRECISION option (CMakeLists.txt:69, dax::Scalar = double),
+// so every worklet evaluates in double from the same float32 field and grid
+// description; the marching-cubes positions and weights and the cell
+// gradients come out as double, and every entry point is named ref64_*.
+#ifdef DAXREF_F64
+#define REF_API(name) ref64_##name
+typedef double RefReal;
+#else
+#define REF_API(name) ref_##name
+typedef float RefReal;
+#endif
+
 namespace {
 
 struct RefGrid {
@@ -75,10 +88,11 @@ struct Ctx {
     for (int n = 0; n < 8; ++n) c[n] = Coord(v[n]);
     return c;
   }
-  template <typename T>
-  dax::exec::CellField<T, dax::CellTagVoxel> Gather(
-      const dax::exec::CellVertices<dax::CellTagVoxel>& v, const T* f) const {
-    dax::exec::CellField<T, dax::CellTagVoxel> vals;
+  // A float32 point field gathered as dax::Scalar (exact widening in the
+  // FP64 twin).
+  dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> Gather(
+      const dax::exec::CellVertices<dax::CellTagVoxel>& v, const float* f) const {
+    dax::exec::CellField<dax::Scalar, dax::CellTagVoxel> vals;
     for (int n = 0; n < 8; ++n) vals[n] = f[v[n]];
     return vals;
   }
@@ -140,9 +154,9 @@ struct TetCtx {
   }
 };
 
-template <typename Grid, typename Build>
-int64_t GenerateInterpolated(const Grid& ctx, const int32_t* count, int merge, float* verts,
-                             int32_t* conn, int32_t* rec_a, int32_t* rec_b, float* rec_w,
+template <typename Grid, typename Real, typename Build>
+int64_t GenerateInterpolated(const Grid& ctx, const int32_t* count, int merge, Real* verts,
+                             int32_t* conn, int32_t* rec_a, int32_t* rec_b, Real* rec_w,
                              int64_t* nverts, Build build) {
   *nverts = 0;
   std::vector<dax::Id> cellOf;
@@ -193,14 +207,14 @@ int64_t GenerateInterpolated(const Grid& ctx, const int32_t* count, int merge, f
 
 extern "C" {
 
-void ref_set_threads(int n) {
+void REF_API(set_threads)(int n) {
   g_threads = n < 1 ? 1 : n;
 #ifdef _OPENMP
   omp_set_num_threads(g_threads);
 #endif
 }
 
-int ref_max_threads() {
+int REF_API(max_threads)() {
 #ifdef _OPENMP
   return omp_get_num_procs();
 #else
@@ -208,7 +222,7 @@ int ref_max_threads() {
 #endif
 }
 
-void ref_mc_count(const RefGrid* g, const float* field, float iso, int32_t* count,
+void REF_API(mc_count)(const RefGrid* g, const float* field, float iso, int32_t* count,
                   uint8_t* cases) {
   Ctx ctx(g);
   dax::worklet::MarchingCubesCount worklet(iso);
@@ -223,9 +237,9 @@ void ref_mc_count(const RefGrid* g, const float* field, float iso, int32_t* coun
   }
 }
 
-int64_t ref_mc_generate(const RefGrid* g, const float* field, float iso, const int32_t* count,
-                        int merge, float* verts, int32_t* conn, int32_t* rec_a, int32_t* rec_b,
-                        float* rec_w, int64_t* nverts) {
+int64_t REF_API(mc_generate)(const RefGrid* g, const float* field, float iso,
+                             const int32_t* count, int merge, RefReal* verts, int32_t* conn,
+                             int32_t* rec_a, int32_t* rec_b, RefReal* rec_w, int64_t* nverts) {
   Ctx ctx(g);
   dax::worklet::MarchingCubesGenerate worklet(iso);
   return GenerateInterpolated(
@@ -239,7 +253,7 @@ int64_t ref_mc_generate(const RefGrid* g, const float* field, float iso, const i
 
 // SliceCount over all cells: the cell's point coordinates against the plane
 // (dax/worklet/Slice.h:28-77).
-void ref_slice_count(const RefGrid* g, const float* origin, const float* normal, int32_t* count) {
+void REF_API(slice_count)(const RefGrid* g, const float* origin, const float* normal, int32_t* count) {
   Ctx ctx(g);
   dax::worklet::SliceCount worklet(dax::make_Vector3(origin[0], origin[1], origin[2]),
                                    dax::make_Vector3(normal[0], normal[1], normal[2]));
@@ -248,7 +262,7 @@ void ref_slice_count(const RefGrid* g, const float* origin, const float* normal,
 }
 
 // DispatcherGenerateInterpolatedCells<SliceGenerate> (Slice.h:82-168).
-int64_t ref_slice_generate(const RefGrid* g, const float* origin, const float* normal,
+int64_t REF_API(slice_generate)(const RefGrid* g, const float* origin, const float* normal,
                            const int32_t* count, int merge, float* verts, int32_t* conn,
                            int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
   Ctx ctx(g);
@@ -264,7 +278,7 @@ int64_t ref_slice_generate(const RefGrid* g, const float* origin, const float* n
 
 // DispatcherMapField<Magnitude> over the grid's point coordinates
 // (dax/worklet/Magnitude.h:27-38).
-void ref_point_magnitude(const RefGrid* g, float* out) {
+void REF_API(point_magnitude)(const RefGrid* g, float* out) {
   Ctx ctx(g);
   dax::worklet::Magnitude worklet;
 #pragma omp parallel for schedule(static) if (g_threads > 1)
@@ -278,7 +292,7 @@ void ref_point_magnitude(const RefGrid* g, float* out) {
 // DispatcherGenerateTopology<Tetrahedralize> with a constant count of 5 and
 // no point merging (UnitTestWorkletTetrahedralize.cxx:73-90): output cell o
 // is the worklet's visit o % 5 of input cell o / 5.
-void ref_tetrahedralize(const RefGrid* g, int32_t* conn) {
+void REF_API(tetrahedralize)(const RefGrid* g, int32_t* conn) {
   Ctx ctx(g);
   dax::worklet::Tetrahedralize worklet;
 #pragma omp parallel for schedule(static) if (g_threads > 1)
@@ -291,7 +305,7 @@ void ref_tetrahedralize(const RefGrid* g, int32_t* conn) {
 
 // DispatcherMapCell<MarchingTetrahedraCount> over a tetrahedral grid
 // (dax/worklet/MarchingTetrahedra.h:49-80).
-void ref_mt_count(const int32_t* conn, int64_t C, const float* field, float iso, int32_t* count) {
+void REF_API(mt_count)(const int32_t* conn, int64_t C, const float* field, float iso, int32_t* count) {
   TetCtx ctx{nullptr, conn, (dax::Id)C};
   dax::worklet::MarchingTetrahedraCount worklet(iso);
 #pragma omp parallel for schedule(static) if (g_threads > 1)
@@ -301,7 +315,7 @@ void ref_mt_count(const int32_t* conn, int64_t C, const float* field, float iso,
 
 // DispatcherGenerateInterpolatedCells<MarchingTetrahedraGenerate>
 // (MarchingTetrahedra.h:85-161) with the grid's explicit coordinates.
-int64_t ref_mt_generate(const float* pts, const int32_t* conn, int64_t C, const float* field,
+int64_t REF_API(mt_generate)(const float* pts, const int32_t* conn, int64_t C, const float* field,
                         float iso, const int32_t* count, int merge, float* verts, int32_t* tconn,
                         int32_t* rec_a, int32_t* rec_b, float* rec_w, int64_t* nverts) {
   TetCtx ctx{pts, conn, (dax::Id)C};
@@ -314,13 +328,13 @@ int64_t ref_mt_generate(const float* pts, const int32_t* conn, int64_t C, const 
       });
 }
 
-void ref_interpolate_point_field(const int32_t* rec_a, const int32_t* rec_b, const float* rec_w,
+void REF_API(interpolate_point_field)(const int32_t* rec_a, const int32_t* rec_b, const float* rec_w,
                                  int64_t n, const float* in, float* out) {
 #pragma omp parallel for schedule(static) if (g_threads > 1)
   for (int64_t i = 0; i < n; ++i) out[i] = dax::math::Lerp(in[rec_a[i]], in[rec_b[i]], rec_w[i]);
 }
 
-void ref_threshold_count(const RefGrid* g, const float* field, float lo, float hi,
+void REF_API(threshold_count)(const RefGrid* g, const float* field, float lo, float hi,
                          int32_t* count) {
   Ctx ctx(g);
   dax::worklet::ThresholdCount<dax::Scalar> worklet(lo, hi);
@@ -329,7 +343,7 @@ void ref_threshold_count(const RefGrid* g, const float* field, float lo, float h
     count[c] = (int32_t)worklet(ctx.Gather(ctx.Verts(c), field));
 }
 
-int64_t ref_threshold_generate(const RefGrid* g, const float* field, const int32_t* count,
+int64_t REF_API(threshold_generate)(const RefGrid* g, const float* field, const int32_t* count,
                                int32_t* conn, float* coords, float* field_out, int64_t* p_used) {
   Ctx ctx(g);
   *p_used = 0;
@@ -369,7 +383,7 @@ int64_t ref_threshold_generate(const RefGrid* g, const float* field, const int32
   return K;
 }
 
-void ref_cell_gradient(const RefGrid* g, const float* field, float* out) {
+void REF_API(cell_gradient)(const RefGrid* g, const float* field, RefReal* out) {
   Ctx ctx(g);
   dax::worklet::CellGradient worklet;
 #pragma omp parallel for schedule(static) if (g_threads > 1)
