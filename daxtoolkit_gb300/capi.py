@@ -118,6 +118,14 @@ SIGNATURES = {
     "dax_gb300_report_error": ([ctypes.c_int, ctypes.c_char_p], i32),
     "dax_gb300_set_blocks_per_sm": ([ctypes.c_int, ctypes.c_int], i32),
     "dax_gb300_set_pipeline_slabs": ([ctypes.c_int], i32),
+    "dax_gb300_device_alloc": ([ctypes.POINTER(vp), ctypes.c_uint64], i32),
+    "dax_gb300_device_free": ([vp], i32),
+    "dax_gb300_set_alloc_limit": ([ctypes.c_uint64], i32),
+    "dax_gb300_memcpy": ([vp, vp, ctypes.c_uint64, ctypes.c_int], i32),
+    "dax_gb300_timer_create": ([ctypes.POINTER(vp)], i32),
+    "dax_gb300_timer_start": ([vp, vp], i32),
+    "dax_gb300_timer_elapsed": ([vp, vp, ctypes.POINTER(ctypes.c_double)], i32),
+    "dax_gb300_timer_destroy": ([vp], i32),
     "dax_gb300_set_pipeline_options": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], i32),
     "dax_gb300_pipeline_timeline": ([ctypes.c_int, vp, ctypes.c_int, vp], i32),
     "dax_gb300_mc_pipeline_plan": ([gp, ctypes.c_int, vp], i32),

@@ -611,6 +611,42 @@ int dax_gb300_stream_compact(const void* d_input, int value_bytes, const void* d
 int dax_gb300_bounds(const void* d_sorted, int64_t n, const void* d_values, int64_t m,
                      int key_type, int upper, int32_t* d_out, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Device memory, copies and timers (the ArrayManagerExecution and Timer of  */
+/* the device-adapter tag, include/dax_gb300_tag.h)                          */
+/* ------------------------------------------------------------------------ */
+
+/* Allocates `bytes` of device memory on the current device (NULL for 0
+ * bytes): ArrayManagerExecution::AllocateArrayForOutput / LoadDataForInput
+ * (dax/cont/internal/ArrayManagerExecution.h:44-143; the CUDA adapter's
+ * device_vector, dax/thrust/cont/internal/ArrayManagerExecutionThrustDevice.h:
+ * 65-186).  Failure is DAX_GB300_ERROR_OUT_OF_MEMORY, the reference's
+ * ErrorControlOutOfMemory (:97-100), with *d_ptr = NULL. */
+int dax_gb300_device_alloc(void** d_ptr, uint64_t bytes);
+int dax_gb300_device_free(void* d_ptr);
+
+/* Allocations above `bytes` fail with DAX_GB300_ERROR_OUT_OF_MEMORY without
+ * reaching the device (0 = no limit): a way to exercise a caller's
+ * out-of-memory path. */
+int dax_gb300_set_alloc_limit(uint64_t bytes);
+
+/* Synchronous copy of `bytes` (ArrayManagerExecution LoadDataForInput,
+ * RetrieveOutputData, CopyInto). */
+#define DAX_GB300_HOST_TO_DEVICE 0
+#define DAX_GB300_DEVICE_TO_HOST 1
+#define DAX_GB300_DEVICE_TO_DEVICE 2
+int dax_gb300_memcpy(void* dst, const void* src, uint64_t bytes, int kind);
+
+/* A device timer, dax::cont::Timer<Tag> (dax/cont/Timer.h:39-75;
+ * DeviceAdapterTimerImplementation, DeviceAdapterAlgorithm.h:343-406; the
+ * CUDA adapter's events, DeviceAdapterAlgorithmCuda.h:49-88): start records
+ * an event on `stream`, elapsed records a second one, waits for it and
+ * returns the seconds between them. */
+int dax_gb300_timer_create(void** timer);
+int dax_gb300_timer_start(void* timer, void* stream);
+int dax_gb300_timer_elapsed(void* timer, void* stream, double* seconds);
+int dax_gb300_timer_destroy(void* timer);
+
 #ifdef __cplusplus
 }
 #endif

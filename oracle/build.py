@@ -142,20 +142,22 @@ def _system_include_dirs():
     return sorted(dirs, key=len, reverse=True)
 
 
-def _export_portable_source(gen, omp, defs=(), out_pp=REF_PP):
+def _export_portable_source(gen, omp, defs=(), out_pp=REF_PP, src=None, includes=()):
     """Write oracle/_ref/ref_driver_pp.cpp: ref_driver.cpp with the reference
     headers expanded by the preprocessor and every system header left as an
     #include line, so that the same reference-built driver can be compiled on
     a host without the reference tree (e.g. an aarch64 GPU host).  The file is
     a build output: it lives in the git-ignored oracle/_ref/ only."""
-    src = os.path.join(HERE, "ref_driver.cpp")
+    src = src or os.path.join(HERE, "ref_driver.cpp")
+    inc = [x for d in includes for x in ("-I", d)]
     r = subprocess.run(["g++"] + REF_DEFS + list(defs) + omp +
                        ["-E", "-I", os.path.join(HERE, "ref_shim"), "-I", gen, "-I",
-                        REFERENCE_DIR, src],
+                        REFERENCE_DIR] + inc + [src],
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, check=True)
     sysdirs = _system_include_dirs()
     marker = re.compile(r'^# (\d+) "([^"]*)"((?: \d)*)$')
-    out = ["// Generated by oracle/build.py from ref_driver.cpp; not part of the repository.",
+    out = ["// Generated by oracle/build.py from %s; not part of the repository."
+           % os.path.basename(src),
            "#include <omp.h>" if omp else ""]
     # Stack of (is_system) for the files being read; only markers with flag 1
     # (enter) or 2 (return) change it -- a marker without flags inside a

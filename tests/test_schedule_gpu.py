@@ -1,9 +1,10 @@
 """The header-only parts of the device adapter, for arbitrary functors and
 types: dax_gb300::Schedule (include/dax_gb300_schedule.cuh; the reference's
 TestAlgorithmSchedule and TestErrorExecution, TestingDeviceAdapter.h:382-466,
-:1003-1036, in tests/schedule/test_schedule.cu) and the generic algorithms
-with comparison objects (include/dax_gb300_algorithm.cuh;
-tests/schedule/test_algorithm.cu).  Each program is built with nvcc against
+:1003-1036, in tests/schedule/test_schedule.cu; TestDispatcher and the map-field / map-cell
+worklets with their errors, :468-560 and :1038-1200, in
+tests/schedule/test_dispatch.cu) and the generic algorithms with comparison
+objects (include/dax_gb300_algorithm.cuh; tests/schedule/test_algorithm.cu).  Each program is built with nvcc against
 the library and run."""
 import os
 import subprocess
@@ -11,7 +12,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-PROGRAMS = {"test_schedule": 8, "test_algorithm": 14}  # program -> its number of checks
+PROGRAMS = {"test_schedule": 8, "test_algorithm": 14, "test_dispatch": 8}  # program -> checks
 
 
 def _nvcc(name, out, link=True):
