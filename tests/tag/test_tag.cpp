@@ -78,6 +78,16 @@ dax::cont::ArrayHandle<T, Basic, Tag> Make(const std::vector<T>& v) {
   return dax::cont::make_ArrayHandle(v, Basic(), Tag());
 }
 
+// A handle that owns its arrays: in-place algorithms refuse handles over
+// user memory, so (as the reference's tests do) the values are copied into a
+// new handle first.
+template <typename T>
+dax::cont::ArrayHandle<T, Basic, Tag> Owned(const std::vector<T>& v) {
+  dax::cont::ArrayHandle<T, Basic, Tag> h;
+  Algorithm::Copy(Make(v), h);
+  return h;
+}
+
 void TestArrayManagerExecution() {
   std::cout << "ArrayManagerExecution" << std::endl;
   typedef dax::cont::internal::ArrayManagerExecution<dax::Scalar, Basic, Tag> Manager;
@@ -168,12 +178,12 @@ void TestAlgorithms() {
   // Sort, Unique, LowerBounds / UpperBounds on i % 50 (OFFSET added)
   std::vector<dax::Id> mod((size_t)ARRAY_SIZE);
   for (dax::Id i = 0; i < ARRAY_SIZE; ++i) mod[(size_t)i] = OFFSET + (i % 50);
-  IdHandle sorted = Make(mod);
+  IdHandle sorted = Owned(mod);
   Algorithm::Sort(sorted);
   std::vector<dax::Id> ref = mod;
   std::sort(ref.begin(), ref.end());
   Check(ToHost(sorted) == ref, "Sort");
-  IdHandle uniq = Make(ref);
+  IdHandle uniq = Owned(ref);
   Algorithm::Unique(uniq);
   Check(uniq.GetNumberOfValues() == 50, "Unique length");
   std::vector<dax::Id> u = ToHost(uniq);
@@ -186,7 +196,7 @@ void TestAlgorithms() {
     Check(lo[(size_t)i] == i % 50, "LowerBounds");
     Check(up[(size_t)i] == i % 50 + 1, "UpperBounds");
   }
-  IdHandle inplace = Make(mod);
+  IdHandle inplace = Owned(mod);
   Algorithm::LowerBounds(uniq, inplace);
   Check(ToHost(inplace) == lo, "LowerBounds in place");
   // SortByKey with dax::Vector3 values
@@ -196,8 +206,8 @@ void TestAlgorithms() {
     keys[(size_t)i] = ARRAY_SIZE - 1 - i;
     vals[(size_t)i] = dax::make_Vector3(dax::Scalar(i), dax::Scalar(2 * i), dax::Scalar(3 * i));
   }
-  IdHandle hk = Make(keys);
-  Vector3Handle hv = Make(vals);
+  IdHandle hk = Owned(keys);
+  Vector3Handle hv = Owned(vals);
   Algorithm::SortByKey(hk, hv);
   std::vector<dax::Id> k2 = ToHost(hk);
   std::vector<dax::Vector3> v2 = ToHost(hv);
@@ -230,8 +240,8 @@ void TestAlgorithms() {
   // a mismatched argument is the reference's ErrorControlBadValue
   bool bad = false;
   try {
-    IdHandle k3 = Make(keys);
-    Vector3Handle v3 = Make(std::vector<dax::Vector3>(3));
+    IdHandle k3 = Owned(keys);
+    Vector3Handle v3 = Owned(std::vector<dax::Vector3>(3));
     Algorithm::SortByKey(k3, v3);
   } catch (dax::cont::ErrorControlBadValue&) {
     bad = true;
