@@ -507,11 +507,60 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
 
     t_plain = _event_ms(plain, 5, stream)
     t_batch = _event_ms(batched, 20, stream)
+    t_batch_only = _event_ms(batch.replay, 20, stream)
     ok = bool(torch.equal(gv, bv) and torch.equal(gc, bc))
+
+    # The plain kernels without the host in the loop: per grid
+    # dax_gb300_mc_count + dax_gb300_mc_generate into outputs allocated
+    # beforehand (each grid's own scratch, its exact sizes known from the
+    # batch run), no size read between grids; as direct calls, and captured
+    # once in a CUDA graph and replayed.
+    gsl = []
+    for k, (gr, f, v) in enumerate(zip(grids, fields, isos)):
+        d = gr.desc()
+        nb = L.dax_gb300_mc_scratch_bytes(ctypes.byref(d))
+        T_k, V_k = toff[k + 1] - toff[k], voff[k + 1] - voff[k]
+        gsl.append(dict(d=d, f=f, iso=float(v), nb=nb,
+                        scr=torch.empty(nb, dtype=torch.uint8, device=dev),
+                        verts=torch.empty((max(V_k, 1), 3), dtype=torch.float32, device=dev),
+                        conn=torch.empty((max(T_k, 1), 3), dtype=torch.int32, device=dev),
+                        T=T_k, V=V_k))
+
+    def plain_kernels(st=s):
+        for q in gsl:
+            capi.call("dax_gb300_mc_count", ctypes.byref(q["d"]), ptr(q["f"]), q["iso"],
+                      ptr(q["scr"]), q["nb"], st)
+            capi.call("dax_gb300_mc_generate", ctypes.byref(q["d"]), ptr(q["f"]), q["iso"], 1,
+                      ptr(q["scr"]), q["nb"], ptr(q["verts"]), q["V"], ptr(q["conn"]), q["T"],
+                      None, None, None, st)
+
+    t_plain_kernels = _event_ms(plain_kernels, 10, stream)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(stream)
+    pg = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(pg, stream=side, capture_error_mode="thread_local"):
+        plain_kernels(ctypes.c_void_p(side.cuda_stream))
+    torch.cuda.synchronize()
+    t_plain_graph = _event_ms(pg.replay, 20, stream)
+    for k, q in enumerate(gsl):  # the loop's surfaces are the batch's, grid by grid
+        ok = ok and bool(torch.equal(q["conn"][:q["T"]], bc[toff[k]:toff[k + 1]]))
+        ok = ok and bool(torch.equal(q["verts"][:q["V"]], bv[voff[k]:voff[k + 1]]))
+    del pg, gsl
     out["batched"] = {"grids": 64, "grid_dims": "each U{32..192}, seed 777", "cells": cells,
-                      "triangles": toff[-1], "plain_loop_ms": t_plain, "batched_graph_ms": t_batch,
+                      "triangles": toff[-1],
+                      "plain_loop_ms": t_plain, "batched_graph_ms": t_batch,
                       "speedup": t_plain / t_batch, "target_speedup": 3.0,
+                      "plain_kernels_loop_ms": t_plain_kernels,
+                      "plain_kernels_loop_graph_ms": t_plain_graph,
+                      "batched_graph_replay_only_ms": t_batch_only,
+                      "speedup_vs_plain_kernels_graph": t_plain_graph / t_batch_only,
+                      "speedup_vs_plain_kernels_direct": t_plain_kernels / t_batch_only,
                       "batched_cells_per_s": cells / (t_batch / 1e3),
+                      "note": "plain_loop: cont.marching_cubes per grid (allocation and a host "
+                              "size read per grid); plain_kernels: count + generate per grid into "
+                              "preallocated outputs, no host read, direct or one graph replay; "
+                              "batched_graph_replay_only: the batch's graph replay without the "
+                              "totals read",
                       "graph_replay_matches_batch_run": ok}
     out["primitives"] = primitive_measurements(peak, stream, dev)
     return out

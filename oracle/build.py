@@ -73,6 +73,19 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
+VTK_BIN = os.path.join(BUILD, "vtk_ostream")
+
+
+def build_vtk_ostream(force=False):
+    """The std::ostream VTK writer (vtk_ostream.cpp), the byte-format pin of
+    the library's legacy-VTK writer."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "vtk_ostream.cpp")
+    if force or not _newer(VTK_BIN, [src]):
+        subprocess.check_call(["g++", "-std=c++11", "-O1", src, "-o", VTK_BIN])
+    return VTK_BIN
+
+
 def _configure_headers(gen):
     """Produce what the reference's CMake would configure (CMakeLists.txt:73,
     dax/CMakeLists.txt:37-46, dax/exec/CMakeLists.txt:38-50,

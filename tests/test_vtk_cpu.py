@@ -70,3 +70,49 @@ def test_magnitude_port_matches_reference(g):
     a = oracle.Oracle("port").point_magnitude(grid)
     b = oracle.Oracle("reference").point_magnitude(grid)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def _ostream_bytes(tmp_path, pts, conn, V=3):
+    """The file std::ostream writes (oracle/vtk_ostream.cpp, the reference
+    benchmark's stream insertions) for the same points and cells."""
+    import subprocess
+    pts = np.ascontiguousarray(pts, np.float32)
+    conn = np.ascontiguousarray(conn, np.int32)
+    pf, cf, out = tmp_path / "p.f32", tmp_path / "c.i32", tmp_path / "ostream.vtk"
+    pts.tofile(pf)
+    conn.tofile(cf)
+    exe = oracle.build.build_vtk_ostream()
+    subprocess.check_call([exe, str(pf), str(pts.shape[0]), str(cf),
+                           str(conn.shape[0] if conn.size else 0), str(V), str(out)])
+    return out.read_bytes()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_vtk_bytes_equal_std_ostream(tmp_path, seed):
+    """The library's writer and the Python restatement both produce the bytes
+    that the C++ standard library's operator<< writes: floats of every
+    magnitude, signed zeros, infinities, NaNs of both signs, subnormals, and
+    ragged counts."""
+    rng = np.random.default_rng(seed)
+    n_pts, n_cells = 3000 + seed, 1000 + 7 * seed
+    pts = (rng.standard_normal((n_pts, 3)) *
+           10.0 ** rng.integers(-40, 38, size=(n_pts, 3))).astype(np.float32)
+    pts[:8] = np.array([[0.0, -0.0, np.inf], [-np.inf, 1e-45, -1e-45], [1.0, 0.1, 1.0 / 3],
+                        [123456.5, 1234567.0, 999999.5], [1e-5, 1e-4, 100000.0],
+                        [2.5e-38, 3.4e38, -7.0], [0.5, 65536.0, 1e6], [1e7, 1e-7, 42.0]])[:8]
+    pts[8] = [np.nan, -np.nan, 0.0]
+    conn = rng.integers(0, 2 ** 31 - 1, size=(n_cells, 3)).astype(np.int32)
+    want = _ostream_bytes(tmp_path, pts, conn)
+    assert vtk_writer.polydata_text(pts, conn) == want
+    assert _write(tmp_path, pts, conn) == want
+
+
+def test_vtk_benchmark_surface_equals_std_ostream(tmp_path):
+    from tests import cases
+    O = oracle.Oracle("port")
+    g = oracle.make_grid((26, 26, 26))
+    f = cases.linear_field((26, 26, 26))
+    count, _ = O.mc_count(g, f, 70.0)
+    out = O.mc_generate(g, f, 70.0, count, True)
+    assert _write(tmp_path, out["verts"], out["conn"]) == _ostream_bytes(tmp_path, out["verts"],
+                                                                          out["conn"])
