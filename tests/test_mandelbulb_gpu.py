@@ -3,10 +3,14 @@ of the count-array-driven generate it uses, against the CPU oracle.
 
 The escape-iteration field calls transcendental functions (atan2, pow, sin,
 tan, cos) that CUDA and the host C library round differently in the last
-place, and the iteration amplifies that on the fractal's boundary: the field
-is compared by agreement rate (at least 99.5 % of points identical, every
-difference at most a few iterations, nothing different where the first step
-already decides).  Everything computed from a given field -- the surface,
+place, and the iteration amplifies that on the fractal's boundary.  So the
+field is checked against float32 determinacy (oracle/mandelbulb64.py): where
+an ensemble of FP64 orbits of the same coordinate, perturbed at float32
+precision, agrees on the escape count, the GPU must give that count; points
+where the GPU and the C restatement differ must be points the ensemble
+leaves undetermined, but for at most 1e-4 of all points (a finite ensemble
+can look unanimous on a chaotic orbit by chance; measured: 3.5e-5 at 61^3,
+2.4e-5 at 101^3).  Everything computed from a given field -- the surface,
 the clip counts, the counted generate, normals and colours -- is compared bit
 for bit against the oracle run on that same field."""
 import numpy as np
@@ -35,12 +39,22 @@ def test_escape_iteration_field(gb300, n):
     dims, origin, spacing = _demo_grid(n)
     f = cont.mandlebulb_field(cont.UniformGrid(dims, origin, spacing)).cpu().numpy()
     ref = oracle.Oracle("port").mandelbulb_field(oracle.make_grid(dims, origin, spacing))
+    from oracle import mandelbulb64
     same = f == ref
-    assert same.mean() >= 0.995, same.mean()
-    assert np.abs(f - ref).max() <= 34
+    assert set(np.unique(f).tolist()) <= set(range(36))
     # points that escape at once (or start outside) agree exactly
     assert np.all(same[(ref <= 1) & (f <= 1)])
-    assert set(np.unique(f).tolist()) <= set(range(36))
+    # every difference lies where float32 does not determine the count
+    o, s = np.float32(origin[0]), np.float32(spacing[0])
+    x = (o + s * np.arange(dims[0], dtype=np.float32)).astype(np.float32)
+    z, y, xx = np.meshgrid(x, x, x, indexing="ij")
+    c = np.stack([xx.ravel(), y.ravel(), z.ravel()], 1)
+    diff = np.nonzero(~same)[0]
+    det, count = mandelbulb64.determined(mandelbulb64.ensemble(c[diff]))
+    unexplained = int(det.sum())
+    print("\nmandelbulb %d^3: %d differences, %d at float32-determined points"
+          % (dims[0], diff.size, unexplained))
+    assert unexplained <= 1e-4 * f.size, (unexplained, f.size)
 
 
 @pytest.fixture(scope="module")
