@@ -499,6 +499,7 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
     bv, bc, toff, voff = batch.run(merge=True)
     gv = torch.empty_like(bv)
     gc = torch.empty_like(bc)
+    tuned = batch.autotune(gv, gc, merge=True)
     batch.capture(gv, gc, merge=True)
 
     def batched():
@@ -556,6 +557,8 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                       "speedup_vs_plain_kernels_graph": t_plain_graph / t_batch_only,
                       "speedup_vs_plain_kernels_direct": t_plain_kernels / t_batch_only,
                       "batched_cells_per_s": cells / (t_batch / 1e3),
+                      "autotuned": {"emit_batch": tuned[0], "dealt_count": tuned[1],
+                                    "best_ms": tuned[2]},
                       "note": "plain_loop: cont.marching_cubes per grid (allocation and a host "
                               "size read per grid); plain_kernels: count + generate per grid into "
                               "preallocated outputs, no host read, direct or one graph replay; "

@@ -88,6 +88,10 @@ SIGNATURES = {
     "dax_gb300_mc_batch_totals": ([vp, vp, vp, vp, vp], i32),
     "dax_gb300_mc_batch_generate": ([vp, i32, vp, sz, vp, i64, vp, i64, vp], i32),
     "dax_gb300_mc_batch_capture": ([vp, i32, vp, sz, vp, i64, vp, i64, ctypes.POINTER(vp)], i32),
+    "dax_gb300_mc_batch_autotune": ([vp, i32, vp, sz, vp, i64, vp, i64, vp,
+                                     ctypes.POINTER(ctypes.c_float)], i32),
+    "dax_gb300_mc_batch_set_config": ([vp, i32, i32], i32),
+    "dax_gb300_mc_batch_get_config": ([vp, ctypes.POINTER(i32), ctypes.POINTER(i32)], i32),
     "dax_gb300_graph_launch": ([vp, vp], i32),
     "dax_gb300_graph_destroy": ([vp], i32),
     "dax_gb300_mc_noalloc": ([gp, vp, f32, i32, vp, i64, vp, i64, vp, vp], i32),

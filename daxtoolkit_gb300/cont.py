@@ -853,6 +853,24 @@ class MarchingCubesBatch:
             v = [3 * x for x in t]
         return verts, conn, t, v
 
+    def autotune(self, verts, conn, merge=True, stream=None):
+        """dax_gb300_mc_batch_autotune on these outputs: keeps the fastest
+        emit batch / count pass in the plan; returns (emit_batch, dealt,
+        best_ms), best_ms -1 when the extent class was tuned before."""
+        ms = ctypes.c_float()
+        capi.call("dax_gb300_mc_batch_autotune", self.handle, int(bool(merge)), _ptr(self.scratch),
+                  self.scratch.numel(), _ptr(verts), verts.shape[0], _ptr(conn), conn.shape[0],
+                  _stream(stream), ctypes.byref(ms))
+        return self.config() + (ms.value,)
+
+    def set_config(self, emit_batch=0, dealt=-1):
+        capi.call("dax_gb300_mc_batch_set_config", self.handle, int(emit_batch), int(dealt))
+
+    def config(self):
+        eb, dc = ctypes.c_int(), ctypes.c_int()
+        capi.call("dax_gb300_mc_batch_get_config", self.handle, ctypes.byref(eb), ctypes.byref(dc))
+        return eb.value, dc.value
+
     def capture(self, verts, conn, merge=True):
         """Capture count + generate into a CUDA graph writing into verts/conn."""
         g = ctypes.c_void_p()

@@ -279,6 +279,10 @@ struct dax_gb300_mc_batch {
   bool aligned = true;
   size_t off_goff = 0;
   McLayout L;
+  // tuned by dax_gb300_mc_batch_autotune (or set): active words per emit
+  // warp batch, and the dealt (1) or per-lane (0) count pass
+  int emit_batch = daxgb::kEmitBatch;
+  int dealt = 1;
 
   daxgb::GridSet set() const {
     daxgb::GridSet S{};
@@ -1124,7 +1128,7 @@ int dax_gb300_mc_batch_count(dax_gb300_mc_batch* b, void* d_scratch, size_t scra
   int st = check_launch("batch classify kernel");
   if (st) return st;
   const daxgb::WordOffsets o = b->L.offsets(d_scratch);
-  daxgb::launch_mc_scan(S, bits, o, at<Info>(d_scratch, 0), num_sms(), s);
+  daxgb::launch_mc_scan(S, bits, o, at<Info>(d_scratch, 0), num_sms(), s, b->dealt);
   if ((st = check_launch("batch count/scan kernels"))) return st;
   daxgb::launch_grid_offsets(S, b->L.offsets(d_scratch), at<long long>(d_scratch, b->off_goff), s);
   return check_launch("batch offsets kernel");
@@ -1153,11 +1157,102 @@ int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* b, int merge, void* d_scratc
   if (scratch_bytes < b->L.total) return fail(DAX_GB300_ERROR_BAD_VALUE, "batch scratch too small");
   if ((!d_verts && vert_capacity > 0) || (!d_conn && tri_capacity > 0))
     return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL output with nonzero capacity");
-  daxgb::launch_mc_emit(b->set(), merge != 0, at<uint32_t>(d_scratch, b->L.bits),
-                        b->L.offsets(d_scratch), at<Info>(d_scratch, 0), d_verts, vert_capacity, d_conn,
-                        tri_capacity, nullptr, nullptr, nullptr, num_sms(),
-                        static_cast<cudaStream_t>(stream));
+  const daxgb::GridSet S = b->set();
+  Info* info = at<Info>(d_scratch, 0);
+  daxgb::launch_mc_emit_range(S, merge != 0, at<uint32_t>(d_scratch, b->L.bits),
+                              b->L.offsets(d_scratch), info, d_verts, vert_capacity, d_conn,
+                              tri_capacity, nullptr, nullptr, nullptr, 0, S.rowwords, -1, nullptr,
+                              &info->ticket, &info->done, b->emit_batch, daxgb::kPassEmit,
+                              num_sms(), static_cast<cudaStream_t>(stream));
   return check_launch("batch generate kernel");
+}
+
+int dax_gb300_mc_batch_set_config(dax_gb300_mc_batch* b, int emit_batch, int dealt_count) {
+  if (!b) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch");
+  if (emit_batch < 0 || emit_batch > 32 || dealt_count < -1 || dealt_count > 1)
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "emit_batch in [0, 32], dealt_count in [-1, 1]");
+  b->emit_batch = emit_batch ? emit_batch : daxgb::kEmitBatch;
+  b->dealt = dealt_count < 0 ? 1 : dealt_count;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_mc_batch_get_config(const dax_gb300_mc_batch* b, int* emit_batch, int* dealt_count) {
+  if (!b) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch");
+  if (emit_batch) *emit_batch = b->emit_batch;
+  if (dealt_count) *dealt_count = b->count > 1 ? b->dealt : 0;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_mc_batch_autotune(dax_gb300_mc_batch* b, int merge, void* d_scratch,
+                                size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                                int32_t* d_conn, int64_t tri_capacity, void* stream,
+                                float* h_best_ms) {
+  if (!b || !d_scratch) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or scratch");
+  // extent class: the number of grids and the log2 of their mean point count
+  long long pts = 0;
+  for (const auto& sl : b->slots) pts += sl.g.P;
+  int lg = 0;
+  for (long long m = pts / b->count; m > 1; m >>= 1) ++lg;
+  int lc = 0;
+  for (int c = b->count; c > 1; c >>= 1) ++lc;
+  const long long key = ((long long)lc << 16) | ((long long)lg << 1) | (merge != 0);
+  static std::mutex m;
+  static std::map<long long, std::pair<int, int>> cache;
+  {
+    std::lock_guard<std::mutex> lock(m);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      b->emit_batch = it->second.first;
+      b->dealt = it->second.second;
+      if (h_best_ms) *h_best_ms = -1.0f;  // taken from the cache, not timed
+      return DAX_GB300_SUCCESS;
+    }
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) return cuda_fail(e, "autotune events");
+  float best = 1e30f;
+  int best_batch = b->emit_batch, best_dealt = b->dealt, st = DAX_GB300_SUCCESS;
+  const int batches[3] = {8, 16, 32};
+  for (int d = (b->count > 1 ? 1 : 0); d >= 0 && !st; --d)
+    for (int bi = 0; bi < 3 && !st; ++bi) {
+      b->emit_batch = batches[bi];
+      b->dealt = d;
+      float total = 0.0f;
+      for (int rep = 0; rep < 4 && !st; ++rep) {  // the first run warms up
+        e = cudaEventRecord(e0, s);
+        st = e == cudaSuccess ? dax_gb300_mc_batch_count(b, d_scratch, scratch_bytes, s)
+                              : cuda_fail(e, "autotune");
+        if (!st)
+          st = dax_gb300_mc_batch_generate(b, merge, d_scratch, scratch_bytes, d_verts,
+                                           vert_capacity, d_conn, tri_capacity, s);
+        if (!st) e = cudaEventRecord(e1, s);
+        if (!st && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (!st && e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (!st && e != cudaSuccess) st = cuda_fail(e, "autotune timing");
+        if (!st && rep > 0) total += ms;
+      }
+      if (!st) st = read_totals(d_scratch, nullptr, nullptr, s);
+      if (!st && total / 3 < best) {
+        best = total / 3;
+        best_batch = batches[bi];
+        best_dealt = d;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->emit_batch = best_batch;
+  b->dealt = best_dealt;
+  if (st) return st;
+  {
+    std::lock_guard<std::mutex> lock(m);
+    cache[key] = std::make_pair(best_batch, best_dealt);
+  }
+  if (h_best_ms) *h_best_ms = best;
+  return DAX_GB300_SUCCESS;
 }
 
 int dax_gb300_mc_batch_capture(dax_gb300_mc_batch* b, int merge, void* d_scratch,

@@ -148,8 +148,11 @@ int word_scan_tiles(long long rowwords);
 void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
                       uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s);
 // Marching cubes K2a (counts: triangles, crossing edges) + K2b.
+// dealt != 0: for a grid set, the count pass that deals a warp's active cells
+// to its lanes (the default); 0: the per-lane count pass.  One grid always
+// takes the per-lane pass.
 void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
-                    int num_sms, cudaStream_t s);
+                    int num_sms, cudaStream_t s, int dealt = -1);
 void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
                     Info* info, float* verts, long long vcap, int32_t* conn, long long tcap,
                     int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s);

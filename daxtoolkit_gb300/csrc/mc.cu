@@ -571,9 +571,10 @@ __global__ void __launch_bounds__(256) k_mc_count_dealt(GridSet S, const uint32_
 }
 
 void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o, Info* info,
-                    int num_sms, cudaStream_t s) {
+                    int num_sms, cudaStream_t s, int dealt) {
   const int tiles = word_scan_tiles(S.rowwords);
-  if (S.count > 1) {
+  // the dealt pass reads the device slot table, which only grid sets have
+  if (S.count > 1 && dealt != 0) {
     const int b1 = resident_blocks(k_mc_count_dealt, 256, 0, num_sms, tiles, kPassCount);
     k_mc_count_dealt<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
   } else {

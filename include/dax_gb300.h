@@ -468,6 +468,27 @@ int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* batch, int merge, void* d_sc
 int dax_gb300_mc_batch_capture(dax_gb300_mc_batch* batch, int merge, void* d_scratch,
                                size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
                                int32_t* d_conn, int64_t tri_capacity, void** graph);
+
+/* Autotuner of a batch plan (no counterpart in the reference; its batching
+ * is per grid).  Times the plan's count + generate on the caller's buffers
+ * (three timed runs after one warm-up) for every candidate configuration --
+ * an emit pass taking 8, 16 or 32 active row words per warp batch, and for
+ * grid sets the count pass that deals a warp's active cells to its lanes or
+ * the per-lane one -- and keeps the fastest in the plan, which later count,
+ * generate and capture calls use.  Outputs do not depend on the choice.  The
+ * choice is cached per extent class (the log2 of the number of grids and of
+ * their mean point count, and merge), so a plan of a class already tuned
+ * takes it without timing (*h_best_ms = -1).  Synchronous; the outputs hold
+ * the last candidate's (identical) result. */
+int dax_gb300_mc_batch_autotune(dax_gb300_mc_batch* batch, int merge, void* d_scratch,
+                                size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
+                                int32_t* d_conn, int64_t tri_capacity, void* stream,
+                                float* h_best_ms);
+/* Sets (emit_batch 1..32, 0 = default 16; dealt_count 1, 0, -1 = default)
+ * or reads a plan's configuration. */
+int dax_gb300_mc_batch_set_config(dax_gb300_mc_batch* batch, int emit_batch, int dealt_count);
+int dax_gb300_mc_batch_get_config(const dax_gb300_mc_batch* batch, int* emit_batch,
+                                  int* dealt_count);
 int dax_gb300_graph_launch(void* graph, void* stream);
 int dax_gb300_graph_destroy(void* graph);
 

@@ -65,3 +65,31 @@ def test_batch_single_grid_equals_oracle(gb300, oracle_port):
     ref = oracle_port.mc_generate(og, f, 0.45, count, merge=True)
     assert np.array_equal(conn.cpu().numpy(), ref["conn"])
     assert np.array_equal(verts.cpu().numpy().view(np.uint32), ref["verts"].view(np.uint32))
+
+
+def test_batch_every_configuration_and_the_autotuner(gb300):
+    """The emit batch size and the count pass are performance choices only:
+    every configuration writes the same surface; the autotuner keeps one of
+    them, and a second plan of the same extent class takes it from the cache."""
+    cont = gb300
+    grids, fields, isos = _inputs(cont, 10, 20, 90, 33)
+    batch = cont.MarchingCubesBatch(grids, fields, isos)
+    ref_v, ref_c, toff, voff = batch.run(merge=True)
+    for eb in (1, 8, 16, 32):
+        for dealt in (0, 1):
+            batch.set_config(eb, dealt)
+            assert batch.config() == (eb, dealt)
+            v, c, t, vo = batch.run(merge=True)
+            assert t == toff and vo == voff
+            assert torch.equal(c, ref_c) and torch.equal(v.view(torch.int32), ref_v.view(torch.int32))
+    v = torch.empty_like(ref_v)
+    c = torch.empty_like(ref_c)
+    eb, dealt, ms = batch.autotune(v, c, merge=True)
+    assert eb in (8, 16, 32) and dealt in (0, 1) and ms > 0
+    assert torch.equal(c, ref_c) and torch.equal(v.view(torch.int32), ref_v.view(torch.int32))
+    other = cont.MarchingCubesBatch(grids, fields, isos)
+    assert other.autotune(v, c, merge=True) == (eb, dealt, -1.0)
+    # one grid: always the per-lane count pass
+    single = cont.MarchingCubesBatch(grids[:1], fields[:1], isos[:1])
+    single.set_config(8, 1)
+    assert single.config() == (8, 0)
