@@ -91,6 +91,9 @@ SIGNATURES = {
     "dax_gb300_mc_batch_autotune": ([vp, i32, vp, sz, vp, i64, vp, i64, vp,
                                      ctypes.POINTER(ctypes.c_float)], i32),
     "dax_gb300_mc_batch_set_config": ([vp, i32, i32], i32),
+    "dax_gb300_mc_batch_sizes": ([vp, ctypes.POINTER(i64), ctypes.POINTER(i64)], i32),
+    "dax_gb300_mc_batch_cell_gradient": ([vp, vp, vp], i32),
+    "dax_gb300_mc_batch_field_adjoint": ([vp, vp, sz, vp, vp, vp, vp], i32),
     "dax_gb300_mc_batch_get_config": ([vp, ctypes.POINTER(i32), ctypes.POINTER(i32)], i32),
     "dax_gb300_graph_launch": ([vp, vp], i32),
     "dax_gb300_graph_destroy": ([vp], i32),

@@ -853,6 +853,31 @@ class MarchingCubesBatch:
             v = [3 * x for x in t]
         return verts, conn, t, v
 
+    def sizes(self):
+        """(cells, points) of all grids: the lengths of the concatenated
+        per-cell and per-point arrays."""
+        c, pnt = ctypes.c_int64(), ctypes.c_int64()
+        capi.call("dax_gb300_mc_batch_sizes", self.handle, ctypes.byref(c), ctypes.byref(pnt))
+        return c.value, pnt.value
+
+    def cell_gradient(self, out=None, stream=None):
+        """Every grid's cell gradients in one launch, grid after grid."""
+        if out is None:
+            out = torch.empty((self.sizes()[0], 3), dtype=torch.float32,
+                              device=self.fields[0].device)
+        capi.call("dax_gb300_mc_batch_cell_gradient", self.handle, _ptr(out), _stream(stream))
+        return out
+
+    def field_adjoint(self, grad_vertices=None, grad_cell_gradients=None, out=None, stream=None):
+        """dL/dfield of every grid (concatenated) from dL/d(merged vertices)
+        of this plan's last count pass and/or dL/d(cell gradients)."""
+        if out is None:
+            out = torch.empty(self.sizes()[1], dtype=torch.float32, device=self.fields[0].device)
+        capi.call("dax_gb300_mc_batch_field_adjoint", self.handle, _ptr(self.scratch),
+                  self.scratch.numel(), _ptr(grad_vertices), _ptr(grad_cell_gradients), _ptr(out),
+                  _stream(stream))
+        return out
+
     def autotune(self, verts, conn, merge=True, stream=None):
         """dax_gb300_mc_batch_autotune on these outputs: keeps the fastest
         emit batch / count pass in the plan; returns (emit_batch, dealt,

@@ -54,10 +54,10 @@ __device__ __forceinline__ float width_z(const Grid& g, int k) {
 // rows (jc = j0 - 1 + t) are loaded together (three 4-byte loads per cell,
 // 384 contiguous bytes per warp load), then reduced row by row into the
 // point rows t = 0..kAdjBand-1 they bracket.
-__global__ void __launch_bounds__(kMarchWarps * 32, kAdjMinBlocks)
-    k_grad_adjoint(Grid g, const float* __restrict__ dg, float* __restrict__ out, MarchTiles mt) {
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long task = (long long)blockIdx.x * kMarchWarps + wib;
+__device__ __forceinline__ void grad_adjoint_task(const Grid& g, const float* __restrict__ dg,
+                                                  float* __restrict__ out, const MarchTiles& mt,
+                                                  long long task) {
+  const int lane = threadIdx.x & 31;
   if (task >= mt.tasks) return;  // the whole warp leaves; no block barrier follows
   const int xw = (int)(task % mt.nxw);
   const long long t2 = task / mt.nxw;
@@ -130,6 +130,24 @@ __global__ void __launch_bounds__(kMarchWarps * 32, kAdjMinBlocks)
   }
 }
 
+__global__ void __launch_bounds__(kMarchWarps * 32, kAdjMinBlocks)
+    k_grad_adjoint(Grid g, const float* __restrict__ dg, float* __restrict__ out, MarchTiles mt) {
+  grad_adjoint_task(g, dg, out, mt, (long long)blockIdx.x * kMarchWarps + (threadIdx.x >> 5));
+}
+
+// A grid set: the block's grid (block0 as in k_cell_gradient_set); cell
+// gradients and the output field are concatenated over the set.
+__global__ void __launch_bounds__(kMarchWarps * 32, kAdjMinBlocks)
+    k_grad_adjoint_set(GridSet S, const long long* __restrict__ block0,
+                       const float* __restrict__ dg, float* __restrict__ out) {
+  const int si = block_slot(block0, S.count, blockIdx.x);
+  const Grid g = S.slots[si].g;
+  grad_adjoint_task(g, dg + 3 * S.slots[si].cell0, out + S.slots[si].point0,
+                    march_tiles(g.nx, g.ny, g.nz, kAdjBand),
+                    ((long long)blockIdx.x - __ldg(block0 + si)) * kMarchWarps +
+                        (threadIdx.x >> 5));
+}
+
 namespace {
 
 // Crossing masks of owner word (row (j, k), word m) and its first vertex id.
@@ -195,18 +213,15 @@ __device__ __forceinline__ int nth_set_bit(uint32_t u, int n) {
 // backward edges; those points are then dealt to the lanes (lane = point),
 // which load all of a point's end values and vertex gradients before
 // summing its terms in the fixed order.
-__global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __restrict__ f,
-                                                      float iso,
-                                                      const uint32_t* __restrict__ bits,
-                                                      const uint32_t* __restrict__ wv,
-                                                      const float* __restrict__ dverts,
-                                                      float* __restrict__ out) {
+__device__ __forceinline__ void edge_adjoint_words(const Grid& g, const float* __restrict__ f,
+                                                   float iso, const uint32_t* __restrict__ bits,
+                                                   const uint32_t* __restrict__ wv,
+                                                   const float* __restrict__ dverts,
+                                                   float* __restrict__ out, long long w0) {
   const long long W = g.R * g.wr;  // < 2^27 for grids below 2^31 points
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
   const int lane = threadIdx.x & 31;
-  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long w0 = warp0 * 32; w0 < W; w0 += nwarps * 32) {
+  {
     // ---- lane = word ------------------------------------------------------
     const long long w = w0 + lane;
     uint32_t inc = 0u, xf = 0u, yf = 0u, zf = 0u, xb = 0u, yb = 0u, zb = 0u, base = 0u;
@@ -228,7 +243,7 @@ __global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __res
       zb = k > 0 ? (a ^ bits_at(bits, pos - dz)) & pm : 0u;
       inc = xf | yf | zf | xb | yb | zb;
     }
-    if (__ballot_sync(kFull, inc != 0u) == 0u) continue;
+    if (__ballot_sync(kFull, inc != 0u) == 0u) return;
     // owner words of the backward edges: (j - 1, k), (j, k - 1), and the
     // x edge of bit 0, owned by the previous word's point 31
     uint32_t oyX = 0u, oyY = 0u, oyZ = 0u, oyB = 0u, ozX = 0u, ozY = 0u, ozZ = 0u, ozB = 0u;
@@ -321,6 +336,57 @@ __global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __res
       out[p] = __fadd_rn(prev, acc);
     }
   }
+}
+
+__global__ void __launch_bounds__(256) k_edge_adjoint(Grid g, const float* __restrict__ f,
+                                                      float iso,
+                                                      const uint32_t* __restrict__ bits,
+                                                      const uint32_t* __restrict__ wv,
+                                                      const float* __restrict__ dverts,
+                                                      float* __restrict__ out) {
+  const long long W = g.R * g.wr;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long w0 = warp0 * 32; w0 < W; w0 += nwarps * 32)
+    edge_adjoint_words(g, f, iso, bits, wv, dverts, out, w0);
+}
+
+// A grid set: each block takes 256 consecutive row words of its grid
+// (block0 per grid); bits, word offsets and vertex gradients are the set's,
+// the output field is concatenated over the set.
+__global__ void __launch_bounds__(256) k_edge_adjoint_set(GridSet S,
+                                                          const long long* __restrict__ block0,
+                                                          const uint32_t* __restrict__ bits,
+                                                          const uint32_t* __restrict__ wv,
+                                                          const float* __restrict__ dverts,
+                                                          float* __restrict__ out) {
+  const int si = block_slot(block0, S.count, blockIdx.x);
+  const GridSlot& sl = S.slots[si];
+  const Grid g = sl.g;
+  const long long w0 = ((long long)blockIdx.x - __ldg(block0 + si)) * 256 + (threadIdx.x & ~31);
+  if (w0 < g.R * g.wr)
+    edge_adjoint_words(g, sl.field, sl.iso, bits + sl.word0, wv + sl.rw0, dverts,
+                       out + sl.point0, w0);
+}
+
+long long adjoint_grad_blocks(const Grid& g) {
+  return (march_tiles(g.nx, g.ny, g.nz, kAdjBand).tasks + kMarchWarps - 1) / kMarchWarps;
+}
+long long adjoint_edge_blocks(const Grid& g) { return (g.R * g.wr + 255) / 256; }
+
+void launch_field_adjoint_set(const GridSet& S, const long long* grad_block0,
+                              long long grad_blocks, const long long* edge_block0,
+                              long long edge_blocks, long long points, const uint32_t* bits,
+                              const uint32_t* wv, const float* dverts, const float* dgrad,
+                              float* out, cudaStream_t s) {
+  if (dgrad && grad_blocks > 0)
+    k_grad_adjoint_set<<<(unsigned)grad_blocks, kMarchWarps * 32, 0, s>>>(S, grad_block0, dgrad,
+                                                                          out);
+  else
+    cudaMemsetAsync(out, 0, (size_t)points * sizeof(float), s);
+  if (dverts && edge_blocks > 0)
+    k_edge_adjoint_set<<<(unsigned)edge_blocks, 256, 0, s>>>(S, edge_block0, bits, wv, dverts,
+                                                             out);
 }
 
 void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32_t* bits,

@@ -283,15 +283,29 @@ struct dax_gb300_mc_batch {
   // warp batch, and the dealt (1) or per-lane (0) count pass
   int emit_batch = daxgb::kEmitBatch;
   int dealt = 1;
+  // grid-set CellGradient and adjoint: totals of the concatenated per-cell
+  // and per-point arrays, and per grid the first block of each set launch
+  // (d_blk: [gradient][adjoint gradient term][adjoint vertex term], count + 1
+  // each)
+  long long cells = 0, points = 0;
+  long long* d_blk = nullptr;
+  long long blk_total[3] = {0, 0, 0};
+  bool grad_vec = true, grad_loadv = true;
 
   daxgb::GridSet set() const {
     daxgb::GridSet S{};
-    S.slots = d_slots;
+    S.slots = count > 1 ? d_slots : nullptr;
     S.count = count;
     S.rows = rows;
     S.chunks = chunks;
     S.rowwords = rowwords;
     if (count == 1) S.one = slots[0];
+    return S;
+  }
+  // the set for the grid-set launches, which always read the slot table
+  daxgb::GridSet set_for_sets() const {
+    daxgb::GridSet S = set();
+    S.slots = d_slots;
     return S;
   }
 };
@@ -1083,6 +1097,12 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
     sl.word0 = 4 * b->chunks;
     sl.row0 = b->rows;
     sl.rw0 = b->rowwords;
+    sl.cell0 = b->cells;
+    sl.point0 = b->points;
+    b->cells += (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 1);
+    b->points += g.P;
+    b->grad_vec = b->grad_vec && (sl.cell0 % 2 == 0);
+    b->grad_loadv = b->grad_loadv && (g.nx % 2 == 0) && ((reinterpret_cast<uintptr_t>(fi) & 7) == 0);
     b->rowwords += g.R * g.wr;
     b->chunks += (g.P + 127) / 128;
     b->rows += g.R;
@@ -1092,17 +1112,29 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
   b->words = 4 * b->chunks + 8;
   b->off_goff = align256(sizeof(Info));
   b->L = mc_layout_words(b->rowwords, b->words, b->off_goff + 16 * (size_t)(num_grids + 1));
-  if (num_grids > 1) {
-    cudaError_t e = cudaMalloc(&b->d_slots, sizeof(daxgb::GridSlot) * num_grids);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_slots, b->slots.data(), sizeof(daxgb::GridSlot) * num_grids,
-                     cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      if (b->d_slots) cudaFree(b->d_slots);
-      delete b;
-      return e == cudaErrorMemoryAllocation ? fail(DAX_GB300_ERROR_OUT_OF_MEMORY, "batch table")
-                                            : cuda_fail(e, "uploading batch table");
-    }
+  // per grid, the first block of each grid-set launch
+  std::vector<long long> blk(3 * (size_t)(num_grids + 1), 0);
+  for (int i = 0; i < num_grids; ++i) {
+    const Grid& g = b->slots[i].g;
+    const long long n[3] = {daxgb::grad_blocks(g), daxgb::adjoint_grad_blocks(g),
+                            daxgb::adjoint_edge_blocks(g)};
+    for (int k = 0; k < 3; ++k) blk[k * (num_grids + 1) + i + 1] = blk[k * (num_grids + 1) + i] + n[k];
+  }
+  for (int k = 0; k < 3; ++k) b->blk_total[k] = blk[k * (num_grids + 1) + num_grids];
+  // the slot table (also for one grid: the grid-set launches read it)
+  cudaError_t e = cudaMalloc(&b->d_slots, sizeof(daxgb::GridSlot) * num_grids);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_slots, b->slots.data(), sizeof(daxgb::GridSlot) * num_grids,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_blk, blk.size() * sizeof(long long));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_blk, blk.data(), blk.size() * sizeof(long long), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (b->d_slots) cudaFree(b->d_slots);
+    if (b->d_blk) cudaFree(b->d_blk);
+    delete b;
+    return e == cudaErrorMemoryAllocation ? fail(DAX_GB300_ERROR_OUT_OF_MEMORY, "batch table")
+                                          : cuda_fail(e, "uploading batch table");
   }
   *out = b;
   return DAX_GB300_SUCCESS;
@@ -1111,6 +1143,7 @@ int dax_gb300_mc_batch_create(int num_grids, const dax_gb300_uniform_grid* grids
 int dax_gb300_mc_batch_destroy(dax_gb300_mc_batch* b) {
   if (!b) return DAX_GB300_SUCCESS;
   if (b->d_slots) cudaFree(b->d_slots);
+  if (b->d_blk) cudaFree(b->d_blk);
   delete b;
   return DAX_GB300_SUCCESS;
 }
@@ -1165,6 +1198,40 @@ int dax_gb300_mc_batch_generate(dax_gb300_mc_batch* b, int merge, void* d_scratc
                               &info->ticket, &info->done, b->emit_batch, daxgb::kPassEmit,
                               num_sms(), static_cast<cudaStream_t>(stream));
   return check_launch("batch generate kernel");
+}
+
+int dax_gb300_mc_batch_sizes(const dax_gb300_mc_batch* b, int64_t* num_cells,
+                             int64_t* num_points) {
+  if (!b) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch");
+  if (num_cells) *num_cells = b->cells;
+  if (num_points) *num_points = b->points;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_mc_batch_cell_gradient(const dax_gb300_mc_batch* b, float* d_out, void* stream) {
+  if (!b || (!d_out && b->cells > 0)) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or output");
+  const bool vec = b->grad_vec && (reinterpret_cast<uintptr_t>(d_out) & 7) == 0;
+  daxgb::launch_cell_gradient_set(b->set_for_sets(), b->d_blk, b->blk_total[0], vec, b->grad_loadv,
+                                  d_out, static_cast<cudaStream_t>(stream));
+  return check_launch("batch cell gradient kernel");
+}
+
+int dax_gb300_mc_batch_field_adjoint(const dax_gb300_mc_batch* b, const void* d_scratch,
+                                     size_t scratch_bytes, const float* d_grad_vertices,
+                                     const float* d_grad_cell_gradients, float* d_grad_fields,
+                                     void* stream) {
+  if (!b || !d_grad_fields) return fail(DAX_GB300_ERROR_BAD_VALUE, "NULL batch or output");
+  if (d_grad_vertices && (!d_scratch || scratch_bytes < b->L.total))
+    return fail(DAX_GB300_ERROR_BAD_VALUE, "the vertex term needs the batch's count scratch");
+  const int n = b->count + 1;
+  void* sc = const_cast<void*>(d_scratch);
+  const daxgb::WordOffsets wo = d_scratch ? b->L.offsets(sc) : daxgb::WordOffsets{};
+  daxgb::launch_field_adjoint_set(b->set_for_sets(), b->d_blk + n, b->blk_total[1],
+                                  b->d_blk + 2 * n, b->blk_total[2], b->points,
+                                  d_scratch ? at<uint32_t>(sc, b->L.bits) : nullptr, wo.wv,
+                                  d_grad_vertices, d_grad_cell_gradients, d_grad_fields,
+                                  static_cast<cudaStream_t>(stream));
+  return check_launch("batch field adjoint kernels");
 }
 
 int dax_gb300_mc_batch_set_config(dax_gb300_mc_batch* b, int emit_batch, int dealt_count) {

@@ -68,6 +68,8 @@ struct GridSlot {
   long long rw0;          // first global row word (row-padded word arrays)
   float3 plane_o;         // field == NULL: the implicit slice field
   float3 plane_n;         //   dot(plane_n, coord - plane_o)
+  long long cell0;        // first cell / point of the grid in per-cell and
+  long long point0;       //   per-point arrays concatenated over a grid set
 };
 
 // A set of grids processed by one launch per pass.  count == 1: the grid is
@@ -146,6 +148,17 @@ __device__ __forceinline__ int slot_after(const GridSet& S, const long long* key
   int si = from;
   while (si + 1 < S.count && (keys ? keys[si + 1] : __ldg(&S.slots[si + 1].rw0)) <= x) ++si;
   return si;
+}
+
+// The slot whose first block (block0[slot], ascending) is the last at or
+// before block b: the grid a block of a grid-set launch works for.
+__device__ __forceinline__ int block_slot(const long long* block0, int count, long long b) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(block0 + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 __device__ __forceinline__ GridSlot load_slot(const GridSet& S, int i) {

@@ -225,11 +225,12 @@ __device__ __forceinline__ void tile_rows(const TilePlane& P, const TilePlane& Q
   }
 }
 
+// One warp tile (task) of one grid; the kernels below map blocks to tasks.
 template <bool VEC, bool LOADV>
-__global__ void __launch_bounds__(kGradWarps * 32, kGradMinBlocks)
-    k_cell_gradient(Grid g, const float* __restrict__ f, float* __restrict__ out, MarchTiles mt) {
+__device__ __forceinline__ void cell_gradient_task(const Grid& g, const float* __restrict__ f,
+                                                   float* __restrict__ out, const MarchTiles& mt,
+                                                   long long task) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long task = (long long)blockIdx.x * kGradWarps + wib;
   if (task >= mt.tasks) return;  // the whole warp leaves; no block barrier follows
   const int xw = (int)(task % mt.nxw);
   const long long t2 = task / mt.nxw;
@@ -304,13 +305,54 @@ __global__ void __launch_bounds__(kGradWarps * 32, kGradMinBlocks)
   }
 }
 
-MarchTiles march_tiles(int nx, int ny, int nz, int band) {
+template <bool VEC, bool LOADV>
+__global__ void __launch_bounds__(kGradWarps * 32, kGradMinBlocks)
+    k_cell_gradient(Grid g, const float* __restrict__ f, float* __restrict__ out, MarchTiles mt) {
+  cell_gradient_task<VEC, LOADV>(g, f, out, mt,
+                                 (long long)blockIdx.x * kGradWarps + (threadIdx.x >> 5));
+}
+
+// Cell tiles of one grid's CellGradient.
+__host__ __device__ inline MarchTiles grad_tiles(const Grid& g) {
   MarchTiles mt;
-  mt.nxw = (nx + kMarchCols - 1) / kMarchCols;
-  mt.nband = (ny + band - 1) / band;
-  mt.nseg = (nz + kSeg - 1) / kSeg;
+  mt.nxw = (g.nx - 1 + kGradCols - 1) / kGradCols;
+  mt.nband = (g.ny - 1 + kGradBand - 1) / kGradBand;
+  mt.nseg = (g.nz - 1 + kGradSeg - 1) / kGradSeg;
   mt.tasks = (long long)mt.nxw * mt.nband * mt.nseg;
   return mt;
+}
+
+// A grid set: block b works for the grid whose first block (block0) is the
+// last at or before b; the grid's gradients start at its first cell.
+template <bool VEC, bool LOADV>
+__global__ void __launch_bounds__(kGradWarps * 32, kGradMinBlocks)
+    k_cell_gradient_set(GridSet S, const long long* __restrict__ block0,
+                        float* __restrict__ out) {
+  const int si = block_slot(block0, S.count, blockIdx.x);
+  const Grid g = S.slots[si].g;
+  cell_gradient_task<VEC, LOADV>(g, S.slots[si].field, out + 3 * S.slots[si].cell0, grad_tiles(g),
+                                 ((long long)blockIdx.x - __ldg(block0 + si)) * kGradWarps +
+                                     (threadIdx.x >> 5));
+}
+
+long long grad_blocks(const Grid& g) {
+  if (g.nx < 2 || g.ny < 2 || g.nz < 2) return 0;
+  return (grad_tiles(g).tasks + kGradWarps - 1) / kGradWarps;
+}
+
+void launch_cell_gradient_set(const GridSet& S, const long long* block0, long long blocks,
+                              bool vec, bool loadv, float* out, cudaStream_t s) {
+  if (blocks <= 0) return;
+  const dim3 block(kGradWarps * 32);
+  const unsigned nb = (unsigned)blocks;
+  if (vec && loadv)
+    k_cell_gradient_set<true, true><<<nb, block, 0, s>>>(S, block0, out);
+  else if (vec)
+    k_cell_gradient_set<true, false><<<nb, block, 0, s>>>(S, block0, out);
+  else if (loadv)
+    k_cell_gradient_set<false, true><<<nb, block, 0, s>>>(S, block0, out);
+  else
+    k_cell_gradient_set<false, false><<<nb, block, 0, s>>>(S, block0, out);
 }
 
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s) {

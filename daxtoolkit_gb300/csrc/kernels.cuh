@@ -226,7 +226,14 @@ struct MarchTiles {
   long long tasks;       // nxw * nband * nseg, x fastest
 };
 // Tiles covering an nx x ny x nz box of cells or points, `band` rows each.
-MarchTiles march_tiles(int nx, int ny, int nz, int band);
+__host__ __device__ inline MarchTiles march_tiles(int nx, int ny, int nz, int band) {
+  MarchTiles mt;
+  mt.nxw = (nx + kMarchCols - 1) / kMarchCols;
+  mt.nband = (ny + band - 1) / band;
+  mt.nseg = (nz + kSeg - 1) / kSeg;
+  mt.tasks = (long long)mt.nxw * mt.nband * mt.nseg;
+  return mt;
+}
 
 // dL/dfield from dL/d(merged vertices) (needs the count pass's bits and
 // word offsets) and/or dL/d(cell gradients); out is fully written.
@@ -235,6 +242,25 @@ void launch_field_adjoint(const Grid& g, const float* f, float iso, const uint32
                           float* out, int num_sms, cudaStream_t s);
 
 void launch_cell_gradient(const Grid& g, const float* f, float* out, int num_sms, cudaStream_t s);
+
+// Grid sets (one launch for all grids; block0[slot] = the grid's first block,
+// from the per-grid block counts below; per-cell and per-point arrays are
+// concatenated over the set at the slots' cell0 / point0).
+long long grad_blocks(const Grid& g);
+long long adjoint_grad_blocks(const Grid& g);
+long long adjoint_edge_blocks(const Grid& g);
+// vec: every grid's output 8-byte aligned; loadv: every grid's nx even and
+// field 8-byte aligned (the single-grid kernel's fast paths).
+void launch_cell_gradient_set(const GridSet& S, const long long* block0, long long blocks,
+                              bool vec, bool loadv, float* out, cudaStream_t s);
+// dL/dfield of every grid, out[points]: the gradient term from dgrad (or
+// zero) then the vertex term from dverts (the set's merged vertices; needs
+// the set's count pass: bits and word offsets wv).
+void launch_field_adjoint_set(const GridSet& S, const long long* grad_block0,
+                              long long grad_blocks, const long long* edge_block0,
+                              long long edge_blocks, long long points, const uint32_t* bits,
+                              const uint32_t* wv, const float* dverts, const float* dgrad,
+                              float* out, cudaStream_t s);
 
 // Slice: the isovalue dot(normal, origin); the classification bits of the
 // implicit field dot(normal, coord - origin) > iso (bit_words(P) words, the

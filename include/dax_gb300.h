@@ -484,6 +484,31 @@ int dax_gb300_mc_batch_autotune(dax_gb300_mc_batch* batch, int merge, void* d_sc
                                 size_t scratch_bytes, float* d_verts, int64_t vert_capacity,
                                 int32_t* d_conn, int64_t tri_capacity, void* stream,
                                 float* h_best_ms);
+/* Sizes of the arrays the grid-set CellGradient and adjoint concatenate over
+ * the batch's grids, in the order the grids were given: cells and points. */
+int dax_gb300_mc_batch_sizes(const dax_gb300_mc_batch* batch, int64_t* num_cells,
+                             int64_t* num_points);
+
+/* DispatcherMapCell<CellGradient> (dax/worklet/CellGradient.h:28-48) on every
+ * grid of the batch in one launch: d_out (float[num_cells][3]) holds grid 0's
+ * cell gradients, then grid 1's, ...; each grid's are those of
+ * dax_gb300_cell_gradient.  Asynchronous. */
+int dax_gb300_mc_batch_cell_gradient(const dax_gb300_mc_batch* batch, float* d_out, void* stream);
+
+/* dax_gb300_field_adjoint on every grid of the batch in two launches (no
+ * counterpart in the reference): d_grad_fields (float[num_points], grids
+ * concatenated) = dL/dfield from d_grad_vertices (float[V][3], the batch's
+ * merged vertices as dax_gb300_mc_batch_generate wrote them; needs the
+ * batch's count pass on d_scratch, which may be recomputed) and/or
+ * d_grad_cell_gradients (float[num_cells][3] in the order of
+ * dax_gb300_mc_batch_cell_gradient); either may be NULL.  Each grid's slice
+ * equals dax_gb300_field_adjoint's result for that grid bit for bit.
+ * Deterministic, no atomics.  Asynchronous. */
+int dax_gb300_mc_batch_field_adjoint(const dax_gb300_mc_batch* batch, const void* d_scratch,
+                                     size_t scratch_bytes, const float* d_grad_vertices,
+                                     const float* d_grad_cell_gradients, float* d_grad_fields,
+                                     void* stream);
+
 /* Sets (emit_batch 1..32, 0 = default 16; dealt_count 1, 0, -1 = default)
  * or reads a plan's configuration. */
 int dax_gb300_mc_batch_set_config(dax_gb300_mc_batch* batch, int emit_batch, int dealt_count);

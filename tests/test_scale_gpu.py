@@ -216,3 +216,68 @@ def test_batch32_forward_adjoint_graph(gb300):
         scale = ref.abs().max().item()
         err = (it["dfield"].double() - ref).abs().max().item()
         assert err <= TOL * scale, (d, err, scale)
+
+
+def test_batch32_grid_set_forward_adjoint_graph(gb300):
+    """The same 32-grid workload through the grid-set launches: count,
+    generate, CellGradient, the count pass again (recompute in backward) and
+    the field adjoint of every grid, one launch per pass for all grids,
+    captured in one CUDA graph.  Every grid's slice equals the single-grid
+    entry points bit for bit (which the test above checks against FP64)."""
+    from daxtoolkit_gb300 import capi, synthetic
+    cont = gb300
+    dev = torch.device("cuda")
+    dims = synthetic.batch_grid_dims(32, 64, 160, 1024)
+    isos = synthetic.batch_isovalues(32, 0.3, 0.6, 1024)
+    grids, fields = [], []
+    for q, d in enumerate(dims):
+        grids.append(cont.UniformGrid(d, spacing=tuple(1.0 / (x - 1) for x in d)))
+        fields.append(synthetic.blob_field(d, 16, seed=3000 + q, device=dev))
+    batch = cont.MarchingCubesBatch(grids, fields, isos)
+    verts, conn, toff, voff = batch.run(merge=True)
+    C, P = batch.sizes()
+    grad = torch.empty((C, 3), dtype=torch.float32, device=dev)
+    dV = torch.empty_like(verts)
+    dfield = torch.empty(P, dtype=torch.float32, device=dev)
+
+    def pipeline(stream):
+        batch.count(stream)
+        batch.generate(verts, conn, True, stream)
+        batch.cell_gradient(grad, stream)
+        with torch.cuda.stream(stream):
+            torch.mul(verts, 2.0, out=dV)
+            torch.mul(grad, 2.0, out=grad)
+        batch.count(stream)
+        batch.field_adjoint(dV, grad, dfield, stream)
+
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    pipeline(stream)
+    torch.cuda.synchronize()
+    eager = (verts.clone(), conn.clone(), dfield.clone())
+    dfield.zero_()
+    verts.zero_()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        pipeline(stream)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(verts, eager[0]) and torch.equal(conn, eager[1])
+    assert torch.equal(dfield.view(torch.int32), eager[2].view(torch.int32))
+    # grid by grid against the single-grid entry points
+    c0 = p0 = 0
+    for q, (gr, f, iso) in enumerate(zip(grids, fields, isos)):
+        nc, npts = gr.GetNumberOfCells(), gr.GetNumberOfPoints()
+        g1 = cont.cell_gradient(gr, f)
+        assert torch.equal((g1 * 2.0).view(torch.int32), grad[c0:c0 + nc].view(torch.int32)), q
+        nb = capi.lib().dax_gb300_mc_scratch_bytes(ctypes.byref(gr.desc()))
+        scratch = torch.empty(nb, dtype=torch.uint8, device=dev)
+        out1 = torch.empty_like(f)
+        dV1 = dV[voff[q]:voff[q + 1]].contiguous()
+        dG1 = grad[c0:c0 + nc].contiguous()
+        _adjoint(cont, gr, f, iso, dV1, dG1, scratch, out1)
+        torch.cuda.synchronize()
+        assert torch.equal(out1.view(torch.int32), dfield[p0:p0 + npts].view(torch.int32)), q
+        c0 += nc
+        p0 += npts
+    assert (c0, p0) == (C, P)
