@@ -565,8 +565,91 @@ def extra_measurements(field, grid, dims, iso, peak, stream, dev, reps=50):
                               "batched_graph_replay_only: the batch's graph replay without the "
                               "totals read",
                       "graph_replay_matches_batch_run": ok}
+    del grids, fields, batch, bv, bc, gv, gc
+    out["batched_forward_adjoint"] = batch_adjoint_measurements(stream, dev)
     out["primitives"] = primitive_measurements(peak, stream, dev)
     return out
+
+
+def batch_adjoint_measurements(stream, dev, reps=20):
+    """32 grids, each dimension U{64..160}, 16 blobs, isovalue U[0.3,0.6]:
+    forward (count, merged generate, CellGradient) and adjoint (the count
+    pass again, dL/dfield from dL/dvertices and dL/dgradient) of every grid,
+    (a) as the per-grid sequence of single-grid calls, (b) as the grid-set
+    launches (one per pass for all grids), each captured in one CUDA graph
+    and replayed.  The two arms' dL/dfield agree bit for bit."""
+    import torch
+    from daxtoolkit_gb300 import capi, cont, synthetic
+    L = capi.lib()
+    ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    dims = synthetic.batch_grid_dims(32, 64, 160, 1024)
+    isos = synthetic.batch_isovalues(32, 0.3, 0.6, 1024)
+    grids, fields = [], []
+    for q, d in enumerate(dims):
+        grids.append(cont.UniformGrid(d, spacing=tuple(1.0 / (x - 1) for x in d)))
+        fields.append(synthetic.blob_field(d, 16, seed=3000 + q, device=dev))
+    batch = cont.MarchingCubesBatch(grids, fields, isos)
+    verts, conn, toff, voff = batch.run(merge=True)
+    C, P = batch.sizes()
+    grad = torch.empty((C, 3), dtype=torch.float32, device=dev)
+    dV = torch.randn_like(verts)
+    dG = torch.randn((C, 3), dtype=torch.float32, device=dev)
+    dfield = torch.empty(P, dtype=torch.float32, device=dev)
+    items, c0, p0 = [], 0, 0
+    for q, (gr, f, iso) in enumerate(zip(grids, fields, isos)):
+        d = gr.desc()
+        nb = L.dax_gb300_mc_scratch_bytes(ctypes.byref(d))
+        nc, npts = gr.GetNumberOfCells(), gr.GetNumberOfPoints()
+        items.append(dict(d=d, f=f, iso=float(iso), nb=nb,
+                          scr=torch.empty(nb, dtype=torch.uint8, device=dev),
+                          verts=torch.empty((max(voff[q + 1] - voff[q], 1), 3), device=dev),
+                          conn=torch.empty((max(toff[q + 1] - toff[q], 1), 3), dtype=torch.int32,
+                                           device=dev),
+                          V=voff[q + 1] - voff[q], T=toff[q + 1] - toff[q],
+                          grad=grad[c0:c0 + nc], dV=dV[voff[q]:voff[q + 1]].contiguous(),
+                          dG=dG[c0:c0 + nc], out=torch.empty(npts, device=dev), p0=p0))
+        c0 += nc
+        p0 += npts
+
+    def per_grid(st):
+        for it in items:
+            d = ctypes.byref(it["d"])
+            capi.call("dax_gb300_mc_count", d, ptr(it["f"]), it["iso"], ptr(it["scr"]), it["nb"], st)
+            capi.call("dax_gb300_mc_generate", d, ptr(it["f"]), it["iso"], 1, ptr(it["scr"]),
+                      it["nb"], ptr(it["verts"]), it["V"], ptr(it["conn"]), it["T"], None, None,
+                      None, st)
+            capi.call("dax_gb300_cell_gradient", d, ptr(it["f"]), ptr(it["grad"]), st)
+            capi.call("dax_gb300_mc_count", d, ptr(it["f"]), it["iso"], ptr(it["scr"]), it["nb"], st)
+            capi.call("dax_gb300_field_adjoint", d, ptr(it["f"]), it["iso"], ptr(it["scr"]),
+                      it["nb"], ptr(it["dV"]), ptr(it["dG"]), ptr(it["out"]), st)
+
+    def grid_set(st):
+        batch.count(st)
+        batch.generate(verts, conn, True, st)
+        batch.cell_gradient(grad, st)
+        batch.count(st)
+        batch.field_adjoint(dV, dG, dfield, st)
+
+    side = torch.cuda.Stream(device=dev)
+    res = {}
+    for name, fn in (("per_grid", per_grid), ("grid_set", grid_set)):
+        side.wait_stream(stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+            fn(side)
+        torch.cuda.synchronize()
+        res[name] = _event_ms(g.replay, reps, stream)
+        del g
+    ok = all(bool(torch.equal(it["out"].view(torch.int32),
+                              dfield[it["p0"]:it["p0"] + it["out"].numel()].view(torch.int32)))
+             for it in items)
+    return {"grids": 32, "grid_dims": "each U{64..160}, seed 1024",
+            "cells": C, "points": P, "triangles": toff[-1],
+            "per_grid_graph_ms": res["per_grid"], "grid_set_graph_ms": res["grid_set"],
+            "speedup": res["per_grid"] / res["grid_set"],
+            "grid_set_matches_per_grid": ok,
+            "note": "forward (count, merged generate, CellGradient) + adjoint (count recomputed, "
+                    "dL/dfield of vertices and gradients) of every grid, each arm one CUDA graph"}
 
 
 def mt_measurements(peak, stream, dev, reps=10, n=256):

@@ -22,7 +22,7 @@ OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libdax_gb300.so")
 
 SOURCES = ["classify.cu", "mc.cu", "pipeline.cu", "threshold.cu", "gradient.cu", "adjoint.cu", "capi.cu",
-           "noalloc.cu", "memory.cu", "primitives.cu", "slice.cu", "mt.cu",
+           "noalloc.cu", "memory.cu", "fused.cu", "staged.cu", "primitives.cu", "slice.cu", "mt.cu",
            "mandelbulb.cu", "fields.cu", "vtk.cu", "selftest.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "mc_case.cuh", "mc_tables.h", "mt_tables.h",
            "coolwarm_table.h"]

@@ -124,6 +124,8 @@ SIGNATURES = {
     "dax_gb300_colors_and_norms": ([vp, i64, vp, vp, vp], i32),
     "dax_gb300_report_error": ([ctypes.c_int, ctypes.c_char_p], i32),
     "dax_gb300_set_blocks_per_sm": ([ctypes.c_int, ctypes.c_int], i32),
+    "dax_gb300_set_fused_count": ([ctypes.c_int, ctypes.c_int], i32),
+    "dax_gb300_get_fused_count": ([ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], i32),
     "dax_gb300_set_pipeline_slabs": ([ctypes.c_int], i32),
     "dax_gb300_device_alloc": ([ctypes.POINTER(vp), ctypes.c_uint64], i32),
     "dax_gb300_device_free": ([vp], i32),

@@ -91,21 +91,24 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Marching-cubes scratch: [Info][tile totals 3 x tiles][wc][wt][wv][act]
-// [slab: active-word prefixes of the pipelined call's slabs][bits].
+// Marching-cubes scratch: [Info][fused count control words][tile totals
+// 3 x tiles][wc][wt][wv][act][slab: active-word prefixes of the pipelined
+// call's slabs][bits].
 struct McLayout {
   long long rowwords;
   int tiles;
-  size_t info, tile, wc, wt, wv, act, slab, bits, total;
+  size_t info, fctl, tile, wc, wt, wv, act, slab, bits, total;
   daxgb::WordOffsets offsets(void* base) const;
 };
 
-McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head) {
+// fctl_bytes: the control words of the fused count pass (one grid).
+McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head, size_t fctl_bytes = 0) {
   McLayout L;
   L.rowwords = rowwords;
   L.tiles = daxgb::word_scan_tiles(rowwords);
   L.info = 0;
-  L.tile = align256(head);
+  L.fctl = align256(head);
+  L.tile = align256(L.fctl + fctl_bytes);
   L.wc = align256(L.tile + 3 * 4 * (size_t)L.tiles);
   L.wt = align256(L.wc + 4 * (size_t)rowwords);
   L.wv = align256(L.wt + 4 * (size_t)(rowwords + 1));
@@ -117,7 +120,7 @@ McLayout mc_layout_words(long long rowwords, long long bitwords, size_t head) {
 }
 
 McLayout mc_layout(const Grid& g) {
-  return mc_layout_words(g.R * g.wr, daxgb::bit_words(g.P), sizeof(Info));
+  return mc_layout_words(g.R * g.wr, daxgb::bit_words(g.P), sizeof(Info), daxgb::fused_ctl_bytes(g));
 }
 
 // Threshold scratch: the marching-cubes sections, then the per-word kept-cell
@@ -130,7 +133,7 @@ struct Layout {
 Layout layout(const Grid& g) {
   Layout L;
   const long long W = g.R * g.wr;
-  L.m = mc_layout_words(W, daxgb::bit_words(g.P), sizeof(Info));
+  L.m = mc_layout_words(W, daxgb::bit_words(g.P), sizeof(Info), daxgb::fused_ctl_bytes(g));
   L.kept = L.m.total;
   L.used = align256(L.kept + 4 * (size_t)W);
   L.total = align256(L.used + 4 * (size_t)W);
@@ -194,11 +197,27 @@ int read_totals(const void* scratch, int64_t* a, int64_t* b, cudaStream_t s) {
   if (h.error & daxgb::kErrState)
     return fail(DAX_GB300_ERROR_BAD_VALUE,
                 "the merge scratch does not hold dax_gb300_mt_merge's result for this count pass");
+  if (h.error & daxgb::kErrTimeout)
+    return fail(DAX_GB300_ERROR_TIMEOUT,
+                "a bounded device-side wait of the count pass ran out; no result");
   if (h.error & daxgb::kErrBadIndex)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "a cell lists a point id outside [0, num_points)");
   if (h.error & daxgb::kErrCapacity)
     return fail(DAX_GB300_ERROR_CAPACITY, "output capacity smaller than the result; nothing written");
   return DAX_GB300_SUCCESS;
+}
+
+// The fused count pass streams the field with bulk TMA copies: it takes
+// 16-byte aligned device memory (page-locked host and managed fields take
+// the three-launch pass).
+bool fused_ok(const float* field) {
+  if (!daxgb::fused_count_enabled() || !aligned16(field)) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, field) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice;
 }
 
 int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field, float a, float b,
@@ -216,11 +235,25 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
     return e == cudaSuccess ? DAX_GB300_SUCCESS : cuda_fail(e, "clearing scratch");
   }
   const int sms = num_sms();
+  if (fused_ok(field)) {
+    // classification and counts in one launch, then the scan
+    const McLayout M = mode == 0 ? mc_layout(g) : layout(g).m;
+    uint32_t* kept = mode == 0 ? nullptr : at<uint32_t>(scratch, layout(g).kept);
+    uint32_t* used = mode == 0 ? nullptr : at<uint32_t>(scratch, layout(g).used);
+    const int e = daxgb::launch_fused_count(mode, g, field, a, b, at<uint32_t>(scratch, M.bits),
+                                            daxgb::bit_words(g.P), M.offsets(scratch),
+                                            at<Info>(scratch, M.info), kept, used,
+                                            at<uint32_t>(scratch, M.fctl), sms, s);
+    if (e != 0) return cuda_fail(static_cast<cudaError_t>(e), "fused count kernel");
+    return check_launch("fused count kernel");
+  }
   const daxgb::GridSet S = daxgb::single_set(g, field, a, b);
   if (mode == 0) {
     const McLayout L = mc_layout(g);
     uint32_t* bits = at<uint32_t>(scratch, L.bits);
-    daxgb::launch_classify_bits(0, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
+    // the classification clears Info's error words first
+    daxgb::launch_classify_range(0, S, aligned16(field), bits, daxgb::bit_words(g.P), 0, S.chunks,
+                                 at<Info>(scratch, L.info), daxgb::kPassClassify, false, sms, s);
     if ((st = check_launch("classify kernel"))) return st;
     const daxgb::WordOffsets o = L.offsets(scratch);
     daxgb::launch_mc_scan(S, bits, o, at<Info>(scratch, L.info), sms, s);
@@ -228,7 +261,8 @@ int count_pass(int mode, const dax_gb300_uniform_grid* grid, const float* field,
   }
   const Layout L = layout(g);
   uint32_t* bits = at<uint32_t>(scratch, L.m.bits);
-  daxgb::launch_classify_bits(1, S, aligned16(field), bits, daxgb::bit_words(g.P), sms, s);
+  daxgb::launch_classify_range(1, S, aligned16(field), bits, daxgb::bit_words(g.P), 0, S.chunks,
+                               at<Info>(scratch, L.m.info), daxgb::kPassClassify, false, sms, s);
   if ((st = check_launch("classify kernel"))) return st;
   const daxgb::WordOffsets o = L.m.offsets(scratch);
   daxgb::launch_thr_count(g, bits, at<uint32_t>(scratch, L.kept), at<uint32_t>(scratch, L.used),
@@ -262,7 +296,7 @@ int cached_occupancy(const void* kernel, int threads, size_t smem) {
 }
 
 namespace {
-int g_blocks_per_sm[kTunedPasses] = {0, 0, 0, 3, 0, 1};
+int g_blocks_per_sm[kTunedPasses] = {0, 0, 0, 3, 0, 1, 0};
 }
 int tuned_blocks_per_sm(int pass) {
   return pass >= 0 && pass < kTunedPasses ? g_blocks_per_sm[pass] : 0;
@@ -318,6 +352,18 @@ int dax_gb300_set_blocks_per_sm(int pass, int blocks) {
   if (pass < 0 || pass >= daxgb::kTunedPasses || blocks < 0)
     return fail(DAX_GB300_ERROR_BAD_VALUE, "unknown pass or negative block count");
   daxgb::g_blocks_per_sm[pass] = blocks;
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_set_fused_count(int enabled, int unit_stages) {
+  if (enabled < -1 || enabled > 1) return fail(DAX_GB300_ERROR_BAD_VALUE, "enabled must be -1, 0 or 1");
+  daxgb::set_fused_count(enabled, unit_stages);
+  return DAX_GB300_SUCCESS;
+}
+
+int dax_gb300_get_fused_count(int* enabled, int* unit_stages) {
+  if (enabled) *enabled = daxgb::fused_count_enabled();
+  if (unit_stages) *unit_stages = daxgb::fused_unit_stages();
   return DAX_GB300_SUCCESS;
 }
 
@@ -439,6 +485,7 @@ int dax_gb300_mc_pipeline(const dax_gb300_uniform_grid* grid, const float* d_fie
                                    L.offsets(d_scratch), at<Info>(d_scratch, L.info),
                                    at<uint32_t>(d_scratch, L.slab), d_verts, vert_capacity, d_conn,
                                    tri_capacity, d_rec_first, d_rec_second, d_rec_weight,
+                                   fused_ok(d_field) ? at<uint32_t>(d_scratch, L.fctl) : nullptr,
                                    num_sms(), s);
 }
 
@@ -523,6 +570,7 @@ int dax_gb300_slice_count(const dax_gb300_uniform_grid* grid, const float* origi
   const daxgb::WordOffsets wo = L.offsets(d_scratch);
   // the row splits live in the active-word list (R <= R * wr entries), which
   // the scan rewrites afterwards
+  cudaMemsetAsync(at<Info>(d_scratch, L.info), 0, sizeof(Info), s);  // the error words
   daxgb::launch_slice_bits(g, S.one.plane_o, S.one.plane_n, iso, bits, daxgb::bit_words(g.P),
                            wo.act, sms, s);
   if ((st = check_launch("slice classify kernels"))) return st;
@@ -1157,7 +1205,9 @@ int dax_gb300_mc_batch_count(dax_gb300_mc_batch* b, void* d_scratch, size_t scra
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const daxgb::GridSet S = b->set();
   uint32_t* bits = at<uint32_t>(d_scratch, b->L.bits);
-  daxgb::launch_classify_bits(0, S, b->aligned, bits, b->words, num_sms(), s);
+  // the classification clears Info's error words first
+  daxgb::launch_classify_range(0, S, b->aligned, bits, b->words, 0, S.chunks, at<Info>(d_scratch, 0),
+                               daxgb::kPassClassify, false, num_sms(), s);
   int st = check_launch("batch classify kernel");
   if (st) return st;
   const daxgb::WordOffsets o = b->L.offsets(d_scratch);

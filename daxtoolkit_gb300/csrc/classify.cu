@@ -27,8 +27,8 @@ __device__ __forceinline__ uint32_t classify_point(float v, float a, float b) {
 //
 // [c_begin, c_end) restricts a one-grid launch to a range of chunks (the
 // slabs of the pipelined marching cubes); `init`, when not null, is the Info
-// block whose error word and emit counters this launch clears (the first
-// slab's classification runs before every other pass of a pipelined call).
+// block whose error words and emit counters this launch clears (it runs
+// before every other pass of its count pass).
 //
 // KEEP: the field is read with the default cache policy instead of
 // evict-first, so that a slab's values can still be in L2 when the emit of
@@ -51,16 +51,17 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
   __shared__ long long s_keys[kStagedSlots];
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.chunk0; }) ? s_keys : nullptr;
+  if (init && blockIdx.x == 0 && threadIdx.x == 0) {
+    init->error = 0;
+    init->aborted = 0;
+    init->ticket = 0;
+    init->done = 0;
+  }
   if (S.count == 1) {
     // one grid: field pointer and thresholds are loop invariants
     const float* __restrict__ f = S.one.field;
     const long long P = S.one.g.P;
     const float a = S.one.iso, b = S.one.iso_hi;
-    if (init && blockIdx.x == 0 && threadIdx.x == 0) {
-      init->error = 0;
-      init->ticket = 0;
-      init->done = 0;
-    }
     for (long long c0 = c_begin + warp * UNROLL; c0 < c_end; c0 += nwarps * UNROLL) {
       float4 v[UNROLL];
 #pragma unroll

@@ -173,7 +173,9 @@ struct Info {
   int error;              // kErr* bits raised on the device
   unsigned ticket;        // next batch of active words for the MC emit warps
   unsigned done;          // MC emit blocks finished (the last resets both)
-  int pad[7];
+  int aborted;            // a count kernel's bounded wait ran out (the scan
+                          //   reports it as kErrTimeout); cleared with error
+  int pad[6];
 };
 
 constexpr int kErrCapacity = 2;    // output buffer too small
@@ -181,6 +183,7 @@ constexpr int kErrOverflow = 4;    // more than 2^31 - 1 triangles or vertices
 constexpr int kErrBadIndex = 8;    // a cell lists a point id outside [0, P)
 constexpr int kErrState = 16;      // a merge scratch that no merge pass of this count wrote
 constexpr int kErrBadCount = 32;   // a count array asks a cell for a triangle its case lacks
+constexpr int kErrTimeout = 64;    // a bounded device-side wait ran out (the fused count pass)
 
 // Coordinate of grid index i along one axis: origin + spacing * (i + min),
 // computed in float with no fused multiply-add, as the reference's implicit
@@ -254,36 +257,47 @@ __device__ __forceinline__ float slot_value(const GridSlot& sl, long long p, int
   return sl.field ? __ldg(sl.field + p) : plane_value(sl.g, sl.plane_o, sl.plane_n, i, j, k);
 }
 
+// Bit-stream loads.  CG = false: the read-only path (the stream was written
+// by an earlier launch); CG = true: L2 only, for a stream that other blocks
+// of the same launch wrote (the fused classify + count kernel), which the
+// non-coherent path and L1 could serve stale.
+template <bool CG>
+__device__ __forceinline__ uint32_t ld_bits(const uint32_t* p) {
+  return CG ? __ldcg(p) : __ldg(p);
+}
+
 // 32 consecutive bits of the flat bit stream starting at bit `pos` (any
 // alignment).  The stream is padded so pos+63 is always readable.
+template <bool CG = false>
 __device__ __forceinline__ uint32_t bits_at(const uint32_t* __restrict__ bits, long long pos) {
   const long long w = pos >> 5;
-  const uint32_t lo = __ldg(bits + w);
-  const uint32_t hi = __ldg(bits + w + 1);
+  const uint32_t lo = ld_bits<CG>(bits + w);
+  const uint32_t hi = ld_bits<CG>(bits + w + 1);
   return __funnelshift_r(lo, hi, (unsigned)(pos & 31));
 }
 
 // bits_at(pos) and bits_at(pos + 1) (the +x neighbours) from the same two
 // words: the second is the first shifted down one bit with bit pos+32 on top.
+template <bool CG = false>
 __device__ __forceinline__ void bits_at2(const uint32_t* __restrict__ bits, long long pos,
                                          uint32_t& a, uint32_t& a1) {
   const long long w = pos >> 5;
   const unsigned sh = (unsigned)(pos & 31);
-  const uint32_t w0 = __ldg(bits + w), w1 = __ldg(bits + w + 1);
+  const uint32_t w0 = ld_bits<CG>(bits + w), w1 = ld_bits<CG>(bits + w + 1);
   a = __funnelshift_r(w0, w1, sh);
   a1 = __funnelshift_rc(w0, w1, sh + 1u);  // sh = 31: w1 whole
 }
 
-// Mask of the low n bits (n in [0, 32]).
 // Four consecutive 32-bit windows of a row (x = 32m .. 32m+127) and their +x
 // neighbours, from five word fetches.
+template <bool CG = false>
 __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, long long pos,
                                              uint32_t (&a)[4], uint32_t (&a1)[4]) {
   const long long w = pos >> 5;
   const unsigned sh = (unsigned)(pos & 31);
   uint32_t x[5];
 #pragma unroll
-  for (int e = 0; e < 5; ++e) x[e] = __ldg(bits + w + e);
+  for (int e = 0; e < 5; ++e) x[e] = ld_bits<CG>(bits + w + e);
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
     a[e] = __funnelshift_r(x[e], x[e + 1], sh);
@@ -291,6 +305,7 @@ __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, 
   }
 }
 
+// Mask of the low n bits (n in [0, 32]).
 __device__ __forceinline__ uint32_t low_mask(int n) {
   return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
 }

@@ -59,7 +59,8 @@ enum TunedPass {
   kPassPipeClassify = 3,
   kPassPipeCount = 4,
   kPassPipeEmit = 5,
-  kTunedPasses = 6
+  kPassFused = 6,  // the fused count pass (classify + count + scan, one launch)
+  kTunedPasses = 7
 };
 int tuned_blocks_per_sm(int pass);
 
@@ -145,8 +146,35 @@ void set_pipeline_options(const PipeOptions& o);
 PipeOptions pipeline_options();
 
 int word_scan_tiles(long long rowwords);
+
+// The fused count pass of one grid (marching cubes: mode 0; threshold:
+// mode 1): classification and per-word counts in one persistent launch,
+// then the scan -- the bits, wc / tile totals, wt / wv / act, the totals in
+// Info and (mode 1) the kept / used masks, bit for bit as the separate
+// passes write them.  The field must be 16-byte aligned device memory.  Its
+// control words (fctl, fused_ctl_bytes(g) bytes) are cleared first.
+// Returns a cudaError_t.
+int launch_fused_count(int mode, const Grid& g, const float* f, float a, float b, uint32_t* bits,
+                       long long nwords, const WordOffsets& o, Info* info, uint32_t* kept,
+                       uint32_t* used, uint32_t* fctl, int num_sms, cudaStream_t s);
+size_t fused_ctl_bytes(const Grid& g);
+// enabled: 1 / 0 (-1 keeps it); unit_stages: 16 KB stages per classify unit,
+// rounded down to a power of 2 (<= 0 keeps it).
+void set_fused_count(int enabled, int unit_stages);
+int fused_count_enabled();
+int fused_unit_stages();
+// abort (optional): a word that, when non-zero, makes the scan report
+// kErrTimeout (the fused count pass's abort word).
 void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
-                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s);
+                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s,
+                      const uint32_t* abort = nullptr);
+// Marching-cubes K2a of one grid with each scan tile's bits staged in
+// shared memory by bulk TMA copies (staged.cu): k_mc_count's outputs, bit
+// for bit.  False (nothing launched) when a tile's ranges do not fit the
+// shared memory.  A copy that does not arrive sets info->aborted, which the
+// scan reports as kErrTimeout.
+bool launch_mc_count_staged(const Grid& g, const uint32_t* bits, long long nwords,
+                            const WordOffsets& o, Info* info, int num_sms, cudaStream_t s);
 // Marching cubes K2a (counts: triangles, crossing edges) + K2b.
 // dealt != 0: for a grid set, the count pass that deals a warp's active cells
 // to its lanes (the default); 0: the per-lane count pass.  One grid always
@@ -177,11 +205,13 @@ void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, co
                           unsigned* ticket, unsigned* done, int batch, int pass, int num_sms,
                           cudaStream_t s);
 // The whole count + generate of one grid, slab-pipelined (pipeline.cu).
+// fctl: non-null runs a one-slab frame as the fused count pass (fctl: its
+// control words) and the emit, on the caller's stream.
 int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, bool merge,
                        uint32_t* bits, long long nwords, const WordOffsets& o, Info* info,
                        uint32_t* slab_act, float* verts, long long vcap, int32_t* conn,
-                       long long tcap, int32_t* ra, int32_t* rb, float* rw, int num_sms,
-                       cudaStream_t s);
+                       long long tcap, int32_t* ra, int32_t* rb, float* rw, uint32_t* fctl,
+                       int num_sms, cudaStream_t s);
 // goff[2g], goff[2g+1]: first triangle / merged vertex of grid g; then totals.
 void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff,
                          cudaStream_t s);

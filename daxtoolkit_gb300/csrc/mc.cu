@@ -30,6 +30,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mc_case.cuh"
+#include "mc_words.cuh"
 
 namespace daxgb {
 
@@ -39,10 +40,6 @@ namespace daxgb {
 __constant__ unsigned char kEdgeOwner[12] = {
     0 | (0 << 3), 1 | (1 << 3), 2 | (0 << 3), 0 | (1 << 3), 4 | (0 << 3), 5 | (1 << 3),
     6 | (0 << 3), 4 | (1 << 3), 0 | (2 << 3), 1 | (2 << 3), 3 | (2 << 3), 2 | (2 << 3)};
-
-struct CornerWords {
-  uint32_t a, a1, b, b1, c, c1, d, d1;
-};
 
 // The eight corner-bit words of cells 32m..32m+31 of cell row (j, k):
 // a = (i, j, k), a1 = (i+1, j, k), b = (i, j+1, k), c = (i, j, k+1), d = (i, j+1, k+1).
@@ -61,22 +58,6 @@ __device__ __forceinline__ CornerWords corner_words(const Grid& g, const uint32_
   return w;
 }
 
-// Case index of cell q of the word; vertex order v0..v7 =
-// (i,j,k) (i+1,j,k) (i+1,j+1,k) (i,j+1,k) and the same at k+1
-// (dax/exec/internal/TopologyUniform.h:150-157); bit n = value[n] > iso.
-__device__ __forceinline__ int case_of(const CornerWords& w, int q) {
-  return (int)(((w.a >> q) & 1u) | (((w.a1 >> q) & 1u) << 1) | (((w.b1 >> q) & 1u) << 2) |
-               (((w.b >> q) & 1u) << 3) | (((w.c >> q) & 1u) << 4) | (((w.c1 >> q) & 1u) << 5) |
-               (((w.d1 >> q) & 1u) << 6) | (((w.d >> q) & 1u) << 7));
-}
-
-// Cells of the word that are neither all-inside nor all-outside.
-__device__ __forceinline__ uint32_t active_cells(const CornerWords& w, uint32_t cell_mask) {
-  const uint32_t all1 = w.a & w.a1 & w.b & w.b1 & w.c & w.c1 & w.d & w.d1;
-  const uint32_t any1 = w.a | w.a1 | w.b | w.b1 | w.c | w.c1 | w.d | w.d1;
-  return any1 & ~all1 & cell_mask;
-}
-
 // Crossing-edge masks of point row (j, k), word m: bit q of X/Y/Z set when the
 // x/y/z edge owned by point i = 32m + q is a sign-change edge.
 __device__ __forceinline__ void crossing_masks(const Grid& g, const uint32_t* bits, int j, int k,
@@ -93,33 +74,6 @@ __device__ __forceinline__ void crossing_masks(const Grid& g, const uint32_t* bi
 
 // ---------------------------------------------------------------------------
 // K2: counts per row word, then the scan.
-
-// The eight corner words of word m of row r (a, a+x of rows (j..j+1,
-// k..k+1)) and the masks that decide which of them are meaningful.
-struct WordBits {
-  CornerWords w;
-  uint32_t pmask, xmask;
-  bool hy, hz;
-};
-
-__device__ __forceinline__ WordBits load_word_bits(const Grid& g, const uint32_t* bits, unsigned r,
-                                                   int m) {
-  WordBits wb;
-  int j, k;
-  split_row(g, r, j, k);
-  wb.hy = j < g.ny - 1;
-  wb.hz = k < g.nz - 1;
-  const long long dy = g.nx, dz = (long long)g.nx * g.ny;
-  const long long pos = (long long)r * g.nx + 32ll * m;
-  wb.pmask = low_mask(g.nx - 32 * m);
-  wb.xmask = low_mask(g.nx - 1 - 32 * m);
-  wb.w = CornerWords{};
-  bits_at2(bits, pos, wb.w.a, wb.w.a1);
-  if (wb.hy) bits_at2(bits, pos + dy, wb.w.b, wb.w.b1);
-  if (wb.hz) bits_at2(bits, pos + dz, wb.w.c, wb.w.c1);
-  if (wb.hy && wb.hz) bits_at2(bits, pos + dy + dz, wb.w.d, wb.w.d1);
-  return wb;
-}
 
 // Slot, point row and word index of global row word gw; keys: the slots'
 // first row words staged in shared memory, or null; from >= 0: a slot that
@@ -142,19 +96,6 @@ __device__ __forceinline__ int nth_bit(uint32_t u, int n) {
   for (int step = 16; step > 0; step >>= 1)
     if (__popc(u & ((1u << (p + step)) - 1u)) <= n) p += step;
   return p;
-}
-
-// Counts of one word from its eight corner words.
-__device__ __forceinline__ uint32_t packed_counts(const CornerWords& w, bool hy, bool hz,
-                                                  uint32_t pmask, uint32_t xmask,
-                                                  const unsigned char* nf) {
-  int v = __popc((w.a ^ w.a1) & xmask);
-  if (hy) v += __popc((w.a ^ w.b) & pmask);
-  if (hz) v += __popc((w.a ^ w.c) & pmask);
-  int t = 0;
-  if (hy && hz)
-    for (uint32_t u = active_cells(w, xmask); u; u &= u - 1) t += nf[case_of(w, __ffs(u) - 1)];
-  return ((uint32_t)t << 16) | (uint32_t)v;
 }
 
 constexpr int kCountWords = 4;  // consecutive row words per count group
@@ -288,7 +229,8 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
                                                    uint32_t* __restrict__ wv,
                                                    uint32_t* __restrict__ act,
                                                    Info* __restrict__ info, int tile_begin,
-                                                   SlabBounds B, uint32_t* __restrict__ slab_act) {
+                                                   SlabBounds B, uint32_t* __restrict__ slab_act,
+                                                   const uint32_t* __restrict__ abort) {
   __shared__ uint32_t s_red[24];
   __shared__ unsigned long long s_pre[3 * 8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -408,7 +350,9 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
     if (PIPE) {
       slab_act[B.n] = (uint32_t)(ea + ta);
     } else {
-      info->error = (T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0;
+      info->error = ((T > 2147483647ll || V > 2147483647ll) ? kErrOverflow : 0) |
+                    ((abort && *(volatile const uint32_t*)abort) ? kErrTimeout : 0) |
+                    (*(volatile int*)&info->aborted ? kErrTimeout : 0);
       info->ticket = 0;
       info->done = 0;
     }
@@ -420,10 +364,11 @@ int word_scan_tiles(long long rowwords) {
 }
 
 void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* tile_tot,
-                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s) {
+                      uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s,
+                      const uint32_t* abort) {
   const int tiles = word_scan_tiles(rowwords);
   k_word_scan<false><<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info, 0,
-                                           SlabBounds{}, nullptr);
+                                           SlabBounds{}, nullptr, abort);
 }
 
 // K2a for grid sets: the same counts, with the triangles of the active
@@ -574,7 +519,9 @@ void launch_mc_scan(const GridSet& S, const uint32_t* bits, const WordOffsets& o
                     int num_sms, cudaStream_t s, int dealt) {
   const int tiles = word_scan_tiles(S.rowwords);
   // the dealt pass reads the device slot table, which only grid sets have
-  if (S.count > 1 && dealt != 0) {
+  if (S.count == 1 && launch_mc_count_staged(S.one.g, bits, bit_words(S.one.g.P), o, info, num_sms, s)) {
+    // one grid: each tile's bits staged in shared memory
+  } else if (S.count > 1 && dealt != 0) {
     const int b1 = resident_blocks(k_mc_count_dealt, 256, 0, num_sms, tiles, kPassCount);
     k_mc_count_dealt<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles);
   } else {
@@ -595,7 +542,7 @@ void launch_mc_scan_slab(const GridSet& S, const uint32_t* bits, const WordOffse
   k_mc_count<<<b1, 256, 0, s>>>(S, bits, o.wc, o.tile, tiles, tile_begin, tile_end);
   if (after_count) cudaEventRecord(after_count, s);
   k_word_scan<true><<<n, 256, 0, s>>>(S.rowwords, o.wc, o.tile, tiles, o.wt, o.wv, o.act, info,
-                                      tile_begin, B, slab_act);
+                                      tile_begin, B, slab_act, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -644,7 +591,7 @@ __device__ __forceinline__ bool emit_guard(Info* info, long long tcap, long long
   const long long T = info->total_a;
   const long long V = merge ? info->total_b : 3 * T;
   A = info->total_c;
-  if (T > tcap || V > vcap || (info->error & kErrOverflow)) {
+  if (T > tcap || V > vcap || (info->error & (kErrOverflow | kErrTimeout))) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
       atomicOr(&info->error, kErrCapacity);
     return false;
@@ -848,7 +795,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
   } else {
     const long long T = word_t(o, range_end);
     const long long V = MERGE ? word_v(o, range_end) : 3 * T;
-    if (T > tcap || V > vcap || (info->error & kErrOverflow)) {
+    if (T > tcap || V > vcap || (info->error & (kErrOverflow | kErrTimeout))) {
       if (blockIdx.x == 0 && threadIdx.x == 0 && (T > tcap || V > vcap))
         atomicOr(&info->error, kErrCapacity);
       return;

@@ -152,12 +152,30 @@ int pipe_streams(PipeStreams** out) {
 int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, bool merge,
                        uint32_t* bits, long long nwords, const WordOffsets& o, Info* info,
                        uint32_t* slab_act, float* verts, long long vcap, int32_t* conn,
-                       long long tcap, int32_t* ra, int32_t* rb, float* rw, int num_sms,
-                       cudaStream_t s) {
+                       long long tcap, int32_t* ra, int32_t* rb, float* rw, uint32_t* fctl,
+                       int num_sms, cudaStream_t s) {
   PipeStreams* ps = nullptr;
   int st = pipe_streams(&ps);
   if (st) return st;
   const SlabPlan p = plan_slabs(g, g_pipe_slabs);
+  if (p.S == 1 && fctl) {
+    // one slab: the fused count pass (classification and counts in one
+    // launch, then the scan) and the emit, on the caller's stream
+    std::lock_guard<std::mutex> lock(ps->mutex);
+    const bool tl = ps->timeline;
+    ps->timeline_slabs = tl ? 1 : 0;
+    if (tl) cudaEventRecord(ps->t0, s);
+    const int e = launch_fused_count(0, g, f, iso, 0.0f, bits, nwords, o, info, nullptr, nullptr,
+                                     fctl, num_sms, s);
+    if (e != 0) return pipe_fail(static_cast<cudaError_t>(e), "fused count pass");
+    if (tl)
+      for (int j = 0; j < 5; ++j) cudaEventRecord(ps->tl[0][j], s);
+    launch_mc_emit(single_set(g, f, iso, 0.0f), merge, bits, o, info, verts, vcap, conn, tcap, ra,
+                   rb, rw, num_sms, s);
+    if (tl) cudaEventRecord(ps->tl[0][5], s);
+    const cudaError_t le = cudaGetLastError();
+    return le == cudaSuccess ? DAX_GB300_SUCCESS : pipe_fail(le, "pipelined marching cubes");
+  }
   PipeOptions opt = g_pipe_opts;
   // one slab: nothing to overlap, so the passes take the whole device, as in
   // the two-call path

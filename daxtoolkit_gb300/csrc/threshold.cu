@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
                                                   float* __restrict__ coords,
                                                   float* __restrict__ fout, long long ucap) {
   const long long K = info->total_a, U = info->total_b, A = info->total_c;
-  if (K > kcap || U > ucap || (info->error & kErrOverflow)) {
+  if (K > kcap || U > ucap || (info->error & (kErrOverflow | kErrTimeout))) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && (K > kcap || U > ucap))
       atomicOr(&info->error, kErrCapacity);
     return;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(256) k_thr_compact_field(Grid g, const uint32_
                                                            const float* __restrict__ in, int comps,
                                                            float* __restrict__ out, long long cap) {
   const long long U = info->total_b;
-  if (U > cap || (info->error & kErrOverflow)) {
+  if (U > cap || (info->error & (kErrOverflow | kErrTimeout))) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && U > cap) atomicOr(&info->error, kErrCapacity);
     return;
   }

@@ -43,8 +43,9 @@ typedef enum dax_gb300_status {
   DAX_GB300_ERROR_CUDA = 4,
   /* an output buffer is smaller than the result; nothing was written */
   DAX_GB300_ERROR_CAPACITY = 5,
-  /* reserved for a bounded device-side wait that gave up; no entry point of
-     this version waits on the device, so none returns it */
+  /* a bounded device-side wait gave up (the fused count pass's blocks wait
+     on one another; the staged count waits for its bulk copies); the count
+     pass has no result and the generate pass writes nothing */
   DAX_GB300_ERROR_TIMEOUT = 6,
   /* grid shape outside what the kernels support (see each call) */
   DAX_GB300_ERROR_UNSUPPORTED = 7
@@ -65,10 +66,22 @@ int dax_gb300_abi_version(void);
 /* Per-SM block limit of one marching-cubes pass for later launches in this
  * process: pass 0 = classification (K1), 1 = count (K2a), 2 = generate (K3);
  * inside dax_gb300_mc_pipeline 3 = classification (default 3), 4 = count
- * (default: no limit), 5 = generate (default 1);
+ * (default: no limit), 5 = generate (default 1); 6 = the fused count pass;
  * blocks = 0 restores "as many as fit".  A limit leaves room on every SM for
  * the passes of other frames, or other slabs, running on other streams. */
 int dax_gb300_set_blocks_per_sm(int pass, int blocks);
+
+/* The count passes of one grid (dax_gb300_mc_count, dax_gb300_threshold_count,
+ * dax_gb300_mc_pipeline's one-slab frame) on a 16-byte aligned device field,
+ * with enabled = 1, run the classification (the field streamed into shared
+ * memory by bulk TMA copies) and the counts of the row words behind it as ONE
+ * persistent launch, then the scan; 0 (the default: separate classify, count
+ * and scan launches, which measure faster at 512^3); -1 leaves it.
+ * unit_stages = 16 KB field stages per classification work item, rounded
+ * down to a power of 2 (default 16; <= 0 leaves it).  Both forms give the
+ * same bytes.  Process-wide tuning knob. */
+int dax_gb300_set_fused_count(int enabled, int unit_stages);
+int dax_gb300_get_fused_count(int* enabled, int* unit_stages);
 
 /* Slabs dax_gb300_mc_pipeline cuts a grid into (1..16; 0 restores the
  * default, 1: no overlap, the passes take the whole device).  Fewer are used
