@@ -176,14 +176,28 @@ int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, b
     const cudaError_t le = cudaGetLastError();
     return le == cudaSuccess ? DAX_GB300_SUCCESS : pipe_fail(le, "pipelined marching cubes");
   }
-  PipeOptions opt = g_pipe_opts;
-  // one slab: nothing to overlap, so the passes take the whole device, as in
-  // the two-call path
-  const bool one = p.S == 1;
-  if (one) {
-    opt.emit_batch = kEmitBatch;
-    opt.keep_field = false;
+  if (p.S == 1) {
+    // one slab: nothing to overlap, so the two-call passes run on the
+    // caller's stream (no hops to the pipeline's streams): classification
+    // (clearing Info), count and scan, emit
+    std::lock_guard<std::mutex> lock(ps->mutex);
+    const bool tl = ps->timeline;
+    ps->timeline_slabs = tl ? 1 : 0;
+    if (tl) cudaEventRecord(ps->t0, s);
+    const GridSet S1 = single_set(g, f, iso, 0.0f);
+    launch_classify_range(0, S1, aligned, bits, nwords, 0, S1.chunks, info, kPassClassify, false,
+                          num_sms, s);
+    if (tl) cudaEventRecord(ps->tl[0][0], s);
+    if (tl) cudaEventRecord(ps->tl[0][1], s);
+    launch_mc_scan(S1, bits, o, info, num_sms, s);
+    if (tl)
+      for (int j = 2; j < 5; ++j) cudaEventRecord(ps->tl[0][j], s);
+    launch_mc_emit(S1, merge, bits, o, info, verts, vcap, conn, tcap, ra, rb, rw, num_sms, s);
+    if (tl) cudaEventRecord(ps->tl[0][5], s);
+    const cudaError_t le = cudaGetLastError();
+    return le == cudaSuccess ? DAX_GB300_SUCCESS : pipe_fail(le, "pipelined marching cubes");
   }
+  const PipeOptions opt = g_pipe_opts;
   const int ne = opt.emit_streams;
   const GridSet S = single_set(g, f, iso, 0.0f);
   SlabBounds B{};
@@ -204,14 +218,14 @@ int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, b
   for (int i = 0; i < ne && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(ps->c[i], ps->start, 0);
   for (int k = 0; k < p.S && e == cudaSuccess; ++k) {
     launch_classify_range(0, S, aligned, bits, nwords, p.K[k], p.K[k + 1], k == 0 ? info : nullptr,
-                          one ? kPassClassify : kPassPipeClassify, opt.keep_field, num_sms, s);
+                          kPassPipeClassify, opt.keep_field, num_sms, s);
     mark(k, 0, s);
     e = cudaEventRecord(ps->kdone[k], s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ps->b, ps->kdone[k], 0);
     if (e != cudaSuccess) break;
     mark(k, 1, ps->b);
     launch_mc_scan_slab(S, bits, o, info, p.tile[k], p.tile[k + 1], B, slab_act,
-                        one ? kPassCount : kPassPipeCount, num_sms, ps->b,
+                        kPassPipeCount, num_sms, ps->b,
                         tl ? ps->tl[k][2] : nullptr);
     mark(k, 3, ps->b);
     cudaStream_t c = ps->c[k % ne];
@@ -221,7 +235,7 @@ int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, b
     mark(k, 4, c);
     launch_mc_emit_range(S, merge, bits, o, info, verts, vcap, conn, tcap, ra, rb, rw, p.E[k],
                          p.E[k + 1], p.E[k + 1], slab_act + k, ctr + 2 * k, ctr + 2 * k + 1,
-                         opt.emit_batch, one ? kPassEmit : kPassPipeEmit, num_sms, c);
+                         opt.emit_batch, kPassPipeEmit, num_sms, c);
     mark(k, 5, c);
   }
   // join the streams back into the caller's, also after a failed enqueue
