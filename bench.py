@@ -62,6 +62,9 @@ def parse_args():
                         "flight, leaving room for the other frames' passes (0 = no limit)")
     p.add_argument("--slabs", type=int, default=0,
                    help="slabs of the pipelined frame (1..16; 0 = the library default)")
+    p.add_argument("--fused", action="store_true",
+                   help="run the count pass as the fused classify + count launch "
+                        "(dax_gb300_set_fused_count) instead of separate passes")
     p.add_argument("--no-graph", action="store_true",
                    help="time direct pipelined calls instead of a CUDA-graph replay of one")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -918,6 +921,7 @@ def main():
     # and replayed (the same kernels, without the host enqueue cost of the
     # slab launches); --no-graph times the direct calls.
     capi.call("dax_gb300_set_pipeline_slabs", args.slabs)
+    capi.call("dax_gb300_set_fused_count", 1 if args.fused else 0, 0)
     plan = (ctypes.c_int64 * 52)()
     capi.call("dax_gb300_mc_pipeline_plan", ctypes.byref(g), 0, plan)
     slab_count = int(plan[0])
@@ -1160,6 +1164,8 @@ def main():
         "data": "synthetic",
         "config": dict(config_dict(n), frames_in_flight=1, slabs=slab_count,
                        call="dax_gb300_mc_pipeline (count + merged generate, slab-pipelined)",
+                       count_pass="fused classify + count launch, then the scan" if args.fused
+                       else "classification, staged count and scan launches",
                        replay="CUDA graph of the frame's call, captured once" if graph is not None
                        else "direct call per frame"),
         "frames": {"pipelined_direct_calls_ms": ms_direct,
@@ -1185,8 +1191,9 @@ def main():
                 "steps": e2e_steps, "steps_in_flight": E,
                 "path": "C ABI; per step the field is copied from page-locked host memory to the "
                         "device and the surface back to page-locked host memory"},
-        # K1, K2a, K2b and K3 per slab, per step
-        "gpu_launches": 4 * slab_count * args.steps,
+        # per step: K1, K2a, K2b and K3 per slab, or (fused, one slab) the
+        # fused classify + count, the scan and K3
+        "gpu_launches": (3 if args.fused and slab_count == 1 else 4 * slab_count) * args.steps,
         "clocks": clocks,
     }
     if not args.no_extras:
