@@ -485,8 +485,8 @@ int dax_gb300_mc_pipeline(const dax_gb300_uniform_grid* grid, const float* d_fie
                                    L.offsets(d_scratch), at<Info>(d_scratch, L.info),
                                    at<uint32_t>(d_scratch, L.slab), d_verts, vert_capacity, d_conn,
                                    tri_capacity, d_rec_first, d_rec_second, d_rec_weight,
-                                   fused_ok(d_field) ? at<uint32_t>(d_scratch, L.fctl) : nullptr,
-                                   num_sms(), s);
+                                   at<uint32_t>(d_scratch, L.fctl), fused_ok(d_field), num_sms(),
+                                   s);
 }
 
 int dax_gb300_mc_pipeline_plan(const dax_gb300_uniform_grid* grid, int slabs, int64_t* out) {

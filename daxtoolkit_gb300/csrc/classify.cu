@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(256) k_classify_bits(GridSet S, uint32_t* __re
   __shared__ long long s_keys[kStagedSlots];
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.chunk0; }) ? s_keys : nullptr;
+  pdl_trigger();  // the count pass may launch into the SMs this grid frees
   if (init && blockIdx.x == 0 && threadIdx.x == 0) {
     init->error = 0;
     init->aborted = 0;

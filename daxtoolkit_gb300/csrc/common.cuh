@@ -306,6 +306,17 @@ __device__ __forceinline__ void row_windows4(const uint32_t* __restrict__ bits, 
 }
 
 // Mask of the low n bits (n in [0, 32]).
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization (launch_pdl) may start while the kernel before it on the
+// stream drains.  pdl_wait() blocks until that kernel has completed and its
+// writes are visible (a no-op after an ordinary launch); pdl_trigger() lets
+// the next kernel launch once every block of this one has issued it or
+// exited.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t low_mask(int n) {
   return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
 }

@@ -38,7 +38,7 @@ inline GridSet single_set(const Grid& g, const float* field, float a, float b) {
 void launch_classify_bits(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
                           long long nwords, int num_sms, cudaStream_t s);
 // One grid's chunks [c_begin, c_end) only; init != NULL clears that Info
-// block's error word and emit counters first; `pass` selects the per-SM
+// block's error words and emit counters first; `pass` selects the per-SM
 // limit; keep (mode 0) reads the field with the default cache policy
 // instead of evict-first.
 void launch_classify_range(int mode, const GridSet& S, bool all_aligned, uint32_t* bits,
@@ -72,6 +72,24 @@ int tuned_blocks_per_sm(int pass);
 // costs microseconds of host time, which the many launches of a pipelined
 // call would otherwise pay each time.
 int cached_occupancy(const void* kernel, int threads, size_t smem);
+
+// Launches `kernel` with programmatic stream serialization: it may begin
+// (its blocks run up to pdl_wait) while the previous kernel on `s` finishes.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                              cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 template <typename K>
 inline int resident_blocks(K kernel, int threads, size_t smem, int num_sms, long long want,
@@ -203,15 +221,15 @@ void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, co
                           int32_t* ra, int32_t* rb, float* rw, long long word_begin,
                           long long word_end, long long range_end, const uint32_t* slab_act,
                           unsigned* ticket, unsigned* done, int batch, int pass, int num_sms,
-                          cudaStream_t s);
+                          cudaStream_t s, bool pdl = false);
 // The whole count + generate of one grid, slab-pipelined (pipeline.cu).
-// fctl: non-null runs a one-slab frame as the fused count pass (fctl: its
-// control words) and the emit, on the caller's stream.
+// fused: a one-slab frame runs the fused count pass (fctl: its control
+// words) and the emit, on the caller's stream.
 int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, bool merge,
                        uint32_t* bits, long long nwords, const WordOffsets& o, Info* info,
                        uint32_t* slab_act, float* verts, long long vcap, int32_t* conn,
                        long long tcap, int32_t* ra, int32_t* rb, float* rw, uint32_t* fctl,
-                       int num_sms, cudaStream_t s);
+                       bool fused, int num_sms, cudaStream_t s);
 // goff[2g], goff[2g+1]: first triangle / merged vertex of grid g; then totals.
 void launch_grid_offsets(const GridSet& S, const WordOffsets& o, long long* goff,
                          cudaStream_t s);

@@ -115,6 +115,8 @@ __global__ void __launch_bounds__(256) k_mc_count(GridSet S, const uint32_t* __r
   s_nf[threadIdx.x] = (unsigned char)mc_num_tris(threadIdx.x);
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
+  pdl_trigger();
+  pdl_wait();  // the classification's bits
   for (int tile = tile_begin + blockIdx.x; tile < tile_end; tile += gridDim.x) {
     uint32_t st = 0, sv = 0, sa = 0;
 #pragma unroll 1
@@ -235,6 +237,8 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
   __shared__ unsigned long long s_pre[3 * 8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tile = tile_begin + blockIdx.x;
+  pdl_trigger();
+  pdl_wait();  // the count pass's per-word counts and tile totals
   // exclusive prefix over the tiles before this one (64-bit: totals may pass 2^32)
   unsigned long long pt = 0, pv = 0, pa = 0;
   for (int x = tid; x < tile; x += 256) {
@@ -367,8 +371,8 @@ void launch_word_scan(long long rowwords, const uint32_t* wc, const uint32_t* ti
                       uint32_t* wt, uint32_t* wv, uint32_t* act, Info* info, cudaStream_t s,
                       const uint32_t* abort) {
   const int tiles = word_scan_tiles(rowwords);
-  k_word_scan<false><<<tiles, 256, 0, s>>>(rowwords, wc, tile_tot, tiles, wt, wv, act, info, 0,
-                                           SlabBounds{}, nullptr, abort);
+  launch_pdl(k_word_scan<false>, (unsigned)tiles, 256u, 0, s, rowwords, wc, tile_tot, tiles, wt, wv,
+             act, info, 0, SlabBounds{}, (uint32_t*)nullptr, abort);
 }
 
 // K2a for grid sets: the same counts, with the triangles of the active
@@ -789,6 +793,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 4) k_mc_emit(GridSet S,
   if (threadIdx.x < 12) s_edge[threadIdx.x] = kEdgeOwner[threadIdx.x];
   const long long* keys =
       stage_slot_keys(S, s_keys, [](const GridSlot& sl) { return sl.rw0; }) ? s_keys : nullptr;
+  pdl_wait();  // the scan's offsets and totals
   long long A0 = 0, A;
   if (range_end < 0) {
     if (!emit_guard(info, tcap, vcap, MERGE, A)) return;
@@ -989,7 +994,7 @@ void launch_mc_emit(const GridSet& S, bool merge, const uint32_t* bits, const Wo
                     int32_t* ra, int32_t* rb, float* rw, int num_sms, cudaStream_t s) {
   launch_mc_emit_range(S, merge, bits, o, info, verts, vcap, conn, tcap, ra, rb, rw, 0,
                        S.rowwords, -1, nullptr, &info->ticket, &info->done, kEmitBatch,
-                       kPassEmit, num_sms, s);
+                       kPassEmit, num_sms, s, true);
 }
 
 void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, const WordOffsets& o,
@@ -997,21 +1002,23 @@ void launch_mc_emit_range(const GridSet& S, bool merge, const uint32_t* bits, co
                           int32_t* ra, int32_t* rb, float* rw, long long word_begin,
                           long long word_end, long long range_end, const uint32_t* slab_act,
                           unsigned* ticket, unsigned* done, int batch, int pass, int num_sms,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool pdl) {
   // the active count lives on the device: one resident wave, warp-stride
   const long long words = word_end - word_begin;
   const long long want = (words + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
-  if (merge) {
-    const int b = resident_blocks(k_mc_emit<true>, kEmitWarps * 32, 0, num_sms, want, pass);
-    k_mc_emit<true><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
-                                                  rb, rw, range_end, slab_act, ticket, done,
-                                                  batch);
-  } else {
-    const int b = resident_blocks(k_mc_emit<false>, kEmitWarps * 32, 0, num_sms, want, pass);
-    k_mc_emit<false><<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra,
-                                                   rb, rw, range_end, slab_act, ticket, done,
-                                                  batch);
-  }
+  auto go = [&](auto kernel) {
+    const int b = resident_blocks(kernel, kEmitWarps * 32, 0, num_sms, want, pass);
+    if (pdl)
+      launch_pdl(kernel, (unsigned)b, (unsigned)(kEmitWarps * 32), 0, s, S, bits, o, info, verts,
+                 vcap, conn, tcap, ra, rb, rw, range_end, slab_act, ticket, done, batch);
+    else
+      kernel<<<b, kEmitWarps * 32, 0, s>>>(S, bits, o, info, verts, vcap, conn, tcap, ra, rb, rw,
+                                           range_end, slab_act, ticket, done, batch);
+  };
+  if (merge)
+    go(k_mc_emit<true>);
+  else
+    go(k_mc_emit<false>);
 }
 
 // Per-grid offsets: goff[2g], goff[2g+1] = first triangle / merged vertex of

@@ -153,12 +153,12 @@ int launch_mc_pipeline(const Grid& g, const float* f, bool aligned, float iso, b
                        uint32_t* bits, long long nwords, const WordOffsets& o, Info* info,
                        uint32_t* slab_act, float* verts, long long vcap, int32_t* conn,
                        long long tcap, int32_t* ra, int32_t* rb, float* rw, uint32_t* fctl,
-                       int num_sms, cudaStream_t s) {
+                       bool fused, int num_sms, cudaStream_t s) {
   PipeStreams* ps = nullptr;
   int st = pipe_streams(&ps);
   if (st) return st;
   const SlabPlan p = plan_slabs(g, g_pipe_slabs);
-  if (p.S == 1 && fctl) {
+  if (p.S == 1 && fused) {
     // one slab: the fused count pass (classification and counts in one
     // launch, then the scan) and the emit, on the caller's stream
     std::lock_guard<std::mutex> lock(ps->mutex);

@@ -116,6 +116,67 @@ __device__ bool stage_tile(const uint32_t* bits, const Ranges& R, uint32_t* s, i
   return ok;
 }
 
+// Packed counts (triangles << 16 | crossing edges) of row words g0..g0+3
+// (0 past W) from the staged ranges: sa holds rows r_lo .. r_hi + 1, its
+// first word at global bit ba; sb the same rows one plane up, its first word
+// at global bit bb + dz (so a row's own position minus bb indexes its
+// plane-up row).
+__device__ __forceinline__ void staged_counts4(const Grid& g, long long W, long long g0,
+                                               const uint32_t* sa, const uint32_t* sb,
+                                               long long ba, long long bb,
+                                               const unsigned char* s_nf, uint32_t (&out)[4]) {
+  const long long dy = g.nx;
+  out[0] = out[1] = out[2] = out[3] = 0u;
+  int m;
+  const unsigned r = split_word(g, (unsigned)g0, m);
+  if (m + 4 <= g.wr && g0 + 4 <= W) {
+    int j, k;
+    split_row(g, r, j, k);
+    const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
+    const long long pos = (long long)r * g.nx + 32ll * m;
+    uint32_t a[4], a1[4], b[4] = {0, 0, 0, 0}, b1[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0},
+             c1[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0}, d1[4] = {0, 0, 0, 0};
+    s_windows4(sa, pos - ba, a, a1);
+    if (hy) s_windows4(sa, pos + dy - ba, b, b1);
+    if (hz) s_windows4(sb, pos - bb, c, c1);
+    if (hy && hz) s_windows4(sb, pos + dy - bb, d, d1);
+    uint32_t diff = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      diff |= a[q] ^ a1[q];
+      if (hy) diff |= (a[q] ^ b[q]) | (a[q] ^ b1[q]);
+      if (hz) diff |= (a[q] ^ c[q]) | (a[q] ^ c1[q]);
+      if (hy && hz) diff |= (a[q] ^ d[q]) | (a[q] ^ d1[q]);
+    }
+    if (diff) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const CornerWords w{a[q], a1[q], b[q], b1[q], c[q], c1[q], d[q], d1[q]};
+        out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + q)),
+                               low_mask(g.nx - 1 - 32 * (m + q)), s_nf);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long gw = g0 + q;
+      if (gw >= W) break;
+      int mq, jq, kq;
+      const unsigned rq = split_word(g, (unsigned)gw, mq);
+      split_row(g, rq, jq, kq);
+      const bool hy = jq < g.ny - 1, hz = kq < g.nz - 1;
+      const long long pos = (long long)rq * g.nx + 32ll * mq;
+      CornerWords w{};
+      s_bits2(sa, pos - ba, w.a, w.a1);
+      if (hy) s_bits2(sa, pos + dy - ba, w.b, w.b1);
+      if (hz) s_bits2(sb, pos - bb, w.c, w.c1);
+      if (hy && hz) s_bits2(sb, pos + dy - bb, w.d, w.d1);
+      out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * mq), low_mask(g.nx - 1 - 32 * mq),
+                             s_nf);
+    }
+  }
+}
+
 // Marching cubes, one grid: packed counts (triangles << 16 | crossing
 // edges) of every row word and the per-tile totals, as k_mc_count writes
 // them.  Range 0 holds rows r_lo .. r_hi + 1, range 1 the same rows one
@@ -134,6 +195,8 @@ __global__ void __launch_bounds__(256) k_mc_count_staged(Grid g, const uint32_t*
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  pdl_trigger();
+  pdl_wait();  // the classification's bits
   unsigned long long policy;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(policy));
   unsigned phase = 0;
@@ -153,55 +216,8 @@ __global__ void __launch_bounds__(256) k_mc_count_staged(Grid g, const uint32_t*
     for (int e = 0; e < kScanItems / 4; ++e) {
       const long long g0 = (long long)tile * kScanTile + 4ll * (threadIdx.x + 256 * e);
       if (g0 >= W) break;
-      int m;
-      const unsigned r = split_word(g, (unsigned)g0, m);
-      uint32_t out[4] = {0u, 0u, 0u, 0u};
-      if (m + 4 <= g.wr && g0 + 4 <= W) {
-        int j, k;
-        split_row(g, r, j, k);
-        const bool hy = j < g.ny - 1, hz = k < g.nz - 1;
-        const long long pos = (long long)r * g.nx + 32ll * m;
-        uint32_t a[4], a1[4], b[4] = {0, 0, 0, 0}, b1[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0},
-                 c1[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0}, d1[4] = {0, 0, 0, 0};
-        s_windows4(sa, pos - ba, a, a1);
-        if (hy) s_windows4(sa, pos + dy - ba, b, b1);
-        if (hz) s_windows4(sb, pos - bb, c, c1);
-        if (hy && hz) s_windows4(sb, pos + dy - bb, d, d1);
-        uint32_t diff = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          diff |= a[q] ^ a1[q];
-          if (hy) diff |= (a[q] ^ b[q]) | (a[q] ^ b1[q]);
-          if (hz) diff |= (a[q] ^ c[q]) | (a[q] ^ c1[q]);
-          if (hy && hz) diff |= (a[q] ^ d[q]) | (a[q] ^ d1[q]);
-        }
-        if (diff) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const CornerWords w{a[q], a1[q], b[q], b1[q], c[q], c1[q], d[q], d1[q]};
-            out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * (m + q)),
-                                   low_mask(g.nx - 1 - 32 * (m + q)), s_nf);
-          }
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const long long gw = g0 + q;
-          if (gw >= W) break;
-          int mq, jq, kq;
-          const unsigned rq = split_word(g, (unsigned)gw, mq);
-          split_row(g, rq, jq, kq);
-          const bool hy = jq < g.ny - 1, hz = kq < g.nz - 1;
-          const long long pos = (long long)rq * g.nx + 32ll * mq;
-          CornerWords w{};
-          s_bits2(sa, pos - ba, w.a, w.a1);
-          if (hy) s_bits2(sa, pos + dy - ba, w.b, w.b1);
-          if (hz) s_bits2(sb, pos - bb, w.c, w.c1);
-          if (hy && hz) s_bits2(sb, pos + dy - bb, w.d, w.d1);
-          out[q] = packed_counts(w, hy, hz, low_mask(g.nx - 32 * mq), low_mask(g.nx - 1 - 32 * mq),
-                                 s_nf);
-        }
-      }
+      uint32_t out[4];
+      staged_counts4(g, W, g0, sa, sb, ba, bb, s_nf, out);
       if (g0 + 4 <= W) {
         *reinterpret_cast<uint4*>(wc + g0) = make_uint4(out[0], out[1], out[2], out[3]);
       } else {
@@ -224,6 +240,7 @@ __global__ void __launch_bounds__(256) k_mc_count_staged(Grid g, const uint32_t*
     }
   }
 }
+
 
 // Words a staged range can need: the tile's rows (at most kScanTile / wr + 2
 // of them) plus the two rows after, the margins and the alignment.
@@ -261,8 +278,11 @@ bool launch_mc_count_staged(const Grid& g, const uint32_t* bits, long long nword
   if (!opt_in(k_mc_count_staged, smem)) return false;
   const int tiles = word_scan_tiles(g.R * g.wr);
   const int blocks = resident_blocks(k_mc_count_staged, 256, smem, num_sms, tiles, kPassCount);
-  k_mc_count_staged<<<blocks, 256, smem, s>>>(g, bits, nwords, o.wc, o.tile, tiles, rw, info);
+  // a failed launch is reported by the caller's launch check
+  (void)launch_pdl(k_mc_count_staged, blocks, 256, smem, s, g, bits, nwords, o.wc, o.tile, tiles, rw,
+                   info);
   return true;
 }
+
 
 }  // namespace daxgb
