@@ -54,6 +54,8 @@ __device__ __forceinline__ uint32_t kept_word(const Grid& g, const uint32_t* __r
 // corner row.
 __global__ void __launch_bounds__(256) k_thr_kept(Grid g, const uint32_t* __restrict__ bits,
                                                   uint32_t* __restrict__ kept) {
+  pdl_trigger();
+  pdl_wait();  // the classification's bits
   const long long W = g.R * g.wr;  // < 2^27 for grids below 2^31 points
   const long long groups = (W + 3) / 4;
   const long long dy = g.nx, dz = (long long)g.nx * g.ny;
@@ -119,6 +121,8 @@ __global__ void __launch_bounds__(256) k_thr_used(Grid g, const uint32_t* __rest
                                                   uint32_t* __restrict__ wc,
                                                   uint32_t* __restrict__ tile_tot, int tiles) {
   __shared__ uint32_t s_red[24];
+  pdl_trigger();
+  pdl_wait();  // the kept masks
   const long long W = g.R * g.wr;
   const uint32_t wy = (uint32_t)g.wr, wz = (uint32_t)g.wr * (uint32_t)g.ny;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -196,10 +200,10 @@ void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint3
                       uint32_t* wc, uint32_t* tile_tot, int num_sms, cudaStream_t s) {
   const long long W = g.R * g.wr;
   const int b1 = resident_blocks(k_thr_kept, 256, 0, num_sms, (W + 1023) / 1024);
-  k_thr_kept<<<b1, 256, 0, s>>>(g, bits, kept);
+  launch_pdl(k_thr_kept, (unsigned)b1, 256u, 0, s, g, bits, kept);
   const int tiles = word_scan_tiles(W);
   const int b2 = resident_blocks(k_thr_used, 256, 0, num_sms, tiles);
-  k_thr_used<<<b2, 256, 0, s>>>(g, kept, used, wc, tile_tot, tiles);
+  launch_pdl(k_thr_used, (unsigned)b2, 256u, 0, s, g, kept, used, wc, tile_tot, tiles);
 }
 
 // Per active word, what the emit loop needs: its masks and offsets, and for
@@ -383,6 +387,9 @@ void launch_thr_emit(const Grid& g, const float* f, const WordOffsets& o, const 
   // the active count lives on the device: one resident wave, grid-stride
   const long long want = (g.R * g.wr + 255) / 256;
   const int blocks = resident_blocks(k_thr_emit, 256, 0, num_sms, want);
+  // an ordinary launch: the warps split the active words statically, so all
+  // blocks should start together on an idle device (launched early into the
+  // SMs the scan frees, they measured 20 us slower at 512^3)
   k_thr_emit<<<blocks, 256, 0, s>>>(g, f, kept, used, o.wt, o.wv, o.act, info, conn, kcap, coords,
                                     fout, ucap);
 }
