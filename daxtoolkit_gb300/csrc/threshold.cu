@@ -207,12 +207,14 @@ void launch_thr_count(const Grid& g, const uint32_t* bits, uint32_t* kept, uint3
 }
 
 // Per active word, what the emit loop needs: its masks and offsets, and for
-// kept cells the used masks / offsets of the 7 other corner words: rows
-// q = dj + 2 dk (q = 1..3) at word m, and rows q = 0..3 at word m + 1.
+// kept cells the used masks and offsets of corner rows q = dj + 2 dk
+// (q = 1..3) at word m, and the first used-point offsets of rows q = 0..3 at
+// word m + 1 (the +x corner of a cell at bit 31 is that word's first point,
+// always used).
 struct ThrWord {
   uint32_t w, u, kw, v0, t0;
   uint32_t r, m, j, k;  // the word's point row (j, k) and word index in the row
-  uint32_t cu[7], cv[7];
+  uint32_t cu[3], cv[7];
 };
 
 __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restrict__ f,
@@ -266,10 +268,7 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
         }
         if (m + 1 < wr) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            d.cu[3 + q] = __ldg(used + rows[q] + 1);
-            d.cv[3 + q] = __ldg(wv + rows[q] + 1);
-          }
+          for (int q = 0; q < 4; ++q) d.cv[3 + q] = __ldg(wv + rows[q] + 1);
         }
       }
     }
@@ -306,14 +305,13 @@ __global__ void __launch_bounds__(256) k_thr_emit(Grid g, const float* __restric
       }
       if (kw == 0u) continue;  // uniform across the warp
       const uint32_t t0 = __shfl_sync(kFull, d.t0, s);
-      uint32_t cu[8], cv[8];  // corner rows q at word m (0..3) and m + 1 (4..7)
+      uint32_t cu[4], cv[8];  // corner rows q at word m (0..3); cv[4 + q]: at word m + 1
       cu[0] = u;
       cv[0] = v0;
 #pragma unroll
-      for (int e = 0; e < 7; ++e) {
-        cu[e + 1] = __shfl_sync(kFull, d.cu[e], s);
-        cv[e + 1] = __shfl_sync(kFull, d.cv[e], s);
-      }
+      for (int e = 0; e < 3; ++e) cu[e + 1] = __shfl_sync(kFull, d.cu[e], s);
+#pragma unroll
+      for (int e = 0; e < 7; ++e) cv[e + 1] = __shfl_sync(kFull, d.cv[e], s);
       if ((kw >> lane) & 1u) {
         const long long cid = (long long)t0 + __popc(kw & below);
         // used-point ranks of the corners at i (lo) and i + 1 (hi) of corner
