@@ -1086,11 +1086,6 @@ def main():
     pipe_gbs = alg_bytes / (ms_per_step / 1e3) / 1e9
 
     # --- end to end through the public API, host buffers ------------------
-    # The field stays in page-locked host memory and is handed to the API as
-    # is: K1 streams it over the host link (the same bytes a separate H2D
-    # copy would move, in one pass instead of copy-then-read), the emit kernel
-    # reads crossing-edge values from it, and the surface comes back to
-    # page-locked host buffers.
     # End to end through the C ABI from page-locked host memory: every step
     # copies its whole 512^3 field from page-locked host memory to the device,
     # sizes its outputs from the totals, generates and copies the surface back
@@ -1157,6 +1152,18 @@ def main():
         assert torch.equal(q["hv"], verts.cpu()) and torch.equal(q["hc"], conn.cpu())
     e2e_value = world * C / t_e2e
 
+    # The floor e2e is held to: the field's host-to-device copy alone, from the
+    # same page-locked buffer on the same stream, back to back.
+    q = eslots[0]
+
+    def h2d():
+        with torch.cuda.stream(q["stream"]):
+            q["dfield"].copy_(q["host"], non_blocking=True)
+
+    h2d()
+    h2d_ms = _event_ms(h2d, 10, q["stream"])
+    h2d_gbs = 4 * P / (h2d_ms / 1e3) / 1e9
+
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_per_step,
@@ -1189,6 +1196,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 4 * P,
                 "d2h_bytes_per_step": 12 * V + 12 * T, "ms_per_step": 1e3 * t_e2e,
                 "steps": e2e_steps, "steps_in_flight": E,
+                "h2d_field_copy_ms": h2d_ms, "h2d_link_gbs": h2d_gbs,
+                "frac_of_h2d_floor": h2d_ms / (1e3 * t_e2e),
                 "path": "C ABI; per step the field is copied from page-locked host memory to the "
                         "device and the surface back to page-locked host memory"},
         # per step: K1, K2a, K2b and K3 per slab, or (fused, one slab) the

@@ -7,8 +7,12 @@
 // to 16 bytes (a dax::Vector3 is 12).
 //
 // Every primitive works on tiles of kPTile elements (256 threads x 16):
-//   scan     reduce-then-scan: tile sums, one block scanning the sums, then
-//            each tile scanned with its prefix (in place allowed);
+//   scan     integers: one pass, each tile's prefix found by a decoupled
+//            look-back over the tiles before it; floats (and the sort's
+//            histograms): reduce-then-scan, tile sums, one block scanning
+//            the sums, then each tile scanned with its prefix, whose fixed
+//            order of additions gives the same result on every run (in place
+//            allowed for both);
 //   sort     LSD radix sort, 8-bit digits, stable: per pass a per-tile digit
 //            histogram, a scan of the histograms in digit-major order, and a
 //            scatter that ranks each element among equal digits of its tile
@@ -24,6 +28,7 @@
 #include "../../include/dax_gb300.h"
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace daxgb {
 
@@ -231,6 +236,370 @@ void scan_t(const T* in, T* out, long long n, bool exclusive, void* scratch, voi
   scan_sums<A>(sums, tiles, sums + tiles + 1, s);
   k_tile_scan<T><<<b, kPT, 0, s>>>(in, out, n, sums, tiles, exclusive ? 1 : 0);
   if (d_total) cudaMemcpyAsync(d_total, sums + tiles, sizeof(T), cudaMemcpyDeviceToDevice, s);
+}
+
+// ---- single-pass scan of integer elements ---------------------------------
+//
+// One read and one write of every element, by one persistent block an SM.
+// The block takes tiles (64 KB) from a ticket counter and keeps kSStages of
+// them in a ring of shared-memory stages, each filled by one bulk TMA copy.
+// Its eight compute warps reduce a tile as soon as it lands and publish the
+// tile's sum (AGG); a ninth warp then finds the tile's prefix by looking back
+// over the published states of the tiles before it (32 a step, lane = tile)
+// and publishes the inclusive prefix (INC), while the compute warps reduce
+// the next tile; they then scan the tile in shared memory and write it back
+// with one bulk copy, and the stage loads the block's next ticket.
+//
+// Why this shape (measured at 2^30 int32): a plain copy with the same
+// tickets and bulk copies runs at 7.1 TB/s, but a block that waits in its own
+// look-back holds its tile and starves the loads (one tile a block: 0.61 of
+// the copy bandwidth); the look-back step is an L2 round trip and the prefix
+// crosses the ~152 tiles in flight 32 tiles a step, so the look-back runs
+// beside the reductions instead.  Wider steps and smaller tiles polled more
+// and measured slower; a short sleep between polls helped a little.
+//
+// Tiles are taken in ticket order and each block's tickets increase in the
+// order it processes them, so the smallest unfinished tile always has all
+// its predecessors' sums published and its block working on it: no tile
+// waits on a later one.  Every wait is still bounded (Spin), and a wait that
+// runs out marks the scan failed (DAX_GB300_ERROR_TIMEOUT when the total is
+// read).
+//
+// Integer sums wrap, so any split of the look-back gives the same result;
+// float scans keep the deterministic reduce-then-scan above.
+//
+// Shared-memory layout of a tile: warp w owns elements [w, w + 1) * kWarpElems;
+// its lane reads and writes 16-byte chunk c at element c * 32 * E + lane * E
+// of that range (E elements a chunk), so every access of a warp covers 512
+// consecutive bytes and no two lanes share a bank.  The scan goes chunk by
+// chunk: a lane's E elements, a warp scan of the chunk totals, and the carry
+// of the chunks before.  Arrays that are not 16-byte aligned, and the ragged
+// last tile, are loaded and stored element by element instead.
+//
+// Scratch (zeroed before the launch, the states included): ticket, error,
+// total, then per tile its state: flag << 32 | sum in one 64-bit word for
+// 32-bit sums, two such words (low and high halves) for 64-bit sums.
+constexpr unsigned kStAgg = 1u, kStInc = 2u;
+constexpr size_t kScanHead = 64;
+constexpr int kSThreads = 256;                                // compute threads
+constexpr int kSChunks = 16;                                  // 16-byte chunks a thread
+constexpr unsigned kSTileBytes = 16u * kSChunks * kSThreads;  // 64 KB
+constexpr int kSStages = 3;
+
+struct ScanCtl {
+  unsigned ticket, error;
+  unsigned long long total;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <typename A> struct TileStates;
+
+template <> struct TileStates<uint32_t> {
+  unsigned long long* word;
+  __host__ __device__ static size_t bytes(int tiles) { return (size_t)tiles * 8; }
+  __host__ __device__ static size_t clear_bytes(int tiles) { return (size_t)tiles * 8; }
+  __host__ __device__ explicit TileStates(char* base, int) : word((unsigned long long*)base) {}
+  __device__ void publish(int t, unsigned flag, uint32_t v) const {
+    st_relaxed64(word + t, (unsigned long long)flag << 32 | v);
+  }
+  __device__ unsigned read(int t, uint32_t& v) const {
+    const unsigned long long w = ld_relaxed64(word + t);
+    v = (uint32_t)w;
+    return (unsigned)(w >> 32);
+  }
+};
+
+// 64-bit sums: two 64-bit words, each the flag above 32 bits of the sum,
+// stored and loaded as one 16-byte access (each word is single-copy atomic,
+// the pair need not be); words with different flags are a read that caught a
+// publication half done, and count as not yet published.
+template <> struct TileStates<unsigned long long> {
+  unsigned long long* pair;
+  __host__ __device__ static size_t bytes(int tiles) { return (size_t)tiles * 16; }
+  __host__ __device__ static size_t clear_bytes(int tiles) { return (size_t)tiles * 16; }
+  __host__ __device__ explicit TileStates(char* base, int) : pair((unsigned long long*)base) {}
+  __device__ void publish(int t, unsigned flag, unsigned long long v) const {
+    const unsigned long long f = (unsigned long long)flag << 32;
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(pair + 2 * t),
+                 "l"(f | (v & 0xffffffffull)), "l"(f | (v >> 32))
+                 : "memory");
+  }
+  __device__ unsigned read(int t, unsigned long long& v) const {
+    unsigned long long lo, hi;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+                 : "=l"(lo), "=l"(hi)
+                 : "l"(pair + 2 * t)
+                 : "memory");
+    const unsigned f = (unsigned)(lo >> 32);
+    if (f != (unsigned)(hi >> 32)) return 0u;
+    v = (lo & 0xffffffffull) | (hi << 32);
+    return f;
+  }
+};
+
+template <typename A>
+__device__ __forceinline__ A warp_inclusive(A x, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const A y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  return x;
+}
+
+// The exclusive prefix of `tile` from the states of the tiles before it
+// (one warp; every lane returns it).  A step reads the states of tiles
+// top - lane, polls those not yet published (a short sleep between polls),
+// and ends at the nearest inclusive prefix.  Sets `failed` if a wait ran out.
+template <typename A>
+__device__ A look_back(const TileStates<A>& st, int tile, int lane, bool& failed) {
+  A prefix = 0;
+  for (int top = tile - 1; top >= 0; top -= 32) {
+    const int t = top - lane;
+    A x = 0;
+    unsigned f = kStInc;  // before tile 0: an inclusive zero
+    if (t >= 0) {
+      Spin spin;
+      while ((f = st.read(t, x)) == 0u) {
+        if (!spin.more()) {
+          failed = true;
+          f = kStInc;
+          x = 0;
+          break;
+        }
+        __nanosleep(300);
+      }
+    }
+    // the nearest tile with its inclusive prefix ends the look-back
+    const unsigned incl = __ballot_sync(kFull, f == kStInc);
+    const int last = incl ? __ffs(incl) - 1 : 31;
+    A part = lane <= last ? x : (A)0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(kFull, part, d);
+    prefix += part;
+    if (incl) break;
+  }
+  return prefix;
+}
+
+__device__ __forceinline__ void compute_sync() {  // the compute warps only
+  asm volatile("bar.sync 1, %0;" ::"r"(kSThreads) : "memory");
+}
+
+__device__ __forceinline__ bool wait_phase(uint64_t* bar, unsigned parity) {
+  Spin sp;
+  while (!mbar_test(bar, parity))
+    if (!sp.more()) return false;
+  return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSThreads + 32, 1)
+    k_scan_single(const T* __restrict__ in, T* out, long long n, int tiles, ScanCtl* ctl,
+                  char* states, int exclusive, int bulk) {
+  typedef typename Acc<T>::type A;
+  constexpr int E = 16 / (int)sizeof(A);  // elements a chunk
+  constexpr int kTileElems = (int)(kSTileBytes / sizeof(A));
+  constexpr int kWarps = kSThreads / 32;
+  constexpr int kWarpElems = kTileElems / kWarps;
+  struct Chunk { A e[E]; };
+  static_assert(sizeof(Chunk) == 16, "16-byte chunks");
+  const TileStates<A> st(states, tiles);
+  extern __shared__ __align__(128) unsigned char scan_smem[];
+  __shared__ __align__(8) uint64_t b_full[kSStages], b_agg[kSStages], b_pre[kSStages];
+  __shared__ int s_tile[kSStages];  // the stage's occupant
+  __shared__ int s_seen[kSStages];  // the occupant as handed to the look-back warp
+  __shared__ A s_tot[kSStages], s_pre[kSStages], s_wsum[kSStages][kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // a tile is copied in bulk when it is whole and both arrays are 16-byte aligned
+  auto whole = [&](int t) { return bulk && (long long)(t + 1) * kTileElems <= n; };
+  auto stage = [&](int k) { return reinterpret_cast<A*>(scan_smem + (size_t)k * kSTileBytes); };
+  unsigned long long policy = 0;  // read once: evict first
+  auto fill = [&](int k) {        // thread 0: the stage's next tile
+    const int t = (int)atomicAdd(&ctl->ticket, 1u);
+    s_tile[k] = t;
+    if (t < tiles && whole(t)) {
+      mbar_arrive_tx(&b_full[k], kSTileBytes);
+      bulk_load(stage(k), in + (long long)t * kTileElems, kSTileBytes, &b_full[k], policy);
+    }
+  };
+  if (threadIdx.x == 0) {
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+    for (int k = 0; k < kSStages; ++k) {
+      mbar_init(&b_full[k], 1);
+      mbar_init(&b_agg[k], 1);
+      mbar_init(&b_pre[k], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int k = 0; k < kSStages; ++k) fill(k);
+  }
+  __syncthreads();
+
+  if (warp == kWarps) {
+    // the look-back warp: the block's tiles in order
+    for (int i = 0;; ++i) {
+      const int k = i % kSStages;
+      bool failed = !wait_phase(&b_agg[k], (i / kSStages) & 1);
+      const int tile = s_seen[k];
+      if (tile >= tiles) break;
+      const A tot = s_tot[k];
+      const A prefix = look_back(st, tile, lane, failed);
+      failed = __any_sync(kFull, failed);
+      if (lane == 0) {
+        if (tile > 0) st.publish(tile, kStInc, prefix + tot);
+        if (failed) atomicOr(&ctl->error, 1u);
+        if (tile == tiles - 1) ctl->total = (unsigned long long)(prefix + tot);
+        s_pre[k] = prefix;
+        mbar_arrive(&b_pre[k]);
+      }
+      __syncwarp();
+    }
+    return;
+  }
+
+  // compute warps.  reduce(k): the stage's tile lands (bulk) or is loaded
+  // here (elements), is summed, and its sum published and handed on; false
+  // once the tiles are done (the later stages hold later tickets)
+  unsigned fullp = 0;  // bit k: the parity stage k's next bulk copy completes
+  auto reduce = [&](int k) -> bool {
+    const int tile = s_tile[k];
+    if (tile >= tiles) {
+      if (threadIdx.x == 0) {
+        s_seen[k] = tile;
+        mbar_arrive(&b_agg[k]);
+      }
+      return false;
+    }
+    A* s_data = stage(k);
+    bool ok = true;
+    if (whole(tile)) {
+      ok = wait_phase(&b_full[k], (fullp >> k) & 1u);
+      fullp ^= 1u << k;
+    } else {
+      const long long b = (long long)tile * kTileElems;
+      const long long cnt = n - b < kTileElems ? n - b : kTileElems;
+      for (int i = threadIdx.x; i < kTileElems; i += kSThreads)
+        s_data[i] = i < cnt ? (A)in[b + i] : (A)0;
+      compute_sync();
+    }
+    const Chunk* sc = reinterpret_cast<const Chunk*>(s_data + warp * kWarpElems) + lane;
+    A sum = 0;
+#pragma unroll 4
+    for (int c = 0; c < kSChunks; ++c) {
+      const Chunk x = sc[32 * c];
+#pragma unroll
+      for (int e = 0; e < E; ++e) sum += x.e[e];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
+    if (lane == 0) s_wsum[k][warp] = sum;
+    compute_sync();
+    if (threadIdx.x == 0) {
+      A tot = 0;
+      for (int w = 0; w < kWarps; ++w) tot += s_wsum[k][w];
+      st.publish(tile, tile == 0 ? kStInc : kStAgg, tot);
+      if (!ok) {
+        atomicOr(&ctl->error, 1u);
+        // wait (bounded) once more for the copy, so that none lands in
+        // shared memory after the block leaves
+        wait_phase(&b_full[k], (fullp >> k) & 1u ^ 1u);
+      }
+      s_tot[k] = tot;
+      s_seen[k] = tile;
+      mbar_arrive(&b_agg[k]);
+    }
+    return true;
+  };
+
+  bool more = reduce(0);
+  for (int i = 0; more; ++i) {
+    const int k = i % kSStages;
+    const bool next = reduce((i + 1) % kSStages);  // beside this tile's look-back
+    wait_phase(&b_pre[k], (i / kSStages) & 1);      // a timeout is the look-back warp's to report
+    const int tile = s_seen[k];
+    A run = s_pre[k];
+    for (int w = 0; w < warp; ++w) run += s_wsum[k][w];
+    A* s_data = stage(k);
+    Chunk* sc = reinterpret_cast<Chunk*>(s_data + warp * kWarpElems) + lane;
+#pragma unroll 4
+    for (int c = 0; c < kSChunks; ++c) {
+      Chunk x = sc[32 * c];
+      A l[E];
+      A acc = 0;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        l[e] = acc;  // exclusive within the lane's chunk
+        acc += x.e[e];
+      }
+      const A ci = warp_inclusive(acc, lane);
+      const A base = run + ci - acc;
+#pragma unroll
+      for (int e = 0; e < E; ++e) x.e[e] = base + l[e] + (exclusive ? (A)0 : x.e[e]);
+      sc[32 * c] = x;
+      run += __shfl_sync(kFull, ci, 31);
+    }
+    // the scanned tile, before the bulk copy reads it (and this tile's reads
+    // before the stage's next bulk copy writes it)
+    fence_proxy_async();
+    compute_sync();
+    const long long b = (long long)tile * kTileElems;
+    if (whole(tile)) {
+      if (threadIdx.x == 0) bulk_store_and_wait_read(out + b, s_data, kSTileBytes);
+    } else {
+      const long long cnt = n - b < kTileElems ? n - b : kTileElems;
+      for (int j = threadIdx.x; j < cnt; j += kSThreads) out[b + j] = (T)s_data[j];
+      compute_sync();  // the stores read the stage before it is refilled
+    }
+    if (threadIdx.x == 0) fill(k);
+    compute_sync();  // s_tile[k]
+    more = next;
+  }
+}
+
+template <typename T>
+int single_scan_tiles(long long n) {
+  const long long per = kSTileBytes / sizeof(T);
+  return (int)((n + per - 1) / per);
+}
+
+template <typename T>
+size_t single_scan_bytes(long long n) {
+  return kScanHead + TileStates<typename Acc<T>::type>::bytes(single_scan_tiles<T>(n));
+}
+
+template <typename T>
+void scan_single(const T* in, T* out, long long n, bool exclusive, char* scratch, int num_sms,
+                 cudaStream_t s) {
+  typedef typename Acc<T>::type A;
+  const size_t smem = (size_t)kSStages * kSTileBytes;
+  // the ring is above the 48 KB of shared memory a launch gets without
+  // opting in; set once per device (a failure shows as the launch's error)
+  static int opted[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !opted[dev]) {
+    if (cudaFuncSetAttribute(k_scan_single<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) == cudaSuccess &&
+        cudaFuncSetAttribute(k_scan_single<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess)
+      opted[dev] = 1;
+  }
+  const int tiles = single_scan_tiles<T>(n);
+  const int blocks = tiles < num_sms ? tiles : num_sms;
+  const int bulk = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+  cudaMemsetAsync(scratch, 0, kScanHead + TileStates<A>::clear_bytes(tiles), s);
+  k_scan_single<T><<<blocks, kSThreads + 32, smem, s>>>(in, out, n, tiles,
+                                                        reinterpret_cast<ScanCtl*>(scratch),
+                                                        scratch + kScanHead, exclusive ? 1 : 0,
+                                                        bulk);
 }
 
 // ---- radix sort -------------------------------------------------------------
@@ -657,6 +1026,13 @@ int read_back(void* host, const void* dev, size_t bytes, cudaStream_t s, const c
 
 size_t scan_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
 
+// dax_gb300_scan: the reduce-then-scan sums (floats) or the single-pass
+// states (integers), whichever is larger.
+size_t public_scan_bytes(long long n) {
+  const size_t a = scan_bytes(n), b = align256(single_scan_bytes<int64_t>(n));
+  return a > b ? a : b;
+}
+
 size_t keep_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
 
 }  // namespace
@@ -686,7 +1062,9 @@ using daxgb::align256;
 
 extern "C" {
 
-size_t dax_gb300_scan_scratch_bytes(int64_t n) { return daxgb::scan_bytes(n < 1 ? 1 : n); }
+size_t dax_gb300_scan_scratch_bytes(int64_t n) {
+  return daxgb::public_scan_bytes(n < 1 ? 1 : n);
+}
 
 int dax_gb300_scan(const void* d_in, void* d_out, int64_t n, int type, int exclusive,
                    void* d_scratch, size_t scratch_bytes, void* h_total, void* stream) {
@@ -700,20 +1078,32 @@ int dax_gb300_scan(const void* d_in, void* d_out, int64_t n, int type, int exclu
     return DAX_GB300_SUCCESS;
   }
   if (!d_in || !d_out || !d_scratch) return bad("NULL input, output or scratch");
-  if (scratch_bytes < scan_bytes(n)) return bad("scratch smaller than dax_gb300_scan_scratch_bytes()");
+  if (scratch_bytes < public_scan_bytes(n))
+    return bad("scratch smaller than dax_gb300_scan_scratch_bytes()");
   const int sms = prim_sms();
   char* sc = static_cast<char*>(d_scratch);
+  const bool ex = exclusive != 0;
   switch (type) {
-    case DAX_GB300_TYPE_I32: scan_t<int32_t>((const int32_t*)d_in, (int32_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
-    case DAX_GB300_TYPE_U32: scan_t<uint32_t>((const uint32_t*)d_in, (uint32_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
-    case DAX_GB300_TYPE_F32: scan_t<float>((const float*)d_in, (float*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
-    case DAX_GB300_TYPE_I64: scan_t<int64_t>((const int64_t*)d_in, (int64_t*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
-    default: scan_t<unsigned long long>((const unsigned long long*)d_in, (unsigned long long*)d_out, n, exclusive != 0, sc, nullptr, sms, s); break;
+    case DAX_GB300_TYPE_I32: scan_single<int32_t>((const int32_t*)d_in, (int32_t*)d_out, n, ex, sc, sms, s); break;
+    case DAX_GB300_TYPE_U32: scan_single<uint32_t>((const uint32_t*)d_in, (uint32_t*)d_out, n, ex, sc, sms, s); break;
+    case DAX_GB300_TYPE_F32: scan_t<float>((const float*)d_in, (float*)d_out, n, ex, sc, nullptr, sms, s); break;
+    case DAX_GB300_TYPE_I64: scan_single<int64_t>((const int64_t*)d_in, (int64_t*)d_out, n, ex, sc, sms, s); break;
+    default: scan_single<unsigned long long>((const unsigned long long*)d_in, (unsigned long long*)d_out, n, ex, sc, sms, s); break;
   }
   int st = launched("scan kernels");
   if (st || !h_total) return st;
-  // the scanned tile sums end with the grand total, in a type as wide as the element
-  return read_back(h_total, sc + (size_t)ptiles(n) * tb, (size_t)tb, s, "reading the scan total");
+  if (type == DAX_GB300_TYPE_F32)  // the scanned tile sums end with the grand total
+    return read_back(h_total, sc + (size_t)ptiles(n) * tb, (size_t)tb, s, "reading the scan total");
+  // the single pass: the error word and the total (little-endian, as wide as the element)
+  ScanCtl ctl;
+  st = read_back(&ctl, sc, sizeof(ctl), s, "reading the scan total");
+  if (st) return st;
+  if (ctl.error) {
+    set_last_error("scan: a look-back wait expired on the device");
+    return DAX_GB300_ERROR_TIMEOUT;
+  }
+  memcpy(h_total, &ctl.total, (size_t)tb);
+  return DAX_GB300_SUCCESS;
 }
 
 size_t dax_gb300_sort_scratch_bytes(int64_t n, int key_type, int value_bytes) {

@@ -70,6 +70,19 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// Shared-memory bytes [src, src + bytes) to global memory as one bulk copy
+// (both addresses and the size multiples of 16), then wait until the copy has
+// read all of its source, after which the shared memory may be reused.
+// The threads that wrote src must run fence_proxy_async() and meet the
+// issuing thread at a barrier first.
+__device__ __forceinline__ void bulk_store_and_wait_read(void* dst, const void* src,
+                                                         unsigned bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"(smem_addr(src)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
 
 // Bounded waiting: more() is false once kSpinIters polls or kSpinNs have
 // passed since the first poll.

@@ -626,7 +626,10 @@ size_t dax_gb300_scan_scratch_bytes(int64_t n);
  * d_in[0..i] (inclusive) or d_in[0..i-1] (exclusive), any type above; d_out
  * may equal d_in.  Integer sums wrap in the element width.  If h_total is
  * not NULL it receives the sum of all elements (one element of the type; the
- * stream is synchronised for it), which is what the reference returns. */
+ * stream is synchronised for it), which is what the reference returns.
+ * Integer scans run in one pass whose tiles wait, bounded, on the sums of the
+ * tiles before them; a wait that ran out is reported as
+ * DAX_GB300_ERROR_TIMEOUT when h_total is read. */
 int dax_gb300_scan(const void* d_in, void* d_out, int64_t n, int type, int exclusive,
                    void* d_scratch, size_t scratch_bytes, void* h_total, void* stream);
 

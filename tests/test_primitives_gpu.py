@@ -160,6 +160,70 @@ def test_scan_int32_wraps(A):
     assert total == int(ref[-1])
 
 
+# Integer scans run in one pass, each tile's prefix found by looking back
+# over the tiles before it (64 KB tiles: 16384 int32 or 8192 int64 elements;
+# 32 tiles a look-back step).  These sizes span thousands of tiles and many
+# steps, exactly 33 tiles, and ragged ends; the scan is repeated in place and
+# out of place and must give the same bits.
+@pytest.mark.parametrize("n,dtype", [(50_000_001, np.int32), (12_345_679, np.int64),
+                                     (16384 * 33, np.int32), (8192 * 32 + 1, np.int64)])
+def test_scan_single_pass_large(A, n, dtype):
+    rng = np.random.default_rng(n)
+    x = _rand(dtype, n, rng)  # the type's full range: sums wrap all the time
+    ref = np.cumsum(x, dtype=dtype)
+    ref_ex = np.concatenate([np.zeros(1, dtype), ref[:-1]])
+    d = cuda(x)
+    for _ in range(2):
+        total, out = A.ScanInclusive(d)
+        assert np.array_equal(out.cpu().numpy(), ref)
+        assert total == int(ref[-1])
+    total, out = A.ScanExclusive(d)
+    assert np.array_equal(out.cpu().numpy(), ref_ex)
+    assert total == int(ref[-1])
+    total, out = A.ScanInclusive(d, d)  # in place
+    assert out.data_ptr() == d.data_ptr()
+    assert np.array_equal(d.cpu().numpy(), ref)
+
+
+def test_scan_single_pass_unaligned(A):
+    """Arrays that do not start on a 16-byte boundary take element loads and
+    stores instead of the bulk copies; results are the same."""
+    n = 16384 * 5 + 77
+    rng = np.random.default_rng(11)
+    x = rng.integers(-2 ** 31, 2 ** 31 - 1, n + 3, dtype=np.int32, endpoint=True)
+    d = cuda(x)
+    src, dst = d[1:n + 1], torch.empty(n + 2, dtype=torch.int32, device="cuda")[2:]
+    total, out = A.ScanInclusive(src, dst)
+    ref = np.cumsum(x[1:n + 1], dtype=np.int32)
+    assert np.array_equal(dst.cpu().numpy(), ref)
+    assert total == int(ref[-1])
+
+
+@pytest.mark.parametrize("unsigned", [np.uint32, np.uint64])
+def test_scan_unsigned_through_abi(gb300, unsigned):
+    """U32 / U64 through the C ABI directly (torch has no unsigned scan types
+    to carry them in the wrapper): the bits of the signed scan of the same
+    words, and the total in the element's width."""
+    import ctypes
+    from daxtoolkit_gb300 import capi
+    n = 3_000_017
+    rng = np.random.default_rng(5)
+    x = rng.integers(0, np.iinfo(unsigned).max, n, dtype=unsigned, endpoint=True)
+    ref = np.cumsum(x, dtype=unsigned)
+    signed = np.int32 if unsigned == np.uint32 else np.int64
+    d = cuda(x.view(signed))
+    out = torch.empty_like(d)
+    nb = capi.lib().dax_gb300_scan_scratch_bytes(n)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    total = np.zeros(1, unsigned)
+    t = 1 if unsigned == np.uint32 else 4  # DAX_GB300_TYPE_U32 / _U64
+    capi.call("dax_gb300_scan", ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(out.data_ptr()), n,
+              t, 0, ctypes.c_void_p(scratch.data_ptr()), nb,
+              ctypes.c_void_p(total.ctypes.data), None)
+    assert np.array_equal(out.cpu().numpy().view(unsigned), ref)
+    assert total[0] == ref[-1]
+
+
 def _ordered_bits(k):
     """Unsigned integers with the order of k (IEEE order for floats)."""
     if k.dtype == np.float32:
