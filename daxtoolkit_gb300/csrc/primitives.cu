@@ -6,7 +6,8 @@
 // (dax::Id = int32, int64, unsigned, dax::Scalar = float) with values of up
 // to 16 bytes (a dax::Vector3 is 12).
 //
-// Every primitive works on tiles of kPTile elements (256 threads x 16):
+// Tiles: the float scan and the sort work on kPTile elements (256 threads x
+// 16), the integer scan and the compaction on 64 KB of elements:
 //   scan     integers: one pass, each tile's prefix found by a decoupled
 //            look-back over the tiles before it; floats (and the sort's
 //            histograms): reduce-then-scan, tile sums, one block scanning
@@ -17,9 +18,10 @@
 //            histogram, a scan of the histograms in digit-major order, and a
 //            scatter that ranks each element among equal digits of its tile
 //            (warp match + per-warp counts) in element order;
-//   compact  per-tile counts of the kept elements, their scan, and an
-//            order-preserving scatter (Unique = compact of "differs from the
-//            previous element", through shared memory for 4-byte keys;
+//   compact  one pass on the integer scan's machinery: a tile's kept
+//            elements are counted as it lands, its offset found by the
+//            look-back, and the kept elements written at their places
+//            (Unique = compact of "differs from the previous key", in place;
 //            StreamCompact = compact of "stencil != 0").
 #include <cstdint>
 #include <cstring>
@@ -761,143 +763,284 @@ size_t scatter_smem() {
          (kPT / 32) * 4;
 }
 
-// ---- compaction (Unique, StreamCompact) ----------------------------------
-
-// Whether element i is kept.  mode 0: stencil int32 != 0; 1: stencil float
-// != 0; 2: key differs from the previous key (word-sized keys compared as
-// values of the key type, so +0.0 and -0.0 are equal and NaNs all differ).
-struct KeepTest {
-  int mode;
-  int key_kind;   // for mode 2: 0 unsigned, 1 signed, 2 float
-  int key_bytes;  // 4 or 8
-  const void* data;
-  __device__ __forceinline__ bool operator()(long long i) const {
-    if (mode == 0) return static_cast<const int32_t*>(data)[i] != 0;
-    if (mode == 1) return static_cast<const float*>(data)[i] != 0.0f;
-    if (i == 0) return true;
-    if (key_bytes == 4) {
-      if (key_kind == 2) {
-        const float* k = static_cast<const float*>(data);
-        return k[i] != k[i - 1];
-      }
-      const uint32_t* k = static_cast<const uint32_t*>(data);
-      return k[i] != k[i - 1];
-    }
-    const unsigned long long* k = static_cast<const unsigned long long*>(data);
-    return k[i] != k[i - 1];
-  }
+// ---- single-pass compaction ------------------------------------------------
+//
+// StreamCompact and Unique in one read of the stencil (or keys), on the
+// single-pass scan's machinery: one persistent block an SM, a ring of 64 KB
+// tiles of the tested array filled by bulk TMA copies, compute warps that
+// count a tile's kept elements as it lands and publish the count, and a warp
+// that finds the tile's offset by the bounded look-back over the tiles
+// before it.  The compute warps then write the tile's kept elements at their
+// places: the key itself (Unique), the value gathered from its array
+// (StreamCompact with an input), or the element's index.
+//
+// Unique writes in place: a tile's kept keys go below its own start, into
+// tiles that have already loaded (their counts are published before this
+// tile's offset is known); the only place it shares with a later read is the
+// key before the next tile, which it rewrites only when no key before it was
+// dropped, that is with the same key.
+struct CompactOp {
+  int mode;          // 0 stencil int32 != 0; 1 stencil float != 0; 2 key differs from the previous
+  int key_kind;      // mode 2: 0 unsigned, 1 signed, 2 float (compared as values)
+  const void* test;  // the staged array: stencil or keys
+  const uint32_t* values;  // modes 0 / 1: the values to gather (NULL: the index instead)
+  int words;               // 32-bit words a value
+  void* out;
 };
 
-__global__ void __launch_bounds__(kPT) k_keep_count(KeepTest keep, long long n,
-                                                    unsigned long long* __restrict__ cnt,
-                                                    int tiles) {
-  __shared__ unsigned long long s_warp[kPT / 32];
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    unsigned long long c = 0;
-    const long long b = (long long)tile * kPTile;
-#pragma unroll 4
-    for (int e = 0; e < kPI; ++e) {
-      const long long i = b + e * kPT + threadIdx.x;
-      if (i < n && keep(i)) ++c;
-    }
-    unsigned long long tot;
-    block_exclusive(c, s_warp, &tot);
-    if (threadIdx.x == 0) cnt[tile] = tot;
-  }
+template <typename S>
+__device__ __forceinline__ bool keep_of(const CompactOp& op, S x, S prev, bool first) {
+  if (op.mode == 0) return (int32_t)x != 0;
+  if (op.mode == 1) return __uint_as_float((uint32_t)x) != 0.0f;
+  if (first) return true;
+  if (sizeof(S) == 4 && op.key_kind == 2)
+    return __uint_as_float((uint32_t)x) != __uint_as_float((uint32_t)prev);
+  return x != prev;
 }
 
-// Order-preserving scatter of the kept elements: element bytes (a multiple of
-// 4) from `in`, or the element's index as int32 when `in` is NULL.
-__global__ void __launch_bounds__(kPT) k_keep_scatter(KeepTest keep, const uint32_t* __restrict__ in,
-                                                      int words, long long n, uint32_t* __restrict__ out,
-                                                      const unsigned long long* __restrict__ pre,
-                                                      int tiles) {
-  __shared__ unsigned long long s_warp[kPT / 32];
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const long long b = (long long)tile * kPTile + (long long)threadIdx.x * kPI;
-    uint32_t flags = 0;
-    unsigned long long c = 0;
+// S: the staged element (uint32_t or unsigned long long).  W: 32-bit words a
+// gathered value (StreamCompact with an input: the tile's values are
+// prefetched into L2 by one bulk copy when the tile is taken, and a lane
+// loads its chunks' W x 16 bytes of values four chunks at a time, before
+// their stores), or 0 (Unique's keys, or indices).
+template <typename S, int W>
+__global__ void __launch_bounds__(kSThreads + 32, 1)
+    k_compact_single(CompactOp op, long long n, int tiles, ScanCtl* ctl, char* states, int bulk,
+                     int vec) {
+  typedef uint32_t A;  // counts: fewer than 2^31 elements
+  constexpr int E = 16 / (int)sizeof(S);
+  constexpr int kTileElems = (int)(kSTileBytes / sizeof(S));
+  constexpr int kWarps = kSThreads / 32;
+  constexpr int kWarpElems = kTileElems / kWarps;
+  struct Chunk { S e[E]; };
+  static_assert(sizeof(Chunk) == 16, "16-byte chunks");
+  const TileStates<A> st(states, tiles);
+  const S* in = static_cast<const S*>(op.test);
+  extern __shared__ __align__(128) unsigned char scan_smem[];
+  __shared__ __align__(8) uint64_t b_full[kSStages], b_agg[kSStages], b_pre[kSStages];
+  __shared__ int s_tile[kSStages];
+  __shared__ int s_seen[kSStages];
+  __shared__ A s_tot[kSStages], s_pre[kSStages], s_wsum[kSStages][kWarps];
+  // the key before the tile (Unique), read once by thread 0 while counting,
+  // before this tile writes anything, and used by thread 0 alone
+  __shared__ S s_prev[kSStages];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto whole = [&](int t) { return bulk && (long long)(t + 1) * kTileElems <= n; };
+  auto stage = [&](int k) { return reinterpret_cast<S*>(scan_smem + (size_t)k * kSTileBytes); };
+  unsigned long long policy = 0;
+  auto fill = [&](int k) {
+    const int t = (int)atomicAdd(&ctl->ticket, 1u);
+    s_tile[k] = t;
+    if (t < tiles && whole(t)) {
+      mbar_arrive_tx(&b_full[k], kSTileBytes);
+      bulk_load(stage(k), in + (long long)t * kTileElems, kSTileBytes, &b_full[k], policy);
+      if (W > 0 && vec)  // the tile's values, into L2 ahead of the gather
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                         op.values + (long long)t * kTileElems * W),
+                     "r"((unsigned)(kTileElems * W * 4))
+                     : "memory");
+    }
+  };
+  if (threadIdx.x == 0) {
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+    for (int k = 0; k < kSStages; ++k) {
+      mbar_init(&b_full[k], 1);
+      mbar_init(&b_agg[k], 1);
+      mbar_init(&b_pre[k], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int k = 0; k < kSStages; ++k) fill(k);
+  }
+  __syncthreads();
+
+  if (warp == kWarps) {
+    for (int i = 0;; ++i) {
+      const int k = i % kSStages;
+      bool failed = !wait_phase(&b_agg[k], (i / kSStages) & 1);
+      const int tile = s_seen[k];
+      if (tile >= tiles) break;
+      const A tot = s_tot[k];
+      const A prefix = look_back(st, tile, lane, failed);
+      failed = __any_sync(kFull, failed);
+      if (lane == 0) {
+        if (tile > 0) st.publish(tile, kStInc, prefix + tot);
+        if (failed) atomicOr(&ctl->error, 1u);
+        if (tile == tiles - 1) ctl->total = (unsigned long long)(prefix + tot);
+        s_pre[k] = prefix;
+        mbar_arrive(&b_pre[k]);
+      }
+      __syncwarp();
+    }
+    return;
+  }
+
+  // kept mask of the lane's chunk c (bit e: element e), from the staged tile
+  auto kept = [&](int k, long long b, int c, Chunk& x) -> unsigned {
+    const S* s_data = stage(k);
+    const int idx0 = warp * kWarpElems + (32 * c + lane) * E;  // tile-local index of element 0
+    x = reinterpret_cast<const Chunk*>(s_data + idx0)[0];
+    S prev = 0;
+    if (op.mode == 2 && b + idx0 > 0) prev = idx0 > 0 ? s_data[idx0 - 1] : s_prev[k];
+    unsigned m = 0;
 #pragma unroll
-    for (int e = 0; e < kPI; ++e)
-      if (b + e < n && keep(b + e)) {
-        flags |= 1u << e;
-        ++c;
-      }
-    unsigned long long tot;
-    unsigned long long pos = pre[tile] + block_exclusive(c, s_warp, &tot);
-    for (uint32_t f = flags; f; f &= f - 1, ++pos) {
-      const long long i = b + __ffs(f) - 1;
-      if (in) {
-        for (int q = 0; q < words; ++q) out[pos * words + q] = in[i * words + q];
-      } else {
-        out[pos] = (uint32_t)i;
-      }
+    for (int e = 0; e < E; ++e) {
+      if (b + idx0 + e < n && keep_of<S>(op, x.e[e], prev, b + idx0 + e == 0)) m |= 1u << e;
+      prev = x.e[e];
     }
-  }
-}
-
-// The same scatter for 4-byte elements, through shared memory:
-// the tile's elements and keep flags are loaded striped (coalesced), each
-// thread ranks its 16 consecutive elements, the kept ones are gathered in
-// element order in shared memory, and the tile's kept run is written out
-// striped (coalesced) at its offset.
-__global__ void __launch_bounds__(kPT) k_keep_scatter1(KeepTest keep, const uint32_t* __restrict__ in,
-                                                       long long n, uint32_t* __restrict__ out,
-                                                       const unsigned long long* __restrict__ pre,
-                                                       int tiles) {
-  __shared__ unsigned long long s_warp[kPT / 32];
-  __shared__ uint32_t s_v[kPTile + kPTile / 32];  // the tile's elements, padded
-  __shared__ uint32_t s_o[kPTile];                // its kept elements, in order
-  __shared__ unsigned char s_f[kPTile];           // its keep flags
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const long long b = (long long)tile * kPTile;
+    return m;
+  };
+  unsigned fullp = 0;
+  auto reduce = [&](int k) -> bool {
+    const int tile = s_tile[k];
+    if (tile >= tiles) {
+      if (threadIdx.x == 0) {
+        s_seen[k] = tile;
+        mbar_arrive(&b_agg[k]);
+      }
+      return false;
+    }
+    S* s_data = stage(k);
+    const long long b = (long long)tile * kTileElems;
+    bool ok = true;
+    if (whole(tile)) {
+      ok = wait_phase(&b_full[k], (fullp >> k) & 1u);
+      fullp ^= 1u << k;
+    } else {
+      const long long cnt = n - b < kTileElems ? n - b : kTileElems;
+      for (int i = threadIdx.x; i < kTileElems; i += kSThreads) s_data[i] = i < cnt ? in[b + i] : (S)0;
+      compute_sync();
+    }
+    if (threadIdx.x == 0) s_prev[k] = op.mode == 2 && b > 0 ? in[b - 1] : (S)0;
+    A sum = 0;
 #pragma unroll 4
-    for (int e = 0; e < kPI; ++e) {
-      const int li = e * kPT + threadIdx.x;
-      const long long i = b + li;
-      const bool ok = i < n;
-      s_f[li] = ok && keep(i) ? 1 : 0;
-      s_v[pad(li)] = in ? (ok ? in[i] : 0u) : (uint32_t)i;
+    for (int c = 0; c < kSChunks; ++c) {
+      Chunk x;
+      sum += __popc(kept(k, b, c, x));
     }
-    __syncthreads();
-    uint32_t flags = 0;
-    unsigned long long c = 0;
 #pragma unroll
-    for (int e = 0; e < kPI; ++e)
-      if (s_f[threadIdx.x * kPI + e]) {
-        flags |= 1u << e;
-        ++c;
+    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
+    if (lane == 0) s_wsum[k][warp] = sum;
+    compute_sync();
+    if (threadIdx.x == 0) {
+      A tot = 0;
+      for (int w = 0; w < kWarps; ++w) tot += s_wsum[k][w];
+      st.publish(tile, tile == 0 ? kStInc : kStAgg, tot);
+      if (!ok) {
+        atomicOr(&ctl->error, 1u);
+        wait_phase(&b_full[k], (fullp >> k) & 1u ^ 1u);
       }
-    unsigned long long tot;
-    unsigned long long pos = block_exclusive(c, s_warp, &tot);
-    for (uint32_t f = flags; f; f &= f - 1, ++pos)
-      s_o[pos] = s_v[pad(threadIdx.x * kPI + __ffs(f) - 1)];
-    __syncthreads();
-    const unsigned long long base = pre[tile];
-    for (int j = threadIdx.x; j < (int)tot; j += kPT) out[base + j] = s_o[j];
-    __syncthreads();
+      s_tot[k] = tot;
+      s_seen[k] = tile;
+      mbar_arrive(&b_agg[k]);
+    }
+    return true;
+  };
+
+  bool more = reduce(0);
+  for (int i = 0; more; ++i) {
+    const int k = i % kSStages;
+    const bool next = reduce((i + 1) % kSStages);
+    wait_phase(&b_pre[k], (i / kSStages) & 1);
+    const int tile = s_seen[k];
+    const long long b = (long long)tile * kTileElems;
+    unsigned long long run = s_pre[k];
+    for (int w = 0; w < warp; ++w) run += s_wsum[k][w];
+    const long long wb = b + warp * kWarpElems;  // the warp's first element
+    constexpr int kV = W > 0 ? W : 1;
+    constexpr int kG = 4;  // chunks whose values are loaded before any of their stores
+    // the W words of each of the lane's E elements of chunk c
+    auto load_values = [&](int c, uint4* v) {
+      if constexpr (W > 0) {
+        const long long i0 = wb + (32 * c + lane) * E;
+        if (vec && i0 + E <= n) {
+          const uint4* src = reinterpret_cast<const uint4*>(op.values + i0 * W);
+#pragma unroll
+          for (int q = 0; q < W; ++q) v[q] = __ldcs(src + q);
+        } else {
+          uint32_t* u = reinterpret_cast<uint32_t*>(v);
+#pragma unroll
+          for (int e = 0; e < E; ++e)
+#pragma unroll
+            for (int q = 0; q < W; ++q) u[e * W + q] = i0 + e < n ? op.values[(i0 + e) * W + q] : 0u;
+        }
+      }
+    };
+#pragma unroll 1
+    for (int c0 = 0; c0 < kSChunks; c0 += kG) {
+      uint4 vals[kG][kV];
+#pragma unroll
+      for (int g = 0; g < kG; ++g) load_values(c0 + g, vals[g]);
+#pragma unroll
+      for (int g = 0; g < kG; ++g) {
+        const int c = c0 + g;
+        Chunk x;
+        const unsigned m = kept(k, b, c, x);
+        const A cm = __popc(m);
+        const A ci = warp_inclusive(cm, lane);
+        unsigned long long pos = run + ci - cm;
+        const long long i0 = wb + (32 * c + lane) * E;
+        const uint32_t* u = reinterpret_cast<const uint32_t*>(vals[g]);
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+          if ((m >> e) & 1u) {
+            if constexpr (W > 0) {
+              uint32_t* dst = static_cast<uint32_t*>(op.out) + pos * W;
+#pragma unroll
+              for (int q = 0; q < W; ++q) dst[q] = u[e * W + q];
+            } else if (op.mode == 2) {
+              static_cast<S*>(op.out)[pos] = x.e[e];
+            } else {
+              static_cast<int32_t*>(op.out)[pos] = (int32_t)(i0 + e);
+            }
+            ++pos;
+          }
+        run += __shfl_sync(kFull, ci, 31);
+      }
+    }
+    // this tile's reads of the stage before its next bulk copy writes it
+    fence_proxy_async();
+    compute_sync();
+    if (threadIdx.x == 0) fill(k);
+    compute_sync();
+    more = next;
   }
 }
 
-// Kept elements of `in` (or their indices) into `out`; the count goes to
-// cnt_pre[tiles] on the device.  cnt_pre holds sum_slots(n) entries.
-void keep_pass(const KeepTest& keep, const void* in, int words, long long n, void* out,
-               unsigned long long* cnt_pre, int num_sms, cudaStream_t s) {
-  const int tiles = ptiles(n);
-  const int b = resident((const void*)k_keep_count, kPT, num_sms, tiles);
-  k_keep_count<<<b, kPT, 0, s>>>(keep, n, cnt_pre, tiles);
-  scan_sums<unsigned long long>(cnt_pre, tiles, cnt_pre + tiles + 1, s);
-  // Unique of 4-byte keys through shared memory: its test reads each key and
-  // its predecessor, which the per-thread scatter loads with a 64-byte lane
-  // stride (0.97 -> 0.78 ms for 100 M keys).  A stencil compaction stays on
-  // the per-thread scatter, which reads only the kept values (0.44 ms against
-  // 0.84 ms staged, 30 % kept).
-  if (keep.mode == 2 && words == 1)
-    k_keep_scatter1<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), n,
-                                      static_cast<uint32_t*>(out), cnt_pre, tiles);
-  else
-    k_keep_scatter<<<b, kPT, 0, s>>>(keep, static_cast<const uint32_t*>(in), words, n,
-                                     static_cast<uint32_t*>(out), cnt_pre, tiles);
+template <typename S, int W>
+void compact_single_w(const CompactOp& op, long long n, char* scratch, int num_sms,
+                      cudaStream_t s) {
+  const size_t smem = (size_t)kSStages * kSTileBytes;
+  static int opted[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !opted[dev]) {
+    if (cudaFuncSetAttribute(k_compact_single<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) == cudaSuccess &&
+        cudaFuncSetAttribute(k_compact_single<S, W>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess)
+      opted[dev] = 1;
+  }
+  const long long per = kSTileBytes / sizeof(S);
+  const int tiles = (int)((n + per - 1) / per);
+  const int blocks = tiles < num_sms ? tiles : num_sms;
+  const int bulk = (reinterpret_cast<uintptr_t>(op.test) & 15) == 0;
+  const int vec = (reinterpret_cast<uintptr_t>(op.values) & 15) == 0;
+  cudaMemsetAsync(scratch, 0, kScanHead + TileStates<uint32_t>::clear_bytes(tiles), s);
+  k_compact_single<S, W><<<blocks, kSThreads + 32, smem, s>>>(
+      op, n, tiles, reinterpret_cast<ScanCtl*>(scratch), scratch + kScanHead, bulk, vec);
+}
+
+// Kept elements into op.out, the count to ctl->total on the device.
+template <typename S>
+void compact_single(const CompactOp& op, long long n, char* scratch, int num_sms, cudaStream_t s) {
+  switch (op.values ? op.words : 0) {
+    case 1: compact_single_w<S, 1>(op, n, scratch, num_sms, s); break;
+    case 2: compact_single_w<S, 2>(op, n, scratch, num_sms, s); break;
+    case 3: compact_single_w<S, 3>(op, n, scratch, num_sms, s); break;
+    case 4: compact_single_w<S, 4>(op, n, scratch, num_sms, s); break;
+    default: compact_single_w<S, 0>(op, n, scratch, num_sms, s); break;
+  }
 }
 
 // ---- sort driver -----------------------------------------------------------
@@ -1022,6 +1165,20 @@ int read_back(void* host, const void* dev, size_t bytes, cudaStream_t s, const c
   if (e == cudaSuccess) return DAX_GB300_SUCCESS;
   set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
   return DAX_GB300_ERROR_CUDA;
+}
+
+// The element count of a single-pass compaction (synchronises the stream);
+// a look-back wait that ran out is DAX_GB300_ERROR_TIMEOUT.
+int read_count(int64_t* h_count, const char* scratch, cudaStream_t s, const char* what) {
+  ScanCtl ctl;
+  int st = read_back(&ctl, scratch, sizeof(ctl), s, what);
+  if (st) return st;
+  if (ctl.error) {
+    set_last_error(std::string(what) + ": a look-back wait expired on the device");
+    return DAX_GB300_ERROR_TIMEOUT;
+  }
+  *h_count = (int64_t)ctl.total;
+  return DAX_GB300_SUCCESS;
 }
 
 size_t scan_bytes(long long n) { return align256((size_t)sum_slots(n) * 8); }
@@ -1161,18 +1318,16 @@ int dax_gb300_unique(void* d_keys, int64_t n, int key_type, void* d_scratch, siz
   if (!d_keys || !d_scratch) return bad("NULL keys or scratch");
   if (scratch_bytes < dax_gb300_compact_scratch_bytes(n, kb))
     return bad("scratch smaller than dax_gb300_compact_scratch_bytes(n, key bytes)");
+  // one pass, in place (the kept keys of a tile go below its start)
   char* sc = static_cast<char*>(d_scratch);
-  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(sc);
-  void* tmp = sc + keep_bytes(n);
-  KeepTest keep{2, type_kind(key_type), kb, d_keys};
-  keep_pass(keep, d_keys, kb / 4, n, tmp, cnt, prim_sms(), s);
-  cudaMemcpyAsync(d_keys, tmp, (size_t)n * kb, cudaMemcpyDeviceToDevice, s);
+  const CompactOp op{2, type_kind(key_type), d_keys, nullptr, 0, d_keys};
+  if (kb == 4)
+    compact_single<uint32_t>(op, n, sc, prim_sms(), s);
+  else
+    compact_single<unsigned long long>(op, n, sc, prim_sms(), s);
   int st = launched("unique kernels");
   if (st || !h_count) return st;
-  unsigned long long c = 0;
-  st = read_back(&c, cnt + ptiles(n), sizeof(c), s, "reading the unique count");
-  *h_count = (int64_t)c;
-  return st;
+  return read_count(h_count, sc, s, "reading the unique count");
 }
 
 int dax_gb300_stream_compact(const void* d_input, int value_bytes, const void* d_stencil,
@@ -1192,15 +1347,14 @@ int dax_gb300_stream_compact(const void* d_input, int value_bytes, const void* d
   if (!d_stencil || !d_output || !d_scratch) return bad("NULL stencil, output or scratch");
   if (scratch_bytes < dax_gb300_compact_scratch_bytes(n, 0))
     return bad("scratch smaller than dax_gb300_compact_scratch_bytes(n, 0)");
-  unsigned long long* cnt = static_cast<unsigned long long*>(d_scratch);
-  KeepTest keep{stencil_type == DAX_GB300_TYPE_I32 ? 0 : 1, 0, 4, d_stencil};
-  keep_pass(keep, d_input, d_input ? value_bytes / 4 : 1, n, d_output, cnt, prim_sms(), s);
+  char* sc = static_cast<char*>(d_scratch);
+  const CompactOp op{stencil_type == DAX_GB300_TYPE_I32 ? 0 : 1, 0, d_stencil,
+                     static_cast<const uint32_t*>(d_input), d_input ? value_bytes / 4 : 1,
+                     d_output};
+  compact_single<uint32_t>(op, n, sc, prim_sms(), s);
   int st = launched("compaction kernels");
   if (st || !h_count) return st;
-  unsigned long long c = 0;
-  st = read_back(&c, cnt + ptiles(n), sizeof(c), s, "reading the compacted count");
-  *h_count = (int64_t)c;
-  return st;
+  return read_count(h_count, sc, s, "reading the compacted count");
 }
 
 int dax_gb300_bounds(const void* d_sorted, int64_t n, const void* d_values, int64_t m,

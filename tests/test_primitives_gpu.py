@@ -307,6 +307,45 @@ def test_stream_compact_random(A, n, stype, vcols):
         assert np.array_equal(got, vv[stencil != 0])
 
 
+# StreamCompact and Unique run in one pass: 64 KB tiles of the stencil (or
+# keys), each tile's offset found by looking back over the tiles before it.
+# These cases span thousands of tiles, NaN and -0.0 stencil entries, 16-byte
+# values, an unaligned stencil (element loads instead of bulk copies) and
+# Unique in place on 8-byte and float keys.
+def test_stream_compact_single_pass_large(A):
+    n = 40_000_003
+    rng = np.random.default_rng(17)
+    stencil = np.where(rng.random(n) < 0.3, rng.standard_normal(n), 0.0).astype(np.float32)
+    stencil[rng.integers(0, n, 1000)] = np.nan   # NaN != 0: kept
+    stencil[rng.integers(0, n, 1000)] = -0.0     # -0.0 == 0: dropped
+    keep = stencil != 0
+    got = A.StreamCompact(cuda(stencil)).cpu().numpy()
+    assert np.array_equal(got, np.nonzero(keep)[0].astype(np.int32))
+    v = rng.integers(-2 ** 31, 2 ** 31 - 1, (n, 4), dtype=np.int32, endpoint=True)  # 16-byte rows
+    got = A.StreamCompact(cuda(v), cuda(stencil)).cpu().numpy()
+    assert np.array_equal(got, v[keep])
+    # an int32 stencil that starts 4 bytes past a 16-byte boundary
+    si = (rng.random(n + 1) < 0.5).astype(np.int32)
+    d = cuda(si)[1:]
+    got = A.StreamCompact(d).cpu().numpy()
+    assert np.array_equal(got, np.nonzero(si[1:])[0].astype(np.int32))
+
+
+@pytest.mark.parametrize("dtype", [np.int64, np.float32, np.int32])
+def test_unique_single_pass_large(A, dtype):
+    n = 30_000_001
+    rng = np.random.default_rng(23)
+    x = np.sort(rng.integers(-5_000_000, 5_000_000, n)).astype(dtype)
+    if dtype == np.float32:
+        x[x == 0] = -0.0
+        x[np.flatnonzero(x == 0)[::2]] = 0.0  # -0.0 and +0.0 adjacent: one run
+    d = cuda(x)
+    got = A.Unique(d)
+    assert got.data_ptr() == d.data_ptr()  # in place
+    ref = x[np.concatenate([[True], x[1:] != x[:-1]])]
+    assert np.array_equal(got.cpu().numpy(), ref)
+
+
 @pytest.mark.parametrize("n", [0, 1, 4097, 300_001])
 @pytest.mark.parametrize("dtype", [np.int32, np.int64, np.float32])
 def test_bounds_random(A, n, dtype):
