@@ -672,11 +672,15 @@ __global__ void __launch_bounds__(kPT) k_digit_hist(const U* __restrict__ keys, 
 // consecutive threads write consecutive places of one digit's run (the
 // tile's offset for the digit, from the scanned histograms), values gathered
 // from the tile's own range.
-template <typename U>
+// VW: 32-bit words a value (0 for Sort).  The tile's 16 keys a thread are
+// loaded before any is ranked, and in the write-out each thread gathers its
+// 16 values before storing them: each of those loads is otherwise a DRAM
+// round trip of its own.
+template <typename U, int VW>
 __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin,
                                                        U* __restrict__ kout,
                                                        const uint32_t* __restrict__ vin,
-                                                       uint32_t* __restrict__ vout, int vwords,
+                                                       uint32_t* __restrict__ vout,
                                                        long long n, int shift,
                                                        const uint32_t* __restrict__ off,
                                                        int tiles) {
@@ -700,8 +704,11 @@ __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin
 #pragma unroll
     for (int e = 0; e < kPI; ++e) {
       const long long i = tb + lb + e * 32 + lane;
-      const bool ok = i < n;
-      key[e] = ok ? kin[i] : (U)0;
+      key[e] = i < n ? kin[i] : (U)0;
+    }
+#pragma unroll
+    for (int e = 0; e < kPI; ++e) {
+      const bool ok = tb + lb + e * 32 + lane < n;
       const unsigned d = ok ? ((unsigned)(key[e] >> shift) & 255u) : 256u;
       const unsigned peers = __match_any_sync(kFull, d);
       const uint32_t before = d < 256u ? cnt[d] : 0u;
@@ -746,12 +753,29 @@ __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin
     }
     __syncthreads();
     const int valid = (int)min((long long)kPTile, n - tb);
-    for (int j = threadIdx.x; j < valid; j += kPT) {
-      const U k = s_key[j];
-      const uint32_t pos = s_dst[(unsigned)(k >> shift) & 255u] + j;
-      kout[pos] = k;
-      const long long src = tb + s_src[j];
-      for (int q = 0; q < vwords; ++q) vout[(long long)pos * vwords + q] = vin[src * vwords + q];
+    constexpr int kJ = kPTile / kPT;
+    constexpr int kV = VW > 0 ? VW : 1;
+    uint32_t at[kJ], v[kJ][kV];
+#pragma unroll
+    for (int jj = 0; jj < kJ; ++jj) {
+      const int j = threadIdx.x + jj * kPT;
+      if (j < valid) {
+        const U k = s_key[j];
+        at[jj] = s_dst[(unsigned)(k >> shift) & 255u] + j;
+        kout[at[jj]] = k;
+        if constexpr (VW > 0) {
+          const long long src = tb + s_src[j];
+#pragma unroll
+          for (int q = 0; q < VW; ++q) v[jj][q] = vin[src * VW + q];
+        }
+      }
+    }
+    if constexpr (VW > 0) {
+#pragma unroll
+      for (int jj = 0; jj < kJ; ++jj)
+        if (threadIdx.x + jj * kPT < valid)
+#pragma unroll
+          for (int q = 0; q < VW; ++q) vout[(long long)at[jj] * VW + q] = v[jj][q];
     }
     __syncthreads();
   }
@@ -1080,10 +1104,14 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
   if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 0);
   const int bh = resident((const void*)k_digit_hist<U>, kPT, num_sms, tiles);
   const size_t sm = scatter_smem<U>();
-  cudaFuncSetAttribute(k_digit_scatter<U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const void* scat = vwords == 0   ? (const void*)k_digit_scatter<U, 0>
+                     : vwords == 1 ? (const void*)k_digit_scatter<U, 1>
+                     : vwords == 2 ? (const void*)k_digit_scatter<U, 2>
+                     : vwords == 3 ? (const void*)k_digit_scatter<U, 3>
+                                   : (const void*)k_digit_scatter<U, 4>;
+  cudaFuncSetAttribute(scat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_digit_scatter<U>, kPT, sm) !=
-          cudaSuccess || per < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scat, kPT, sm) != cudaSuccess || per < 1)
     per = 1;
   const int bs = (int)(tiles < (long long)num_sms * per ? tiles : (long long)num_sms * per);
   for (int p = 0; p < passes; ++p) {
@@ -1093,7 +1121,10 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
     uint32_t* vdst = (p & 1) ? vals : vtmp;
     k_digit_hist<U><<<bh, kPT, 0, s>>>(ksrc, n, 8 * p, hist, tiles);
     scan_t<uint32_t>(hist, hist, 256ll * tiles, true, sums, nullptr, num_sms, s);
-    k_digit_scatter<U><<<bs, kPT, sm, s>>>(ksrc, kdst, vsrc, vdst, vwords, n, 8 * p, hist, tiles);
+    void* args[] = {&ksrc, &kdst, &vsrc, &vdst, &n, nullptr, &hist, const_cast<int*>(&tiles)};
+    int shift = 8 * p;
+    args[5] = &shift;
+    cudaLaunchKernel(scat, dim3(bs), dim3(kPT), args, sm, s);
   }
   if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 1);
 }
