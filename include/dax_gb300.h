@@ -170,8 +170,9 @@ int dax_gb300_mc_classify_count(const dax_gb300_uniform_grid* grid, const float*
  * (cudaMalloc's are); others are refused with DAX_GB300_ERROR_BAD_VALUE. */
 size_t dax_gb300_mc_scratch_bytes(const dax_gb300_uniform_grid* grid);
 
-/* Classify every point, count triangles and crossing edges per grid row and
- * scan them (single pass, decoupled look-back): everything
+/* Classify every point, count triangles and crossing edges per row word and
+ * scan them (a classification, a staged count and a reduce-then-scan
+ * launch; or the fused count, dax_gb300_set_fused_count): everything
  * DispatcherGenerateInterpolatedCells::GenerateNewTopology does before its
  * generate worklet (dax/cont/DispatcherGenerateInterpolatedCells.h:178-223).
  * Asynchronous; results stay in d_scratch. */
