@@ -45,7 +45,9 @@ typedef enum dax_gb300_status {
   DAX_GB300_ERROR_CAPACITY = 5,
   /* a bounded device-side wait gave up (the fused count pass's blocks wait
      on one another; the staged count waits for its bulk copies); the count
-     pass has no result and the generate pass writes nothing */
+     pass has no result and the generate pass writes nothing.  The single-pass
+     integer scan, StreamCompact and Unique (whose tiles wait on the sums of
+     earlier tiles) report it when their total or count is read */
   DAX_GB300_ERROR_TIMEOUT = 6,
   /* grid shape outside what the kernels support (see each call) */
   DAX_GB300_ERROR_UNSUPPORTED = 7
