@@ -34,9 +34,8 @@
 // tiles' look-backs behind one another), so the only waits are for a queue
 // slot whose tile a running block has reserved, or, once every unit is handed
 // out, for the last tiles to become ready; both end, and both are bounded
-// (kSpinIters polls and
-// kSpinNs of %globaltimer), after which the block sets the abort word, the
-// launch winds down and the scan reports kErrTimeout.
+// (kSpinIters polls and kSpinNs of %globaltimer), after which the block sets
+// the abort word, the launch winds down and the scan reports kErrTimeout.
 //
 // Control words (fctl, cleared before the launch): [0] unit ticket counter,
 // [1] abort, [2] queue pushes, [3] queue pops, [4 .. 4 + tiles) dependency
