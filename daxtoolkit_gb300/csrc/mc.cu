@@ -239,24 +239,8 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
   const int tile = tile_begin + blockIdx.x;
   pdl_trigger();
   pdl_wait();  // the count pass's per-word counts and tile totals
-  // exclusive prefix over the tiles before this one (64-bit: totals may pass 2^32)
-  unsigned long long pt = 0, pv = 0, pa = 0;
-  for (int x = tid; x < tile; x += 256) {
-    pt += __ldg(tile_tot + x);
-    pv += __ldg(tile_tot + tiles + x);
-    pa += __ldg(tile_tot + 2 * tiles + x);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    pt += __shfl_xor_sync(kFull, pt, o);
-    pv += __shfl_xor_sync(kFull, pv, o);
-    pa += __shfl_xor_sync(kFull, pa, o);
-  }
-  if (lane == 0) {
-    s_pre[warp] = pt;
-    s_pre[8 + warp] = pv;
-    s_pre[16 + warp] = pa;
-  }
+  // the tile's counts first: their loads are in flight while the prefix over
+  // the earlier tiles is summed
   const long long w0 = (long long)tile * kScanTile + (long long)tid * kScanItems;
   uint32_t c[kScanItems];
   const bool full = w0 + kScanItems <= rowwords;
@@ -272,6 +256,26 @@ __global__ void __launch_bounds__(256) k_word_scan(long long rowwords,
   } else {
 #pragma unroll
     for (int e = 0; e < kScanItems; ++e) c[e] = w0 + e < rowwords ? wc[w0 + e] : 0u;
+  }
+  // exclusive prefix over the tiles before this one (64-bit: totals may pass
+  // 2^32); unrolled so that a thread's loads are issued together
+  unsigned long long pt = 0, pv = 0, pa = 0;
+#pragma unroll 4
+  for (int x = tid; x < tile; x += 256) {
+    pt += __ldg(tile_tot + x);
+    pv += __ldg(tile_tot + tiles + x);
+    pa += __ldg(tile_tot + 2 * tiles + x);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pt += __shfl_xor_sync(kFull, pt, o);
+    pv += __shfl_xor_sync(kFull, pv, o);
+    pa += __shfl_xor_sync(kFull, pa, o);
+  }
+  if (lane == 0) {
+    s_pre[warp] = pt;
+    s_pre[8 + warp] = pv;
+    s_pre[16 + warp] = pa;
   }
   uint32_t st = 0, sv = 0, sa = 0;
 #pragma unroll
