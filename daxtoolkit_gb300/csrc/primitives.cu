@@ -634,18 +634,29 @@ __device__ __forceinline__ U from_ordered(U t, int kind, bool desc) {
   return t;
 }
 
-template <typename U>
-__global__ void k_order_keys(U* keys, long long n, int kind, int desc, int inverse) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    keys[i] = inverse ? from_ordered(keys[i], kind, desc != 0) : to_ordered(keys[i], kind, desc != 0);
-}
+// The ordering map of a sort pass: keys read from the caller's array are
+// mapped to ordered bits as they are loaded (the first pass, `in`), and
+// mapped back as the last pass stores them (`out`), so that no pass of its
+// own goes over the keys for either.
+struct KeyOrder {
+  int kind;  // 0 unsigned, 1 signed, 2 float
+  int desc;
+  int in, out;
+  template <typename U>
+  __device__ __forceinline__ U load(U x) const {
+    return in ? to_ordered(x, kind, desc != 0) : x;
+  }
+  template <typename U>
+  __device__ __forceinline__ U store(U t) const {
+    return out ? from_ordered(t, kind, desc != 0) : t;
+  }
+};
 
 // Digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
 template <typename U>
 __global__ void __launch_bounds__(kPT) k_digit_hist(const U* __restrict__ keys, long long n,
                                                     int shift, uint32_t* __restrict__ hist,
-                                                    int tiles) {
+                                                    int tiles, KeyOrder ord) {
   __shared__ uint32_t s_h[256];
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     s_h[threadIdx.x] = 0;
@@ -654,7 +665,7 @@ __global__ void __launch_bounds__(kPT) k_digit_hist(const U* __restrict__ keys, 
 #pragma unroll 4
     for (int e = 0; e < kPI; ++e) {
       const long long i = b + e * kPT + threadIdx.x;
-      if (i < n) atomicAdd(&s_h[(unsigned)(keys[i] >> shift) & 255u], 1u);
+      if (i < n) atomicAdd(&s_h[(unsigned)(ord.load(keys[i]) >> shift) & 255u], 1u);
     }
     __syncthreads();
     hist[(long long)threadIdx.x * tiles + tile] = s_h[threadIdx.x];
@@ -683,7 +694,7 @@ __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin
                                                        uint32_t* __restrict__ vout,
                                                        long long n, int shift,
                                                        const uint32_t* __restrict__ off,
-                                                       int tiles) {
+                                                       int tiles, KeyOrder ord) {
   extern __shared__ unsigned long long s_dyn[];
   U* s_key = reinterpret_cast<U*>(s_dyn);                        // [kPTile]
   uint32_t* s_src = reinterpret_cast<uint32_t*>(s_key + kPTile);  // [kPTile]
@@ -704,7 +715,7 @@ __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin
 #pragma unroll
     for (int e = 0; e < kPI; ++e) {
       const long long i = tb + lb + e * 32 + lane;
-      key[e] = i < n ? kin[i] : (U)0;
+      key[e] = i < n ? ord.load(kin[i]) : (U)0;
     }
 #pragma unroll
     for (int e = 0; e < kPI; ++e) {
@@ -762,7 +773,7 @@ __global__ void __launch_bounds__(kPT) k_digit_scatter(const U* __restrict__ kin
       if (j < valid) {
         const U k = s_key[j];
         at[jj] = s_dst[(unsigned)(k >> shift) & 255u] + j;
-        kout[at[jj]] = k;
+        kout[at[jj]] = ord.store(k);
         if constexpr (VW > 0) {
           const long long src = tb + s_src[j];
 #pragma unroll
@@ -1100,8 +1111,6 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
   uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.hist);
   void* sums = scratch + L.sums;
   const int tiles = ptiles(n);
-  const int ob = resident((const void*)k_order_keys<U>, 256, num_sms, (n + 255) / 256);
-  if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 0);
   const int bh = resident((const void*)k_digit_hist<U>, kPT, num_sms, tiles);
   const size_t sm = scatter_smem<U>();
   const void* scat = vwords == 0   ? (const void*)k_digit_scatter<U, 0>
@@ -1119,14 +1128,13 @@ void radix_sort(U* keys, uint32_t* vals, int vwords, long long n, int kind, bool
     U* kdst = (p & 1) ? keys : ktmp;
     const uint32_t* vsrc = (p & 1) ? vtmp : vals;
     uint32_t* vdst = (p & 1) ? vals : vtmp;
-    k_digit_hist<U><<<bh, kPT, 0, s>>>(ksrc, n, 8 * p, hist, tiles);
+    KeyOrder ord{kind, desc ? 1 : 0, !plain && p == 0, !plain && p == passes - 1};
+    k_digit_hist<U><<<bh, kPT, 0, s>>>(ksrc, n, 8 * p, hist, tiles, ord);
     scan_t<uint32_t>(hist, hist, 256ll * tiles, true, sums, nullptr, num_sms, s);
-    void* args[] = {&ksrc, &kdst, &vsrc, &vdst, &n, nullptr, &hist, const_cast<int*>(&tiles)};
     int shift = 8 * p;
-    args[5] = &shift;
+    void* args[] = {&ksrc, &kdst, &vsrc, &vdst, &n, &shift, &hist, const_cast<int*>(&tiles), &ord};
     cudaLaunchKernel(scat, dim3(bs), dim3(kPT), args, sm, s);
   }
-  if (!plain) k_order_keys<U><<<ob, 256, 0, s>>>(keys, n, kind, desc ? 1 : 0, 1);
 }
 
 // ---- bounds -------------------------------------------------------------------
