@@ -403,34 +403,54 @@ __device__ __forceinline__ bool wait_phase(uint64_t* bar, unsigned parity) {
   return true;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kSThreads + 32, 1)
-    k_scan_single(const T* __restrict__ in, T* out, long long n, int tiles, ScanCtl* ctl,
-                  char* states, int exclusive, int bulk) {
-  typedef typename Acc<T>::type A;
-  constexpr int E = 16 / (int)sizeof(A);  // elements a chunk
-  constexpr int kTileElems = (int)(kSTileBytes / sizeof(A));
+// A lane's first 16-byte chunk of a staged tile: warp w owns elements
+// [w, w + 1) * (tile / warps); chunk c of the lane is 32 * c chunks further.
+template <typename Staged>
+__device__ __forceinline__ Staged* lane_chunk0(Staged* s_data, int warp, int lane) {
+  constexpr int kWarpElems = (int)(kSTileBytes / sizeof(Staged)) / (kSThreads / 32);
+  return s_data + warp * kWarpElems + lane * (16 / (int)sizeof(Staged));
+}
+
+// The single-pass driver the integer scan and the compaction share (run by
+// one persistent block an SM, kSThreads compute threads plus a look-back
+// warp).  Op is the pass's policy:
+//   Staged, Sum        the ring's element type; the tile sums
+//   src                the staged array
+//   on_take(t)         thread 0, when a stage's bulk copy of whole tile t is issued
+//   on_land(k, b, aux) thread 0, when the tile of stage k (first element b)
+//                      has landed, before it is summed; aux[k] is the pass's
+//                      own per-stage word
+//   thread_sum(...)    a compute thread's part of the tile's sum
+//   finish(...)        the compute threads' output of the tile, given the
+//                      sum of everything before the thread's first element
+//   store(...)         after finish and a barrier: the stage's bytes out
+//                      (the scan), or nothing
+template <class Op>
+__device__ __forceinline__ void single_pass(const Op& op, long long n, int tiles, ScanCtl* ctl,
+                                            char* states, int bulk) {
+  typedef typename Op::Staged Staged;
+  typedef typename Op::Sum Sum;
+  constexpr int kTileElems = (int)(kSTileBytes / sizeof(Staged));
   constexpr int kWarps = kSThreads / 32;
-  constexpr int kWarpElems = kTileElems / kWarps;
-  struct Chunk { A e[E]; };
-  static_assert(sizeof(Chunk) == 16, "16-byte chunks");
-  const TileStates<A> st(states, tiles);
+  const TileStates<Sum> st(states, tiles);
   extern __shared__ __align__(128) unsigned char scan_smem[];
   __shared__ __align__(8) uint64_t b_full[kSStages], b_agg[kSStages], b_pre[kSStages];
   __shared__ int s_tile[kSStages];  // the stage's occupant
   __shared__ int s_seen[kSStages];  // the occupant as handed to the look-back warp
-  __shared__ A s_tot[kSStages], s_pre[kSStages], s_wsum[kSStages][kWarps];
+  __shared__ Sum s_tot[kSStages], s_pre[kSStages], s_wsum[kSStages][kWarps];
+  __shared__ unsigned long long s_aux[kSStages];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // a tile is copied in bulk when it is whole and both arrays are 16-byte aligned
+  // a tile is copied in bulk when it is whole and the arrays are 16-byte aligned
   auto whole = [&](int t) { return bulk && (long long)(t + 1) * kTileElems <= n; };
-  auto stage = [&](int k) { return reinterpret_cast<A*>(scan_smem + (size_t)k * kSTileBytes); };
+  auto stage = [&](int k) { return reinterpret_cast<Staged*>(scan_smem + (size_t)k * kSTileBytes); };
   unsigned long long policy = 0;  // read once: evict first
   auto fill = [&](int k) {        // thread 0: the stage's next tile
     const int t = (int)atomicAdd(&ctl->ticket, 1u);
     s_tile[k] = t;
     if (t < tiles && whole(t)) {
       mbar_arrive_tx(&b_full[k], kSTileBytes);
-      bulk_load(stage(k), in + (long long)t * kTileElems, kSTileBytes, &b_full[k], policy);
+      bulk_load(stage(k), op.src + (long long)t * kTileElems, kSTileBytes, &b_full[k], policy);
+      op.on_take(t);
     }
   };
   if (threadIdx.x == 0) {
@@ -452,8 +472,8 @@ __global__ void __launch_bounds__(kSThreads + 32, 1)
       bool failed = !wait_phase(&b_agg[k], (i / kSStages) & 1);
       const int tile = s_seen[k];
       if (tile >= tiles) break;
-      const A tot = s_tot[k];
-      const A prefix = look_back(st, tile, lane, failed);
+      const Sum tot = s_tot[k];
+      const Sum prefix = look_back(st, tile, lane, failed);
       failed = __any_sync(kFull, failed);
       if (lane == 0) {
         if (tile > 0) st.publish(tile, kStInc, prefix + tot);
@@ -480,32 +500,26 @@ __global__ void __launch_bounds__(kSThreads + 32, 1)
       }
       return false;
     }
-    A* s_data = stage(k);
+    Staged* s_data = stage(k);
+    const long long b = (long long)tile * kTileElems;
     bool ok = true;
     if (whole(tile)) {
       ok = wait_phase(&b_full[k], (fullp >> k) & 1u);
       fullp ^= 1u << k;
     } else {
-      const long long b = (long long)tile * kTileElems;
       const long long cnt = n - b < kTileElems ? n - b : kTileElems;
       for (int i = threadIdx.x; i < kTileElems; i += kSThreads)
-        s_data[i] = i < cnt ? (A)in[b + i] : (A)0;
+        s_data[i] = i < cnt ? op.src[b + i] : (Staged)0;
       compute_sync();
     }
-    const Chunk* sc = reinterpret_cast<const Chunk*>(s_data + warp * kWarpElems) + lane;
-    A sum = 0;
-#pragma unroll 4
-    for (int c = 0; c < kSChunks; ++c) {
-      const Chunk x = sc[32 * c];
-#pragma unroll
-      for (int e = 0; e < E; ++e) sum += x.e[e];
-    }
+    if (threadIdx.x == 0) op.on_land(k, b, s_aux);
+    Sum sum = op.thread_sum(s_data, k, b, warp, lane, s_aux);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
     if (lane == 0) s_wsum[k][warp] = sum;
     compute_sync();
     if (threadIdx.x == 0) {
-      A tot = 0;
+      Sum tot = 0;
       for (int w = 0; w < kWarps; ++w) tot += s_wsum[k][w];
       st.publish(tile, tile == 0 ? kStInc : kStAgg, tot);
       if (!ok) {
@@ -527,81 +541,132 @@ __global__ void __launch_bounds__(kSThreads + 32, 1)
     const bool next = reduce((i + 1) % kSStages);  // beside this tile's look-back
     wait_phase(&b_pre[k], (i / kSStages) & 1);      // a timeout is the look-back warp's to report
     const int tile = s_seen[k];
-    A run = s_pre[k];
+    const long long b = (long long)tile * kTileElems;
+    const long long cnt = n - b < kTileElems ? n - b : kTileElems;
+    Sum run = s_pre[k];
     for (int w = 0; w < warp; ++w) run += s_wsum[k][w];
-    A* s_data = stage(k);
-    Chunk* sc = reinterpret_cast<Chunk*>(s_data + warp * kWarpElems) + lane;
-#pragma unroll 4
-    for (int c = 0; c < kSChunks; ++c) {
-      Chunk x = sc[32 * c];
-      A l[E];
-      A acc = 0;
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        l[e] = acc;  // exclusive within the lane's chunk
-        acc += x.e[e];
-      }
-      const A ci = warp_inclusive(acc, lane);
-      const A base = run + ci - acc;
-#pragma unroll
-      for (int e = 0; e < E; ++e) x.e[e] = base + l[e] + (exclusive ? (A)0 : x.e[e]);
-      sc[32 * c] = x;
-      run += __shfl_sync(kFull, ci, 31);
-    }
-    // the scanned tile, before the bulk copy reads it (and this tile's reads
-    // before the stage's next bulk copy writes it)
+    Staged* s_data = stage(k);
+    op.finish(s_data, k, b, run, warp, lane, s_aux);
+    // the tile's shared-memory writes before the bulk copy reads them (and
+    // its reads before the stage's next bulk copy writes it)
     fence_proxy_async();
     compute_sync();
-    const long long b = (long long)tile * kTileElems;
-    if (whole(tile)) {
-      if (threadIdx.x == 0) bulk_store_and_wait_read(out + b, s_data, kSTileBytes);
-    } else {
-      const long long cnt = n - b < kTileElems ? n - b : kTileElems;
-      for (int j = threadIdx.x; j < cnt; j += kSThreads) out[b + j] = (T)s_data[j];
-      compute_sync();  // the stores read the stage before it is refilled
-    }
+    op.store(s_data, b, cnt, whole(tile));
+    compute_sync();  // element stores read the stage before it is refilled
     if (threadIdx.x == 0) fill(k);
     compute_sync();  // s_tile[k]
     more = next;
   }
 }
 
+// The integer scan's policy: sums of the elements; the tile is scanned in
+// shared memory chunk by chunk (a lane's E elements, a warp scan of the chunk
+// totals, the carry of the chunks before) and written back whole.
 template <typename T>
-int single_scan_tiles(long long n) {
-  const long long per = kSTileBytes / sizeof(T);
+struct ScanPass {
+  typedef typename Acc<T>::type Staged;
+  typedef typename Acc<T>::type Sum;
+  static constexpr int E = 16 / (int)sizeof(Staged);
+  struct Chunk { Staged e[E]; };
+  const Staged* src;
+  T* out;
+  int exclusive;
+  __device__ void on_take(int) const {}
+  __device__ void on_land(int, long long, unsigned long long*) const {}
+  __device__ Sum thread_sum(Staged* s_data, int, long long, int warp, int lane,
+                            const unsigned long long*) const {
+    const Chunk* sc = reinterpret_cast<const Chunk*>(lane_chunk0(s_data, warp, lane));
+    Sum sum = 0;
+#pragma unroll 4
+    for (int c = 0; c < kSChunks; ++c) {
+      const Chunk x = sc[32 * c];
+#pragma unroll
+      for (int e = 0; e < E; ++e) sum += x.e[e];
+    }
+    return sum;
+  }
+  __device__ void finish(Staged* s_data, int, long long, Sum run, int warp, int lane,
+                         const unsigned long long*) const {
+    Chunk* sc = reinterpret_cast<Chunk*>(lane_chunk0(s_data, warp, lane));
+#pragma unroll 4
+    for (int c = 0; c < kSChunks; ++c) {
+      Chunk x = sc[32 * c];
+      Sum l[E];
+      Sum acc = 0;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        l[e] = acc;  // exclusive within the lane's chunk
+        acc += x.e[e];
+      }
+      const Sum ci = warp_inclusive(acc, lane);
+      const Sum base = run + ci - acc;
+#pragma unroll
+      for (int e = 0; e < E; ++e) x.e[e] = base + l[e] + (exclusive ? (Sum)0 : x.e[e]);
+      sc[32 * c] = x;
+      run += __shfl_sync(kFull, ci, 31);
+    }
+  }
+  __device__ void store(Staged* s_data, long long b, long long cnt, bool whole) const {
+    if (whole) {
+      if (threadIdx.x == 0) bulk_store_and_wait_read(out + b, s_data, kSTileBytes);
+    } else {
+      for (int j = threadIdx.x; j < cnt; j += kSThreads) out[b + j] = (T)s_data[j];
+    }
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kSThreads + 32, 1)
+    k_scan_single(ScanPass<T> op, long long n, int tiles, ScanCtl* ctl, char* states, int bulk) {
+  single_pass(op, n, tiles, ctl, states, bulk);
+}
+
+template <typename Staged>
+int single_pass_tiles(long long n) {
+  const long long per = kSTileBytes / sizeof(Staged);
   return (int)((n + per - 1) / per);
 }
 
 template <typename T>
 size_t single_scan_bytes(long long n) {
-  return kScanHead + TileStates<typename Acc<T>::type>::bytes(single_scan_tiles<T>(n));
+  typedef typename Acc<T>::type A;
+  return kScanHead + TileStates<A>::bytes(single_pass_tiles<A>(n));
+}
+
+// Clears the scratch's control words and tile states and launches one block
+// an SM of `kernel` (the ring is above the 48 KB of shared memory a launch
+// gets without opting in: set once per device and kernel; a failure shows
+// as the launch's error).
+template <class Op>
+void launch_single_pass(void (*kernel)(Op, long long, int, ScanCtl*, char*, int), const Op& op,
+                        long long n, int bulk, char* scratch, int num_sms, cudaStream_t s) {
+  typedef typename Op::Staged Staged;
+  typedef typename Op::Sum Sum;
+  const size_t smem = (size_t)kSStages * kSTileBytes;
+  static int opted[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !opted[dev]) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess)
+      opted[dev] = 1;
+  }
+  const int tiles = single_pass_tiles<Staged>(n);
+  const int blocks = tiles < num_sms ? tiles : num_sms;
+  cudaMemsetAsync(scratch, 0, kScanHead + TileStates<Sum>::clear_bytes(tiles), s);
+  kernel<<<blocks, kSThreads + 32, smem, s>>>(op, n, tiles, reinterpret_cast<ScanCtl*>(scratch),
+                                              scratch + kScanHead, bulk);
 }
 
 template <typename T>
 void scan_single(const T* in, T* out, long long n, bool exclusive, char* scratch, int num_sms,
                  cudaStream_t s) {
   typedef typename Acc<T>::type A;
-  const size_t smem = (size_t)kSStages * kSTileBytes;
-  // the ring is above the 48 KB of shared memory a launch gets without
-  // opting in; set once per device (a failure shows as the launch's error)
-  static int opted[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !opted[dev]) {
-    if (cudaFuncSetAttribute(k_scan_single<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) == cudaSuccess &&
-        cudaFuncSetAttribute(k_scan_single<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess)
-      opted[dev] = 1;
-  }
-  const int tiles = single_scan_tiles<T>(n);
-  const int blocks = tiles < num_sms ? tiles : num_sms;
+  const ScanPass<T> op{reinterpret_cast<const A*>(in), out, exclusive ? 1 : 0};
   const int bulk = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
-  cudaMemsetAsync(scratch, 0, kScanHead + TileStates<A>::clear_bytes(tiles), s);
-  k_scan_single<T><<<blocks, kSThreads + 32, smem, s>>>(in, out, n, tiles,
-                                                        reinterpret_cast<ScanCtl*>(scratch),
-                                                        scratch + kScanHead, exclusive ? 1 : 0,
-                                                        bulk);
+  launch_single_pass(k_scan_single<T>, op, n, bulk, scratch, num_sms, s);
 }
 
 // ---- radix sort -------------------------------------------------------------
@@ -801,13 +866,10 @@ size_t scatter_smem() {
 // ---- single-pass compaction ------------------------------------------------
 //
 // StreamCompact and Unique in one read of the stencil (or keys), on the
-// single-pass scan's machinery: one persistent block an SM, a ring of 64 KB
-// tiles of the tested array filled by bulk TMA copies, compute warps that
-// count a tile's kept elements as it lands and publish the count, and a warp
-// that finds the tile's offset by the bounded look-back over the tiles
-// before it.  The compute warps then write the tile's kept elements at their
-// places: the key itself (Unique), the value gathered from its array
-// (StreamCompact with an input), or the element's index.
+// single-pass driver: a tile's kept elements are counted as it lands, the
+// look-back warp finds its offset, and the compute warps write the tile's
+// kept elements at their places: the key itself (Unique), the value gathered
+// from its array (StreamCompact with an input), or the element's index.
 //
 // Unique writes in place: a tile's kept keys go below its own start, into
 // tiles that have already loaded (their counts are published before this
@@ -823,195 +885,105 @@ struct CompactOp {
   void* out;
 };
 
-template <typename S>
-__device__ __forceinline__ bool keep_of(const CompactOp& op, S x, S prev, bool first) {
-  if (op.mode == 0) return (int32_t)x != 0;
-  if (op.mode == 1) return __uint_as_float((uint32_t)x) != 0.0f;
-  if (first) return true;
-  if (sizeof(S) == 4 && op.key_kind == 2)
-    return __uint_as_float((uint32_t)x) != __uint_as_float((uint32_t)prev);
-  return x != prev;
-}
-
 // S: the staged element (uint32_t or unsigned long long).  W: 32-bit words a
 // gathered value (StreamCompact with an input: the tile's values are
 // prefetched into L2 by one bulk copy when the tile is taken, and a lane
 // loads its chunks' W x 16 bytes of values four chunks at a time, before
-// their stores), or 0 (Unique's keys, or indices).
+// their stores), or 0 (Unique's keys, or indices).  The key before a tile
+// (Unique) is read by thread 0 when the tile lands, before this tile writes
+// anything, and used by thread 0 alone.
 template <typename S, int W>
-__global__ void __launch_bounds__(kSThreads + 32, 1)
-    k_compact_single(CompactOp op, long long n, int tiles, ScanCtl* ctl, char* states, int bulk,
-                     int vec) {
-  typedef uint32_t A;  // counts: fewer than 2^31 elements
-  constexpr int E = 16 / (int)sizeof(S);
-  constexpr int kTileElems = (int)(kSTileBytes / sizeof(S));
-  constexpr int kWarps = kSThreads / 32;
-  constexpr int kWarpElems = kTileElems / kWarps;
+struct CompactPass {
+  typedef S Staged;
+  typedef uint32_t Sum;  // counts: fewer than 2^31 elements
+  static constexpr int E = 16 / (int)sizeof(S);
+  static constexpr int kTileElems = (int)(kSTileBytes / sizeof(S));
   struct Chunk { S e[E]; };
-  static_assert(sizeof(Chunk) == 16, "16-byte chunks");
-  const TileStates<A> st(states, tiles);
-  const S* in = static_cast<const S*>(op.test);
-  extern __shared__ __align__(128) unsigned char scan_smem[];
-  __shared__ __align__(8) uint64_t b_full[kSStages], b_agg[kSStages], b_pre[kSStages];
-  __shared__ int s_tile[kSStages];
-  __shared__ int s_seen[kSStages];
-  __shared__ A s_tot[kSStages], s_pre[kSStages], s_wsum[kSStages][kWarps];
-  // the key before the tile (Unique), read once by thread 0 while counting,
-  // before this tile writes anything, and used by thread 0 alone
-  __shared__ S s_prev[kSStages];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  auto whole = [&](int t) { return bulk && (long long)(t + 1) * kTileElems <= n; };
-  auto stage = [&](int k) { return reinterpret_cast<S*>(scan_smem + (size_t)k * kSTileBytes); };
-  unsigned long long policy = 0;
-  auto fill = [&](int k) {
-    const int t = (int)atomicAdd(&ctl->ticket, 1u);
-    s_tile[k] = t;
-    if (t < tiles && whole(t)) {
-      mbar_arrive_tx(&b_full[k], kSTileBytes);
-      bulk_load(stage(k), in + (long long)t * kTileElems, kSTileBytes, &b_full[k], policy);
-      if (W > 0 && vec)  // the tile's values, into L2 ahead of the gather
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
-                         op.values + (long long)t * kTileElems * W),
-                     "r"((unsigned)(kTileElems * W * 4))
-                     : "memory");
-    }
-  };
-  if (threadIdx.x == 0) {
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
-    for (int k = 0; k < kSStages; ++k) {
-      mbar_init(&b_full[k], 1);
-      mbar_init(&b_agg[k], 1);
-      mbar_init(&b_pre[k], 1);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    for (int k = 0; k < kSStages; ++k) fill(k);
-  }
-  __syncthreads();
+  int mode, key_kind;
+  const S* src;
+  const uint32_t* values;
+  int vec;  // values 16-byte aligned
+  void* out;
+  long long n;
 
-  if (warp == kWarps) {
-    for (int i = 0;; ++i) {
-      const int k = i % kSStages;
-      bool failed = !wait_phase(&b_agg[k], (i / kSStages) & 1);
-      const int tile = s_seen[k];
-      if (tile >= tiles) break;
-      const A tot = s_tot[k];
-      const A prefix = look_back(st, tile, lane, failed);
-      failed = __any_sync(kFull, failed);
-      if (lane == 0) {
-        if (tile > 0) st.publish(tile, kStInc, prefix + tot);
-        if (failed) atomicOr(&ctl->error, 1u);
-        if (tile == tiles - 1) ctl->total = (unsigned long long)(prefix + tot);
-        s_pre[k] = prefix;
-        mbar_arrive(&b_pre[k]);
-      }
-      __syncwarp();
-    }
-    return;
+  __device__ void on_take(int t) const {
+    if (W > 0 && vec)  // the tile's values, into L2 ahead of the gather
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                       values + (long long)t * kTileElems * W),
+                   "r"((unsigned)(kTileElems * W * 4))
+                   : "memory");
   }
-
-  // kept mask of the lane's chunk c (bit e: element e), from the staged tile
-  auto kept = [&](int k, long long b, int c, Chunk& x) -> unsigned {
-    const S* s_data = stage(k);
-    const int idx0 = warp * kWarpElems + (32 * c + lane) * E;  // tile-local index of element 0
-    x = reinterpret_cast<const Chunk*>(s_data + idx0)[0];
+  __device__ void on_land(int k, long long b, unsigned long long* aux) const {
+    aux[k] = mode == 2 && b > 0 ? (unsigned long long)src[b - 1] : 0ull;
+  }
+  __device__ bool keep(S x, S prev, bool first) const {
+    if (mode == 0) return (int32_t)x != 0;
+    if (mode == 1) return __uint_as_float((uint32_t)x) != 0.0f;
+    if (first) return true;
+    if (sizeof(S) == 4 && key_kind == 2)
+      return __uint_as_float((uint32_t)x) != __uint_as_float((uint32_t)prev);
+    return x != prev;
+  }
+  // kept mask of the lane's chunk c (bit e: element e), and the chunk
+  __device__ unsigned kept(const S* s_data, int k, long long b, int c, int warp, int lane,
+                           const unsigned long long* aux, Chunk& x) const {
+    const S* p = lane_chunk0(s_data, warp, lane) + 32 * c * E;
+    const long long idx0 = p - s_data;  // tile-local index of element 0
+    x = *reinterpret_cast<const Chunk*>(p);
     S prev = 0;
-    if (op.mode == 2 && b + idx0 > 0) prev = idx0 > 0 ? s_data[idx0 - 1] : s_prev[k];
+    if (mode == 2 && b + idx0 > 0) prev = idx0 > 0 ? p[-1] : (S)aux[k];
     unsigned m = 0;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      if (b + idx0 + e < n && keep_of<S>(op, x.e[e], prev, b + idx0 + e == 0)) m |= 1u << e;
+      if (b + idx0 + e < n && keep(x.e[e], prev, b + idx0 + e == 0)) m |= 1u << e;
       prev = x.e[e];
     }
     return m;
-  };
-  unsigned fullp = 0;
-  auto reduce = [&](int k) -> bool {
-    const int tile = s_tile[k];
-    if (tile >= tiles) {
-      if (threadIdx.x == 0) {
-        s_seen[k] = tile;
-        mbar_arrive(&b_agg[k]);
-      }
-      return false;
-    }
-    S* s_data = stage(k);
-    const long long b = (long long)tile * kTileElems;
-    bool ok = true;
-    if (whole(tile)) {
-      ok = wait_phase(&b_full[k], (fullp >> k) & 1u);
-      fullp ^= 1u << k;
-    } else {
-      const long long cnt = n - b < kTileElems ? n - b : kTileElems;
-      for (int i = threadIdx.x; i < kTileElems; i += kSThreads) s_data[i] = i < cnt ? in[b + i] : (S)0;
-      compute_sync();
-    }
-    if (threadIdx.x == 0) s_prev[k] = op.mode == 2 && b > 0 ? in[b - 1] : (S)0;
-    A sum = 0;
+  }
+  __device__ Sum thread_sum(S* s_data, int k, long long b, int warp, int lane,
+                            const unsigned long long* aux) const {
+    Sum sum = 0;
 #pragma unroll 4
     for (int c = 0; c < kSChunks; ++c) {
       Chunk x;
-      sum += __popc(kept(k, b, c, x));
+      sum += __popc(kept(s_data, k, b, c, warp, lane, aux, x));
     }
+    return sum;
+  }
+  // the W words of each of the lane's E elements of chunk c
+  __device__ void load_values(long long wb, int c, int lane, uint4* v) const {
+    if constexpr (W > 0) {
+      const long long i0 = wb + (32 * c + lane) * E;
+      if (vec && i0 + E <= n) {
+        const uint4* src4 = reinterpret_cast<const uint4*>(values + i0 * W);
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
-    if (lane == 0) s_wsum[k][warp] = sum;
-    compute_sync();
-    if (threadIdx.x == 0) {
-      A tot = 0;
-      for (int w = 0; w < kWarps; ++w) tot += s_wsum[k][w];
-      st.publish(tile, tile == 0 ? kStInc : kStAgg, tot);
-      if (!ok) {
-        atomicOr(&ctl->error, 1u);
-        wait_phase(&b_full[k], (fullp >> k) & 1u ^ 1u);
+        for (int q = 0; q < W; ++q) v[q] = __ldcs(src4 + q);
+      } else {
+        uint32_t* u = reinterpret_cast<uint32_t*>(v);
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+#pragma unroll
+          for (int q = 0; q < W; ++q) u[e * W + q] = i0 + e < n ? values[(i0 + e) * W + q] : 0u;
       }
-      s_tot[k] = tot;
-      s_seen[k] = tile;
-      mbar_arrive(&b_agg[k]);
     }
-    return true;
-  };
-
-  bool more = reduce(0);
-  for (int i = 0; more; ++i) {
-    const int k = i % kSStages;
-    const bool next = reduce((i + 1) % kSStages);
-    wait_phase(&b_pre[k], (i / kSStages) & 1);
-    const int tile = s_seen[k];
-    const long long b = (long long)tile * kTileElems;
-    unsigned long long run = s_pre[k];
-    for (int w = 0; w < warp; ++w) run += s_wsum[k][w];
-    const long long wb = b + warp * kWarpElems;  // the warp's first element
+  }
+  __device__ void finish(S* s_data, int k, long long b, Sum run, int warp, int lane,
+                         const unsigned long long* aux) const {
     constexpr int kV = W > 0 ? W : 1;
     constexpr int kG = 4;  // chunks whose values are loaded before any of their stores
-    // the W words of each of the lane's E elements of chunk c
-    auto load_values = [&](int c, uint4* v) {
-      if constexpr (W > 0) {
-        const long long i0 = wb + (32 * c + lane) * E;
-        if (vec && i0 + E <= n) {
-          const uint4* src = reinterpret_cast<const uint4*>(op.values + i0 * W);
-#pragma unroll
-          for (int q = 0; q < W; ++q) v[q] = __ldcs(src + q);
-        } else {
-          uint32_t* u = reinterpret_cast<uint32_t*>(v);
-#pragma unroll
-          for (int e = 0; e < E; ++e)
-#pragma unroll
-            for (int q = 0; q < W; ++q) u[e * W + q] = i0 + e < n ? op.values[(i0 + e) * W + q] : 0u;
-        }
-      }
-    };
+    const long long wb = b + (lane_chunk0(s_data, warp, 0) - s_data);  // the warp's first element
 #pragma unroll 1
     for (int c0 = 0; c0 < kSChunks; c0 += kG) {
       uint4 vals[kG][kV];
 #pragma unroll
-      for (int g = 0; g < kG; ++g) load_values(c0 + g, vals[g]);
+      for (int g = 0; g < kG; ++g) load_values(wb, c0 + g, lane, vals[g]);
 #pragma unroll
       for (int g = 0; g < kG; ++g) {
         const int c = c0 + g;
         Chunk x;
-        const unsigned m = kept(k, b, c, x);
-        const A cm = __popc(m);
-        const A ci = warp_inclusive(cm, lane);
+        const unsigned m = kept(s_data, k, b, c, warp, lane, aux, x);
+        const Sum cm = __popc(m);
+        const Sum ci = warp_inclusive(cm, lane);
         unsigned long long pos = run + ci - cm;
         const long long i0 = wb + (32 * c + lane) * E;
         const uint32_t* u = reinterpret_cast<const uint32_t*>(vals[g]);
@@ -1019,51 +991,42 @@ __global__ void __launch_bounds__(kSThreads + 32, 1)
         for (int e = 0; e < E; ++e)
           if ((m >> e) & 1u) {
             if constexpr (W > 0) {
-              uint32_t* dst = static_cast<uint32_t*>(op.out) + pos * W;
+              uint32_t* dst = static_cast<uint32_t*>(out) + pos * W;
 #pragma unroll
               for (int q = 0; q < W; ++q) dst[q] = u[e * W + q];
-            } else if (op.mode == 2) {
-              static_cast<S*>(op.out)[pos] = x.e[e];
+            } else if (mode == 2) {
+              static_cast<S*>(out)[pos] = x.e[e];
             } else {
-              static_cast<int32_t*>(op.out)[pos] = (int32_t)(i0 + e);
+              static_cast<int32_t*>(out)[pos] = (int32_t)(i0 + e);
             }
             ++pos;
           }
         run += __shfl_sync(kFull, ci, 31);
       }
     }
-    // this tile's reads of the stage before its next bulk copy writes it
-    fence_proxy_async();
-    compute_sync();
-    if (threadIdx.x == 0) fill(k);
-    compute_sync();
-    more = next;
   }
+  __device__ void store(S*, long long, long long, bool) const {}
+};
+
+template <typename S, int W>
+__global__ void __launch_bounds__(kSThreads + 32, 1)
+    k_compact_single(CompactPass<S, W> op, long long n, int tiles, ScanCtl* ctl, char* states,
+                     int bulk) {
+  single_pass(op, n, tiles, ctl, states, bulk);
 }
 
 template <typename S, int W>
-void compact_single_w(const CompactOp& op, long long n, char* scratch, int num_sms,
+void compact_single_w(const CompactOp& a, long long n, char* scratch, int num_sms,
                       cudaStream_t s) {
-  const size_t smem = (size_t)kSStages * kSTileBytes;
-  static int opted[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !opted[dev]) {
-    if (cudaFuncSetAttribute(k_compact_single<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) == cudaSuccess &&
-        cudaFuncSetAttribute(k_compact_single<S, W>,
-                             cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess)
-      opted[dev] = 1;
-  }
-  const long long per = kSTileBytes / sizeof(S);
-  const int tiles = (int)((n + per - 1) / per);
-  const int blocks = tiles < num_sms ? tiles : num_sms;
-  const int bulk = (reinterpret_cast<uintptr_t>(op.test) & 15) == 0;
-  const int vec = (reinterpret_cast<uintptr_t>(op.values) & 15) == 0;
-  cudaMemsetAsync(scratch, 0, kScanHead + TileStates<uint32_t>::clear_bytes(tiles), s);
-  k_compact_single<S, W><<<blocks, kSThreads + 32, smem, s>>>(
-      op, n, tiles, reinterpret_cast<ScanCtl*>(scratch), scratch + kScanHead, bulk, vec);
+  const CompactPass<S, W> op{a.mode,
+                             a.key_kind,
+                             static_cast<const S*>(a.test),
+                             a.values,
+                             (reinterpret_cast<uintptr_t>(a.values) & 15) == 0,
+                             a.out,
+                             n};
+  const int bulk = (reinterpret_cast<uintptr_t>(a.test) & 15) == 0;
+  launch_single_pass(k_compact_single<S, W>, op, n, bulk, scratch, num_sms, s);
 }
 
 // Kept elements into op.out, the count to ctl->total on the device.
