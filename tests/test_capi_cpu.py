@@ -43,6 +43,22 @@ def test_scratch_sizes_grow_with_grid(lib):
     assert big >= 64 ** 3 // 8 + 2 * 8 * 64 * 64
 
 
+@pytest.mark.parametrize("n", [1, 4095, 8192, 8193, 16384, 16385, 1_000_003, 2 ** 31 - 1])
+def test_primitive_scratch_covers_single_pass(lib, n):
+    """The single-pass scan and compaction write a 64-byte control head and a
+    state per 64 KB tile of the staged array: 16 bytes for 64-bit sums (int64
+    scans: 8192 elements a tile), 8 bytes for 32-bit ones (int32 scans and the
+    compaction's counts: 16384 4-byte or 8192 8-byte elements a tile).  The
+    public scratch sizes must cover the largest of these for every n."""
+    def tiles(per):
+        return (n + per - 1) // per
+    assert lib.dax_gb300_scan_scratch_bytes(n) >= 64 + 16 * tiles(8192)
+    assert lib.dax_gb300_scan_scratch_bytes(n) >= 64 + 8 * tiles(16384)
+    assert lib.dax_gb300_compact_scratch_bytes(n, 0) >= 64 + 8 * tiles(16384)
+    assert lib.dax_gb300_compact_scratch_bytes(n, 4) >= 64 + 8 * tiles(16384)
+    assert lib.dax_gb300_compact_scratch_bytes(n, 8) >= 64 + 8 * tiles(8192)
+
+
 def test_bad_extent_rejected(lib):
     g = _desc((0, 0, 0), (-1, 3, 3))
     assert lib.dax_gb300_mc_scratch_bytes(ctypes.byref(g)) == 0
